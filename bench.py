@@ -1,0 +1,303 @@
+"""Benchmark of the render hot path (one JSON line on rank 0).
+
+Workload (default): the large-mesh scene -- Cornell room with a 1,310,720-
+triangle displaced icosphere (GGX, roughness 0.2, F0 0.04) and a 19,800-
+triangle glass sphere (IOR 1.5) -- rendered at 1024 x 1024, 64 spp, max depth
+8 (NIters 7, no Russian roulette), Sobol sampling, FP32 accumulation.  One
+step is one full render.
+
+* value: Msamples/s of the integration + reduction kernels, timed with CUDA
+  events on the renderer's stream (path_render_stats.kernel_ms), scene
+  resident in HBM, image written to device memory.  L2 is flushed (512 MB
+  write) before every timed step.
+* e2e: the same metric through the C ABI call a user makes (path_render) with
+  host buffers: every step re-copies the scene's device arrays from pinned
+  host memory and copies the image back to the host, all inside the timed
+  wall-clock region.
+* roofline: algorithmic bytes of the render kernel (wide nodes x 80 B +
+  triangles tested x 48 B + rays x 96 B of shading data, counted by a
+  counting run of the same render) over the kernel's event time, against the
+  measured HBM copy bandwidth.
+* cpu_baseline: the CPU oracle (a restatement of the reference's CPU path:
+  OpenMP over WorkDivision blocks) on a band of image rows of the same
+  workload, all host threads.
+
+``--impl reference`` times that CPU restatement alone (the reference itself
+cannot be built on this image).  N > 1 runs independent
+replicas, one per GPU (the render has no data-path exchange).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Msamples/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name):
+    from path_gb300 import scenes
+    if name == "large_mesh":
+        scene = scenes.large_mesh_room(subdivisions=8)
+        w = h = 1024
+        spp, depth = 64, 8
+        desc = ("large-mesh room: 1,310,720-tri displaced icosphere (GGX a=0.2 F0=0.04) + "
+                "19,800-tri glass sphere (IOR 1.5), 1024x1024, 64 spp, depth 8")
+    else:
+        scene = scenes.cornell_box()
+        w = h = 256
+        spp, depth = 16, 5
+        desc = "Cornell box: 36 triangles, 256x256, 16 spp, depth 5"
+    return scene, w, h, spp, depth, desc
+
+
+def cpu_sample(scene, settings, spp, w, h, f2w, rows, threads):
+    """The oracle on a band of rows; returns (samples, seconds)."""
+    from oracle import oracle_lib as ol
+    arr = ol.SceneArrays(scene.export())
+    s = ol.settings_from(settings, reduce_order=0, n_threads=threads)
+    r0 = h // 2 - rows // 2
+    _, secs = ol.render(arr, s, spp, w, h, f2w, rows=(r0, r0 + rows))
+    return rows * w * spp, secs
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from path_gb300 import scenes
+    scene, w, h, spp, depth, desc = make_workload(args.workload)
+    settings = scenes.path_settings(depth, "binary")
+    f2w = scenes.cornell_camera(w, h)
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows
+    for _ in range(args.warmup):
+        cpu_sample(scene, settings, spp, w, h, f2w, rows, threads)
+    total_s, total_samples = 0.0, 0
+    for _ in range(args.steps):
+        n, secs = cpu_sample(scene, settings, spp, w, h, f2w, rows, threads)
+        total_s += secs
+        total_samples += n
+    value = total_samples / total_s / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": desc, "sample": f"{rows} rows x {w} px x {spp} spp per step"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows of {w} px at {spp} spp per step (oracle: CPU "
+                                   "restatement of the reference CPU path)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large_mesh", choices=["large_mesh", "cornell"])
+    ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
+    ap.add_argument("--cpu-rows", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+
+    from path_gb300 import api, build, scenes
+    build.build()
+    scene, w, h, spp, depth, desc = make_workload(args.workload)
+    settings = scenes.path_settings(depth, args.traversal)
+    f2w = scenes.cornell_camera(w, h)
+    spec = api.SquareImage(w, h, f2w)
+    r = api.Renderer()
+    dev_out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    t0 = time.time()
+    r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, settings)
+    setup_s = time.time() - t0
+    st0 = r.stats()
+
+    # counting run: rays, wide nodes and triangles of one render
+    cs = settings.copy()
+    cs.count_work = 1
+    r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, cs)
+    counts = r.stats()
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, settings)
+    kernel_ms, launches = [], 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, settings)
+            st = r.stats()
+            kernel_ms.append(st["kernel_ms"])
+            launches += st["gpu_launches"]
+        torch.cuda.synchronize()
+        # end to end through the C ABI with host buffers
+        host_out = np.zeros((h, w, 3), np.float32)
+        es = settings.copy()
+        es.upload_scene_every_render = 1
+        for _ in range(2):
+            r.render(api.ExecutionModel.GPU, spec, host_out, scene, spp, es)
+        e2e_s, h2d, d2h = [], 0, 0
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r.render(api.ExecutionModel.GPU, spec, host_out, scene, spp, es)
+            e2e_s.append(time.perf_counter() - t)
+            st = r.stats()
+            h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+            launches += st["gpu_launches"]
+    torch.cuda.synchronize()
+    total_ms = sum(kernel_ms)
+    if world > 1:
+        t = torch.tensor([total_ms, sum(e2e_s)], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+    else:
+        e2e_total = sum(e2e_s)
+    samples = w * h * spp
+    value = world * samples * args.steps / (total_ms / 1e3) / 1e6
+    e2e_value = world * samples * args.steps / e2e_total / 1e6
+
+    peak, peak_kind = _peaks()
+    mean_ms = total_ms / args.steps
+    alg_bytes = counts["nodes_visited"] * 80 + counts["triangles_tested"] * 48 + \
+        counts["rays_traced"] * 96
+    achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": desc, "triangles": int(scene.sizes()["triangles"]),
+            "width": w, "height": h, "spp": spp,
+            "max_depth": depth, "traversal": args.traversal,
+            "l2": "flushed (512 MB write) before every timed step",
+            "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": int(alg_bytes)},
+        "mrays_per_s": counts["rays_traced"] / (mean_ms / 1e3) / 1e6,
+        "work_counts": {"rays": counts["rays_traced"], "wide_nodes": counts["nodes_visited"],
+                        "triangles": counts["triangles_tested"]},
+        "setup_s": setup_s, "bvh_build_s": st0["bvh_build_seconds"],
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n, secs = cpu_sample(scene, settings, spp, w, h, f2w, args.cpu_rows, threads)
+        line["cpu_baseline"] = {
+            "value": n / secs / 1e6, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{args.cpu_rows} rows of {w} px at {spp} spp (oracle: CPU restatement "
+                      f"of the reference CPU path, {threads} threads)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

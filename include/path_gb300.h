@@ -1,0 +1,288 @@
+/*
+ * path_gb300: C ABI of the GB300-native render hot path.
+ *
+ * The entry points below replace the reference's render API for the path
+ * tracer (rgreenblatt/path).  All types are plain C: pointers, sizes and POD
+ * structs; no C++ or torch types cross the boundary.  Every function returns
+ * a path_status; on failure path_last_error() describes the cause.  Calls on
+ * one renderer are synchronous and a renderer is not thread safe (as with
+ * render::Renderer); use one renderer per host thread.
+ */
+#ifndef PATH_GB300_H
+#define PATH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PATH_OK = 0,
+  PATH_ERR_ARGUMENT = 1,     /* bad pointer, size or setting value */
+  PATH_ERR_SCENE_PARSE = 2,  /* XML / OBJ / MTL / YAML could not be read */
+  PATH_ERR_OOM = 3,          /* device or host allocation failed */
+  PATH_ERR_DEVICE_TIMEOUT = 4, /* a kernel's bounded wait or stack check
+                                  gave up; the device status word says where */
+  PATH_ERR_UNSUPPORTED = 5,  /* setting combination not built */
+  PATH_ERR_CUDA = 6,         /* CUDA runtime error */
+  PATH_ERR_IO = 7            /* file could not be opened or written */
+} path_status;
+
+/* include/execution_model/execution_model.h:3-6.  This library implements
+ * the GPU execution model; PATH_EXEC_CPU is rejected with
+ * PATH_ERR_UNSUPPORTED (there is no CPU fallback in the product). */
+typedef enum { PATH_EXEC_CPU = 0, PATH_EXEC_GPU = 1 } path_exec_model;
+
+/* include/bsdf/union_bsdf.h:17-24 (+ GGX, which the reference lacks) */
+typedef enum {
+  PATH_BSDF_DIFFUSE = 0,
+  PATH_BSDF_GLOSSY = 1,
+  PATH_BSDF_DIFFUSE_GLOSSY = 2,
+  PATH_BSDF_DIFFUSE_MIRROR = 3,
+  PATH_BSDF_MIRROR = 4,
+  PATH_BSDF_DIELECTRIC_REFRACTIVE = 5,
+  PATH_BSDF_GGX = 6
+} path_bsdf_type;
+
+/* scene::Material = bsdf::Material<UnionBSDF> (include/scene/material.h),
+ * 64 bytes.  Field use per type:
+ *   DIFFUSE: diffuse.  GLOSSY: specular, shininess.  MIRROR: specular.
+ *   DIFFUSE_GLOSSY / DIFFUSE_MIRROR: diffuse, specular, shininess,
+ *     diffuse_weight, glossy_weight (include/bsdf/combined.h weights).
+ *   DIELECTRIC_REFRACTIVE: specular, ior.  GGX: specular = F0, roughness. */
+typedef struct {
+  uint32_t type;
+  float diffuse[3];
+  float specular[3];
+  float shininess;
+  float ior;
+  float diffuse_weight;
+  float glossy_weight;
+  float roughness;
+  float emission[3];
+  float pad;
+} path_material;
+
+/* kernel::WorkDivisionSettings (include/kernel/work_division_settings.h) */
+typedef struct {
+  uint32_t block_size;
+  uint32_t target_x_block_size;
+  uint32_t force_target_samples;
+  uint32_t forced_target_samples_per_thread;
+  uint32_t base_num_threads;
+  float samples_per_thread_scaling_power;
+  uint32_t max_samples_per_thread;
+} path_work_division_settings;
+
+typedef enum { PATH_KERNEL_MEGA = 0, PATH_KERNEL_STREAMING = 1 } path_kernel_approach;
+typedef enum { PATH_LIGHT_RANDOM_TRIANGLE = 0, PATH_LIGHT_NONE = 1 } path_light_sampler;
+typedef enum { PATH_DIR_BSDF = 0, PATH_DIR_UNIFORM = 1 } path_dir_sampler;
+typedef enum {
+  PATH_TERM_CONSTANT = 0,
+  PATH_TERM_N_ITERS = 1,
+  PATH_TERM_MULTIPLIER_FUNC = 2,
+  PATH_TERM_NORMALIZE = 3
+} path_term_prob;
+typedef enum { PATH_RNG_SOBEL = 0, PATH_RNG_UNIFORM = 1 } path_rng;
+typedef enum {
+  PATH_TRAVERSAL_BINARY = 0, /* the reference's binary SBVH and traversal order */
+  PATH_TRAVERSAL_WIDE8 = 1   /* compressed 8-wide quantised BVH */
+} path_traversal;
+
+/* render::Settings (include/render/settings.h:27-70), flattened.  The last
+ * block holds the GB300-specific knobs with no reference counterpart. */
+typedef struct {
+  uint32_t kernel_approach; /* path_kernel_approach */
+  uint32_t max_blocks_per_launch_gpu;
+  uint32_t max_blocks_per_launch_cpu;
+  path_work_division_settings render_work_division;
+  path_work_division_settings reduce_work_division;
+  /* accel SBVH (include/intersect/accel/sbvh/settings.h) */
+  float overlap_threshold;
+  uint32_t use_spatial_splits;
+  float traversal_per_intersect_cost;
+  uint32_t target_objects;
+  /* light sampler */
+  uint32_t light_sampler;
+  uint32_t binary_search_threshold;
+  /* direction sampler */
+  uint32_t dir_sampler;
+  /* termination probability */
+  uint32_t term_prob;
+  float term_prob_prob;      /* Constant */
+  uint32_t term_prob_iters;  /* NIters */
+  float term_prob_exp;       /* MultiplierFunc */
+  float term_prob_min_prob;  /* MultiplierFunc, Normalize */
+  /* rng */
+  uint32_t rng;
+  uint32_t max_sample_size;
+  /* integrate::RenderingEquationSettings */
+  uint32_t back_cull_emission;
+  /* GB300 knobs */
+  uint32_t traversal;        /* path_traversal */
+  uint32_t persistent_ctas_per_sm; /* 0 = one launch over all blocks */
+  uint32_t count_work;       /* 1: count rays / nodes / triangles (slower) */
+  uint32_t upload_scene_every_render; /* 1: re-copy the cached scene arrays
+                                         host -> device on every render */
+  uint32_t reserved[4];
+} path_settings;
+
+typedef enum {
+  PATH_SAMPLE_SQUARE_IMAGE = 0,
+  PATH_SAMPLE_INITIAL_RAYS = 1
+} path_sample_spec_type;
+
+/* render::SampleSpec (include/render/renderer.h:19-41) */
+typedef struct {
+  uint32_t type;          /* path_sample_spec_type */
+  uint32_t x_dim, y_dim;  /* SQUARE_IMAGE */
+  float film_to_world[12]; /* 3x4 row-major affine, SQUARE_IMAGE */
+  const float *rays;      /* INITIAL_RAYS: [n_rays][6] origin, direction */
+  uint32_t n_rays;
+} path_sample_spec;
+
+typedef enum {
+  PATH_OUTPUT_BGRA = 0,
+  PATH_OUTPUT_FLOAT_RGB = 1
+} path_output_type;
+
+/* render::Output (include/render/renderer.h:13-17,37-38).  data is host
+ * memory unless on_device is set, in which case it is a device pointer and
+ * the final copy to the host is skipped. */
+typedef struct {
+  uint32_t type;      /* path_output_type */
+  void *data;         /* BGRA: 4 bytes/pixel (B,G,R,0); FLOAT_RGB: 3 floats */
+  uint32_t on_device;
+} path_output;
+
+typedef struct path_scene path_scene;
+typedef struct path_renderer path_renderer;
+
+/* Statistics from the last render (GB300 addition). */
+typedef struct {
+  double seconds;            /* same span as the reference's returned time */
+  double kernel_ms;          /* CUDA-event time of the integration kernels */
+  double bvh_build_seconds;  /* host SBVH build (excluded from seconds) */
+  uint64_t rays_traced;      /* extension + shadow rays (counting runs only) */
+  uint64_t nodes_visited;
+  uint64_t triangles_tested;
+  uint32_t gpu_launches;     /* kernels this library launched for the render */
+  uint32_t device_status;    /* 0, or the first in-kernel error code */
+  uint32_t num_bvh_nodes;
+  uint32_t num_wide_nodes;
+  uint64_t h2d_bytes;        /* host -> device bytes copied by this render */
+  uint64_t d2h_bytes;        /* device -> host bytes copied by this render */
+} path_render_stats;
+
+/* ---- errors ---- */
+/* message of the last failed call on this thread (empty string if none) */
+const char *path_last_error(void);
+
+/* ---- settings ---- */
+/* defaults of render::Settings{} (include/render/settings.h:27-45) */
+path_status path_settings_default(path_settings *out);
+/* reads a render settings YAML file in the reference's schema
+ * (src/render/config_io.cpp:14-35, configs/benchmark.yaml) */
+path_status path_settings_load_yaml(const char *path, path_settings *out);
+
+/* ---- scenes ---- */
+/* scene::TriangleConstructor (include/scene/triangle_constructor.h:8-19) */
+path_status path_scene_create(path_scene **out);
+void path_scene_destroy(path_scene *scene);
+path_status path_scene_add_material(path_scene *scene,
+                                    const path_material *material,
+                                    uint32_t *material_idx);
+/* triangles: [n][3][3]; normals: [n][3][3] vertex normals or NULL for the
+ * face normal (scenefile_loader.cpp:280-284); material_idx per triangle.
+ * Adds one mesh with an identity instance; emissive clusters follow
+ * scene::TriangleConstructor::add_triangle. */
+path_status path_scene_add_mesh(path_scene *scene, const float *triangles,
+                                const float *normals,
+                                const uint32_t *material_idx, uint32_t n,
+                                const float *object_to_world /* 3x4 or NULL */);
+/* ScenefileLoader::load_scene (src/scene/scenefile_compat/scenefile_loader.cpp
+ * :23-62): CS123 XML scene + OBJ/MTL meshes.  film_to_world receives the
+ * camera transform for the given aspect ratio (3x4 row-major). */
+path_status path_scene_load_xml(const char *path, float width_height_ratio,
+                                path_scene **out, float *film_to_world);
+/* scene::get_camera_transform (src/scene/camera.cpp:4-27) */
+path_status path_camera_transform(const float *look, const float *up,
+                                  const float *pos, float height_angle_deg,
+                                  float width_height_ratio,
+                                  float *film_to_world);
+/* sizes: [n_triangles, n_meshes, n_instances, n_clusters, n_materials] */
+path_status path_scene_sizes(const path_scene *scene, uint32_t *sizes);
+/* exports the scene in the reference's scene::Scene arrays (see oracle) */
+path_status path_scene_export(const path_scene *scene, float *triangles,
+                              float *normals, uint32_t *tri_material,
+                              uint32_t *mesh_ends,
+                              uint32_t *cluster_ends_per_mesh,
+                              float *instance_xforms, uint32_t *instance_mesh,
+                              uint32_t *clusters, path_material *materials);
+
+/* ---- renderer ---- */
+/* render::Renderer (include/render/renderer.h:43-70) */
+path_status path_renderer_create(path_renderer **out);
+void path_renderer_destroy(path_renderer *renderer);
+/* Renderer::render (include/render/renderer.h:51-54).  seconds receives the
+ * time from after scene / accel setup through the output copy
+ * (include/render/detail/general_render_impl.h:174-241). */
+path_status path_render(path_renderer *renderer, uint32_t exec_model,
+                        const path_sample_spec *sample_spec,
+                        const path_output *output, const path_scene *scene,
+                        uint32_t samples_per, const path_settings *settings,
+                        uint32_t show_progress, double *seconds);
+path_status path_renderer_stats(const path_renderer *renderer,
+                                path_render_stats *out);
+
+/* ---- accel / intersection (TriangleAccel concept,
+ * include/intersect/accel/accel.h:35-77) ---- */
+/* builds the SBVH of a world-space triangle soup (Generator::gen,
+ * src/intersect/accel/sbvh/detail/generator.cu:17-66).  sizes receives
+ * [n_nodes, n_extra_idxs]; the arrays may be NULL to query sizes. */
+path_status path_sbvh_build(const float *triangles, uint32_t n,
+                            const path_settings *settings, uint32_t *sizes,
+                            uint32_t *node_words, float *node_aabbs,
+                            uint32_t *extra_idxs, uint32_t *permutation);
+/* closest hit of each ray against the triangle soup on the GPU
+ * (AccelRef::intersect_objects with Triangle::intersect): idx = original
+ * triangle index or -1, t = distance (NaN when none).  rays/idx/t are host
+ * pointers. */
+path_status path_intersect(path_renderer *renderer, const float *triangles,
+                           uint32_t n_triangles, const float *rays,
+                           uint32_t n_rays, const path_settings *settings,
+                           int32_t *idx_out, float *t_out);
+
+/* ---- RNG ---- */
+/* Sobol table vals[i * dimension_bound + d] on the GPU
+ * (SobelSequenceGen::gen, src/rng/sobel/sobel.cu:21-93); out is host. */
+path_status path_sobol_table(uint32_t dimension_bound, uint32_t count,
+                             float *out);
+/* the same table produced by cuRAND's own device generator
+ * (curand_init + curand_uniform on curandStateScrambledSobol32), used to
+ * pin the register-XOR generator bit for bit. */
+path_status path_sobol_table_curand(uint32_t dimension_bound, uint32_t count,
+                                    float *out);
+
+/* ---- diagnostics ---- */
+/* evaluates the kernels' transcendental functions on the GPU:
+ * fn 0 sin, 1 cos, 2 asin, 3 acos, 4 pow(x, y); host arrays of n */
+path_status path_debug_pmath(uint32_t fn, const float *x, const float *y,
+                             float *out, uint32_t n);
+/* kernel::WorkDivision (src/kernel/work_division.cpp:12-69): out receives
+ * [block_size, base_samples_per_thread, n_threads_per_unit_extra,
+ *  sample_block_size, x_block_size, y_block_size, num_sample_blocks,
+ *  num_x_blocks, num_y_blocks, x_dim, y_dim] */
+path_status path_work_division(const path_work_division_settings *settings,
+                               uint32_t samples_per, uint32_t x_dim,
+                               uint32_t y_dim, uint32_t *out);
+/* number of GPUs visible and the library's build string */
+const char *path_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PATH_GB300_H */

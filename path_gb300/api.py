@@ -1,0 +1,304 @@
+"""Python mirror of the reference's render API, on top of the C ABI.
+
+Names follow the reference: ``Renderer.render`` (include/render/renderer.h:
+43-70), ``RendererFromFiles`` (include/render/renderer_from_files.h:22-43),
+``Settings`` (include/render/settings.h), ``TriangleConstructor``-style scene
+building (include/scene/triangle_constructor.h) and ``ExecutionModel``.
+Errors are raised as ``capi.PathError`` carrying the C status code.
+"""
+
+import ctypes
+import enum
+
+import numpy as np
+
+from . import capi
+
+
+class ExecutionModel(enum.IntEnum):
+    CPU = capi.EXEC_CPU
+    GPU = capi.EXEC_GPU
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _uptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+class Settings:
+    """render::Settings as a flat C struct with attribute access."""
+
+    def __init__(self, raw=None):
+        self.raw = capi.PathSettings()
+        if raw is not None:
+            ctypes.memmove(ctypes.byref(self.raw), ctypes.byref(raw), ctypes.sizeof(raw))
+        else:
+            capi.check(capi.load().path_settings_default(ctypes.byref(self.raw)))
+
+    @classmethod
+    def from_yaml(cls, path):
+        s = cls()
+        capi.check(capi.load().path_settings_load_yaml(str(path).encode(), ctypes.byref(s.raw)))
+        return s
+
+    def copy(self):
+        return Settings(self.raw)
+
+    def __getattr__(self, name):
+        if name == "raw":
+            raise AttributeError(name)
+        return getattr(self.raw, name)
+
+    def __setattr__(self, name, value):
+        if name == "raw":
+            object.__setattr__(self, name, value)
+        else:
+            setattr(self.raw, name, value)
+
+    def set_term_prob(self, kind, **kw):
+        self.raw.term_prob = capi.TERM[kind]
+        for k, v in kw.items():
+            setattr(self.raw, {"prob": "term_prob_prob", "iters": "term_prob_iters",
+                               "exp": "term_prob_exp", "min_prob": "term_prob_min_prob"}[k], v)
+        return self
+
+
+def material(kind, diffuse=(0, 0, 0), specular=(0, 0, 0), emission=(0, 0, 0), shininess=0.0,
+             ior=1.0, diffuse_weight=0.0, glossy_weight=0.0, roughness=0.0):
+    m = capi.PathMaterial()
+    m.type = capi.BSDF[kind]
+    m.diffuse[:] = [float(x) for x in diffuse]
+    m.specular[:] = [float(x) for x in specular]
+    m.emission[:] = [float(x) for x in emission]
+    m.shininess = shininess
+    m.ior = ior
+    m.diffuse_weight = diffuse_weight
+    m.glossy_weight = glossy_weight
+    m.roughness = roughness
+    return m
+
+
+class Scene:
+    """scene::Scene built like scene::TriangleConstructor, or loaded from XML."""
+
+    def __init__(self, handle=None):
+        lib = capi.load()
+        if handle is None:
+            handle = ctypes.c_void_p()
+            capi.check(lib.path_scene_create(ctypes.byref(handle)))
+        self._h = handle
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and capi._lib is not None:
+            capi._lib.path_scene_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def add_material(self, m):
+        idx = ctypes.c_uint32()
+        capi.check(capi.load().path_scene_add_material(self._h, ctypes.byref(m), ctypes.byref(idx)))
+        return idx.value
+
+    def add_mesh(self, triangles, material_idx, normals=None, object_to_world=None):
+        tris = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+        mats = np.ascontiguousarray(material_idx, dtype=np.uint32).reshape(-1)
+        if mats.size == 1 and tris.shape[0] > 1:
+            mats = np.full(tris.shape[0], mats[0], dtype=np.uint32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
+        xf = None if object_to_world is None else np.ascontiguousarray(object_to_world, dtype=np.float32).reshape(12)
+        capi.check(capi.load().path_scene_add_mesh(
+            self._h, _fptr(tris), None if nrm is None else _fptr(nrm), _uptr(mats),
+            tris.shape[0], None if xf is None else _fptr(xf)))
+
+    def sizes(self):
+        s = (ctypes.c_uint32 * 5)()
+        capi.check(capi.load().path_scene_sizes(self._h, s))
+        return dict(zip(["triangles", "meshes", "instances", "clusters", "materials"], list(s)))
+
+    def export(self):
+        """Arrays in the reference's scene::Scene layout (for the oracle)."""
+        z = self.sizes()
+        n, m, k, c, nm = (z["triangles"], z["meshes"], z["instances"], z["clusters"],
+                          z["materials"])
+        out = {
+            "triangles": np.zeros((n, 9), np.float32), "normals": np.zeros((n, 9), np.float32),
+            "tri_material": np.zeros(n, np.uint32), "mesh_ends": np.zeros(m, np.uint32),
+            "cluster_ends_per_mesh": np.zeros(m, np.uint32),
+            "instance_xforms": np.zeros((k, 12), np.float32),
+            "instance_mesh": np.zeros(k, np.uint32), "clusters": np.zeros((c, 3), np.uint32),
+            "materials": (capi.PathMaterial * max(nm, 1))(),
+        }
+        capi.check(capi.load().path_scene_export(
+            self._h, _fptr(out["triangles"]), _fptr(out["normals"]), _uptr(out["tri_material"]),
+            _uptr(out["mesh_ends"]), _uptr(out["cluster_ends_per_mesh"]),
+            _fptr(out["instance_xforms"]), _uptr(out["instance_mesh"]), _uptr(out["clusters"]),
+            out["materials"]))
+        out["n_materials"] = nm
+        return out
+
+    @classmethod
+    def load_xml(cls, path, width_height_ratio):
+        h = ctypes.c_void_p()
+        f2w = np.zeros(12, np.float32)
+        capi.check(capi.load().path_scene_load_xml(str(path).encode(), width_height_ratio,
+                                                   ctypes.byref(h), _fptr(f2w)))
+        return cls(h), f2w
+
+
+def camera_transform(look, up, pos, height_angle_deg, width_height_ratio):
+    """scene::get_camera_transform (src/scene/camera.cpp:4-27): 3x4 film_to_world."""
+    out = np.zeros(12, np.float32)
+    arr = [np.asarray(v, np.float32) for v in (look, up, pos)]
+    capi.check(capi.load().path_camera_transform(_fptr(arr[0]), _fptr(arr[1]), _fptr(arr[2]),
+                                                 height_angle_deg, width_height_ratio, _fptr(out)))
+    return out
+
+
+class SquareImage:
+    """render::SquareImageSpec."""
+
+    def __init__(self, x_dim, y_dim, film_to_world):
+        self.x_dim = int(x_dim)
+        self.y_dim = int(y_dim)
+        self.film_to_world = np.asarray(film_to_world, np.float32).reshape(12)
+
+    def to_c(self):
+        s = capi.SampleSpec()
+        s.type = capi.SAMPLE_SQUARE_IMAGE
+        s.x_dim = self.x_dim
+        s.y_dim = self.y_dim
+        s.film_to_world[:] = [float(v) for v in self.film_to_world]
+        return s
+
+
+class Renderer:
+    """render::Renderer: caches the scene's accel and device buffers."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        capi.check(capi.load().path_renderer_create(ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and capi._lib is not None:
+            capi._lib.path_renderer_destroy(h)
+            self._h = None
+
+    def render(self, execution_model, sample_spec, output, scene, samples_per, settings,
+               show_progress=False):
+        """Render into ``output``; returns the reference's timed seconds.
+
+        output: numpy float32 [H, W, 3] (FloatRGB) or uint8 [H, W, 4] (BGRA) in
+        host memory, or a torch CUDA tensor of the same shape (device output).
+        """
+        o = capi.Output()
+        dtype = getattr(output, "dtype", None)
+        is_torch = hasattr(output, "data_ptr")
+        if is_torch:
+            import torch
+            if not output.is_contiguous():
+                raise ValueError("output tensor must be contiguous")
+            o.type = capi.OUTPUT_BGRA if output.dtype == torch.uint8 else capi.OUTPUT_FLOAT_RGB
+            o.data = output.data_ptr()
+            o.on_device = 1 if output.is_cuda else 0
+        else:
+            if not output.flags["C_CONTIGUOUS"]:
+                raise ValueError("output array must be C contiguous")
+            o.type = capi.OUTPUT_BGRA if dtype == np.uint8 else capi.OUTPUT_FLOAT_RGB
+            o.data = output.ctypes.data
+            o.on_device = 0
+        spec = sample_spec.to_c()
+        secs = ctypes.c_double()
+        capi.check(capi.load().path_render(self._h, int(execution_model), ctypes.byref(spec),
+                                           ctypes.byref(o), scene.handle, int(samples_per),
+                                           ctypes.byref(settings.raw), int(show_progress),
+                                           ctypes.byref(secs)))
+        return secs.value
+
+    def stats(self):
+        s = capi.RenderStats()
+        capi.check(capi.load().path_renderer_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in capi.RenderStats._fields_}
+
+    def intersect(self, triangles, rays, settings):
+        """Closest hit on the GPU: (idx int32, t float32); idx -1 = miss."""
+        tris = np.ascontiguousarray(triangles, np.float32).reshape(-1, 9)
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        idx = np.zeros(r.shape[0], np.int32)
+        t = np.zeros(r.shape[0], np.float32)
+        capi.check(capi.load().path_intersect(
+            self._h, _fptr(tris), tris.shape[0], _fptr(r), r.shape[0], ctypes.byref(settings.raw),
+            idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _fptr(t)))
+        return idx, t
+
+
+class RendererFromFiles:
+    """render::RendererFromFiles: scene file + YAML config + render."""
+
+    def __init__(self):
+        self.renderer = Renderer()
+        self.settings = Settings()
+        self.scene = None
+        self.film_to_world = None
+
+    def load_scene(self, path, width_height_ratio, quiet=True):
+        self.scene, self.film_to_world = Scene.load_xml(path, width_height_ratio)
+
+    def load_config(self, path):
+        self.settings = Settings.from_yaml(path)
+
+    def render(self, execution_model, x_dim, y_dim, output, samples_per, show_progress=False):
+        return self.renderer.render(execution_model, SquareImage(x_dim, y_dim, self.film_to_world),
+                                    output, self.scene, samples_per, self.settings, show_progress)
+
+
+def sbvh_build(triangles, settings):
+    """Binary SBVH of a triangle soup: dict of node words, boxes, extra idxs, permutation."""
+    tris = np.ascontiguousarray(triangles, np.float32).reshape(-1, 9)
+    n = tris.shape[0]
+    sizes = (ctypes.c_uint32 * 2)()
+    lib = capi.load()
+    capi.check(lib.path_sbvh_build(_fptr(tris), n, ctypes.byref(settings.raw), sizes, None, None,
+                                   None, None))
+    words = np.zeros((sizes[0], 2), np.uint32)
+    boxes = np.zeros((sizes[0], 6), np.float32)
+    extra = np.zeros(max(sizes[1], 1), np.uint32)
+    perm = np.zeros(max(n, 1), np.uint32)
+    capi.check(lib.path_sbvh_build(_fptr(tris), n, ctypes.byref(settings.raw), sizes,
+                                   _uptr(words), _fptr(boxes), _uptr(extra), _uptr(perm)))
+    return {"node_words": words, "node_aabbs": boxes, "extra_idxs": extra[:sizes[1]],
+            "permutation": perm[:n]}
+
+
+def sobol_table(dimension_bound, count, use_curand=False):
+    out = np.zeros(dimension_bound * count, np.float32)
+    fn = capi.load().path_sobol_table_curand if use_curand else capi.load().path_sobol_table
+    capi.check(fn(dimension_bound, count, _fptr(out)))
+    return out.reshape(count, dimension_bound)
+
+
+def debug_pmath(fn, x, y=None):
+    x = np.ascontiguousarray(x, np.float32)
+    yy = None if y is None else np.ascontiguousarray(y, np.float32)
+    out = np.zeros_like(x)
+    capi.check(capi.load().path_debug_pmath(fn, _fptr(x), None if yy is None else _fptr(yy),
+                                            _fptr(out), x.size))
+    return out
+
+
+def work_division(wd_settings, samples_per, x_dim, y_dim):
+    out = (ctypes.c_uint32 * 11)()
+    capi.check(capi.load().path_work_division(ctypes.byref(wd_settings), samples_per, x_dim,
+                                              y_dim, out))
+    names = ["block_size", "base_samples_per_thread", "n_threads_per_unit_extra",
+             "sample_block_size", "x_block_size", "y_block_size", "num_sample_blocks",
+             "num_x_blocks", "num_y_blocks", "x_dim", "y_dim"]
+    return dict(zip(names, list(out)))

@@ -1,0 +1,71 @@
+// Data layout of the render path in device memory.
+//
+//  * BVH-order triangles: 3 x float4 = 48 B, (v0.xyz, e1.x) (e1.yz, e2.xy)
+//    (e2.z, -, -, -) with e1 = v1 - v0, e2 = v2 - v0 precomputed (the same
+//    subtraction Triangle::intersect performs, so the bits are unchanged).
+//  * shading data: 3 x float4 = 48 B, the three vertex normals and the
+//    material index (scene::TriangleData, include/scene/triangle_data.h).
+//  * binary SBVH nodes: 2 x uint4 = 32 B in the reference's node layout.
+//  * compressed 8-wide nodes: 5 x uint4 = 80 B (layout below), children's
+//    boxes quantised to 8 bits per plane relative to the node's origin with
+//    a power-of-two scale per axis, rounded outward.
+//  * wide-leaf triangles: 3 x float4 = 48 B with the BVH-order index in the
+//    fourth lane of the last float4.
+#pragma once
+
+#include <stdint.h>
+
+namespace pg {
+
+// bsdf::UnionBSDF + emission (include/scene/material.h) with the values the
+// reference's BSDF constructors precompute.
+struct DevMaterial {
+  uint32_t type;
+  float diffuse[3];
+  float specular[3];
+  float shininess;
+  float ior;
+  float w_d;
+  float w_g;
+  float roughness;
+  float emission[3];
+  float glossy_norm;      // (shininess + 2) / (2 pi)      glossy.h:19-23
+  float inv_shininess_p1; // 1 / (shininess + 1)
+  float r0;               // ((ior - 1) / (ior + 1))^2     dielectric_refractive.h
+  float cont_inclusive0;  // w_d / (w_d + w_g)              combined.h:22-47
+  float pad[5];
+};
+static_assert(sizeof(DevMaterial) == 96, "DevMaterial is 96 bytes");
+
+// 80-byte compressed wide node.
+//   word 0-2 : origin p (float x3)
+//   word 3   : exponent bytes ex, ey, ez (scale = 2^(e - 127)), imask
+//   word 4   : child_base  (index of the first internal child)
+//   word 5   : tri_base    (index of the first wide-leaf triangle)
+//   word 6-7 : meta[8]: internal child -> rank among internal children;
+//              leaf child -> (count << 5) | triangle offset; 0 -> empty
+//   word 8-19: qlo_x[8] qlo_y[8] qlo_z[8] qhi_x[8] qhi_y[8] qhi_z[8]
+struct WideNode {
+  float p[3];
+  uint8_t e[3];
+  uint8_t imask;
+  uint32_t child_base;
+  uint32_t tri_base;
+  uint8_t meta[8];
+  uint8_t qlo[3][8];
+  uint8_t qhi[3][8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode is 80 bytes");
+
+constexpr uint32_t kMaxLeafTris = 7;      // 3-bit count in meta
+constexpr uint32_t kMaxNodeTris = 32;     // 5-bit offset in meta
+
+// device status word codes (first error wins)
+enum DeviceStatus : uint32_t {
+  kStatusOk = 0,
+  kStatusStackOverflow = 1,
+  kStatusObjectsOverflow = 2,
+  kStatusBadNode = 3,
+};
+
+} // namespace pg

@@ -1,0 +1,893 @@
+// Device side of the render path: BVH traversal (binary and compressed
+// 8-wide), BSDFs, the RandomTriangle light sampler, the Sobol table RNG and
+// the next-event-estimation integrator.
+//
+// Every function restates the reference's arithmetic in the same order
+// (translation units including this header are compiled with --fmad=false):
+//   integrate_sample  <- integrate::rendering_equation +
+//                        rendering_equation_iteration
+//                        (include/integrate/rendering_equation.h:27-129,
+//                         rendering_equation_iteration.h:9-153)
+//   sample_light      <- random_triangle.h:35-90
+//   BSDFs             <- include/bsdf/*.h; GGX is new (Walter et al. 2007)
+//   trace_binary      <- include/intersect/accel/detail/bvh/bvh_impl.h:12-89
+#pragma once
+
+#include "devtypes.h"
+#include "geom.h"
+#include "kernels.h"
+
+namespace pg {
+namespace dev {
+
+constexpr uint32_t kTag = 1u << 31;
+#define PG_INF __int_as_float(0x7f800000)
+
+struct Hit {
+  float t;
+  uint32_t idx; // BVH-order triangle index
+  bool ok;
+  bool back;
+};
+
+struct Counts {
+  uint32_t rays, nodes, tris;
+};
+
+__device__ __forceinline__ Hit no_hit() {
+  Hit h;
+  h.t = PG_INF;
+  h.idx = 0;
+  h.ok = false;
+  h.back = false;
+  return h;
+}
+
+// optional_min fold (include/intersect/optional_min.h:10-26): a later
+// candidate at equal distance replaces the current best
+__device__ __forceinline__ void fold(Hit &best, float t, bool back,
+                                     uint32_t idx) {
+  if (!best.ok || !(best.t < t)) {
+    best.ok = true;
+    best.t = t;
+    best.back = back;
+    best.idx = idx;
+  }
+}
+
+__device__ __forceinline__ void set_status(uint32_t *status, uint32_t code) {
+  atomicCAS(status, 0u, code);
+}
+
+__device__ __forceinline__ void load_tri(const float4 *tris, uint32_t i, f3 &v0,
+                                         f3 &e1, f3 &e2) {
+  float4 a = __ldg(tris + 3 * i);
+  float4 b = __ldg(tris + 3 * i + 1);
+  float4 c = __ldg(tris + 3 * i + 2);
+  v0 = mk(a.x, a.y, a.z);
+  e1 = mk(a.w, b.x, b.y);
+  e2 = mk(b.z, b.w, c.x);
+}
+
+// ---------------------------------------------------------------------------
+// binary SBVH, the reference's traversal order: depth-first stack of 64,
+// candidates gathered until target_objects are pending, then tested
+template <bool kCount>
+__device__ Hit trace_binary(const RenderParams &P, const ray &r, Counts &cnt) {
+  Hit best = no_hit();
+  if (P.n_bin_nodes == 0) {
+    return best;
+  }
+  f3 inv = inv_dir(r.d);
+  uint32_t stack[64];
+  uint32_t sp = 0;
+  stack[sp++] = 0;
+  uint32_t objects[10];
+  uint32_t n_obj = 0;
+  const uint32_t target = P.target_objects;
+  while (sp != 0) {
+    while (n_obj < target && sp != 0) {
+      uint32_t ni = stack[--sp];
+      uint4 a = __ldg(P.bin_nodes + 2 * ni);
+      uint4 b = __ldg(P.bin_nodes + 2 * ni + 1);
+      if (kCount) {
+        ++cnt.nodes;
+      }
+      box bx;
+      bx.lo = mk(__uint_as_float(a.z), __uint_as_float(a.w), __uint_as_float(b.x));
+      bx.hi = mk(__uint_as_float(b.y), __uint_as_float(b.z), __uint_as_float(b.w));
+      float tmin;
+      if (slab(bx, r.o, inv, &tmin) && (!best.ok || best.t > tmin)) {
+        if (a.x & kTag) {
+          if (sp + 2 > 64) {
+            set_status(P.status, kStatusStackOverflow);
+            return no_hit();
+          }
+          stack[sp++] = a.y;
+          stack[sp++] = a.x & ~kTag;
+        } else {
+          uint32_t s = a.x;
+          uint32_t e = a.y & ~kTag;
+          bool extra = (a.y & kTag) != 0;
+          if (e < s || n_obj + (e - s) > 10) {
+            set_status(P.status, kStatusObjectsOverflow);
+            return no_hit();
+          }
+          for (uint32_t i = s; i < e; ++i) {
+            objects[n_obj++] = extra ? __ldg(P.extra_idxs + i) : i;
+          }
+        }
+      }
+    }
+    if (n_obj == 0) {
+      break;
+    }
+    for (uint32_t k = 0; k < n_obj; ++k) {
+      uint32_t idx = objects[k];
+      f3 v0, e1, e2;
+      load_tri(P.tris, idx, v0, e1, e2);
+      if (kCount) {
+        ++cnt.tris;
+      }
+      float t;
+      bool back;
+      if (tri_hit(v0, e1, e2, r, &t, &back)) {
+        fold(best, t, back, idx);
+      }
+    }
+    n_obj = 0;
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+// compressed 8-wide BVH: node loaded with five 128-bit loads, the eight
+// child boxes decoded to exact planes and tested, leaves tested in slot
+// order, internal hits visited nearest first with the rest on a stack of
+// (node, entry distance) pairs that is culled against the current best
+__device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i) {
+  uint32_t w = i < 4 ? lo : hi;
+  return (w >> (8 * (i & 3))) & 0xffu;
+}
+
+__device__ __forceinline__ float exp2_byte(uint32_t e) {
+  return __uint_as_float(e << 23);
+}
+
+constexpr int kWideStack = 128;
+
+template <bool kCount>
+__device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt) {
+  Hit best = no_hit();
+  if (P.n_wide_nodes == 0) {
+    return best;
+  }
+  f3 inv = inv_dir(r.d);
+  uint32_t st_node[kWideStack];
+  float st_t[kWideStack];
+  int sp = 0;
+  uint32_t node = 0;
+  while (true) {
+    const uint4 *np = P.wide_nodes + 5 * (size_t)node;
+    uint4 n0 = __ldg(np);
+    uint4 n1 = __ldg(np + 1);
+    uint4 n2 = __ldg(np + 2);
+    uint4 n3 = __ldg(np + 3);
+    uint4 n4 = __ldg(np + 4);
+    if (kCount) {
+      ++cnt.nodes;
+    }
+    const float px = __uint_as_float(n0.x);
+    const float py = __uint_as_float(n0.y);
+    const float pz = __uint_as_float(n0.z);
+    const float sx = exp2_byte(n0.w & 0xffu);
+    const float sy = exp2_byte((n0.w >> 8) & 0xffu);
+    const float sz = exp2_byte((n0.w >> 16) & 0xffu);
+    const uint32_t imask = n0.w >> 24;
+    const uint32_t child_base = n1.x;
+    const uint32_t tri_base = n1.y;
+    // near / far plane bytes per axis according to the ray direction sign
+    const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
+    const uint32_t nxl = nx ? n3.z : n2.x, nxh = nx ? n3.w : n2.y;
+    const uint32_t fxl = nx ? n2.x : n3.z, fxh = nx ? n2.y : n3.w;
+    const uint32_t nyl = ny ? n4.x : n2.z, nyh = ny ? n4.y : n2.w;
+    const uint32_t fyl = ny ? n2.z : n4.x, fyh = ny ? n2.w : n4.y;
+    const uint32_t nzl = nz ? n4.z : n3.x, nzh = nz ? n4.w : n3.y;
+    const uint32_t fzl = nz ? n3.x : n4.z, fzh = nz ? n3.y : n4.w;
+    float ct[8];
+    uint32_t cn[8];
+    int n_int = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t meta = byte_of(n1.z, n1.w, i);
+      const bool internal = (imask >> i) & 1u;
+      if (!internal && meta == 0) {
+        continue;
+      }
+      // decoded planes p + q 2^e are exact floats
+      float tnx = ((px + (float)byte_of(nxl, nxh, i) * sx) - r.o.x) * inv.x;
+      float tfx = ((px + (float)byte_of(fxl, fxh, i) * sx) - r.o.x) * inv.x;
+      float tny = ((py + (float)byte_of(nyl, nyh, i) * sy) - r.o.y) * inv.y;
+      float tfy = ((py + (float)byte_of(fyl, fyh, i) * sy) - r.o.y) * inv.y;
+      float tnz = ((pz + (float)byte_of(nzl, nzh, i) * sz) - r.o.z) * inv.z;
+      float tfz = ((pz + (float)byte_of(fzl, fzh, i) * sz) - r.o.z) * inv.z;
+      float tmin = fmax2(fmax2(tnx, tny), tnz);
+      float tmax = fmin2(fmin2(tfx, tfy), tfz);
+      if (!(tmin <= tmax) || tmax < 0.f || !(tmin < best.t)) {
+        continue;
+      }
+      if (internal) {
+        ct[n_int] = tmin;
+        cn[n_int] = child_base + meta;
+        ++n_int;
+      } else {
+        uint32_t count = meta >> 5;
+        uint32_t first = tri_base + (meta & 31u);
+        for (uint32_t k = 0; k < count; ++k) {
+          const float4 *tp = P.wide_tris + 3 * (size_t)(first + k);
+          float4 a = __ldg(tp);
+          float4 b = __ldg(tp + 1);
+          float4 c = __ldg(tp + 2);
+          if (kCount) {
+            ++cnt.tris;
+          }
+          float t;
+          bool back;
+          if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), r,
+                      &t, &back)) {
+            fold(best, t, back, __float_as_uint(c.y));
+          }
+        }
+      }
+    }
+    if (n_int > 0) {
+      // order internal hits by entry distance (insertion sort, <= 8)
+      for (int i = 1; i < n_int; ++i) {
+        float kt = ct[i];
+        uint32_t kn = cn[i];
+        int j = i - 1;
+        while (j >= 0 && ct[j] > kt) {
+          ct[j + 1] = ct[j];
+          cn[j + 1] = cn[j];
+          --j;
+        }
+        ct[j + 1] = kt;
+        cn[j + 1] = kn;
+      }
+      if (sp + n_int - 1 > kWideStack) {
+        set_status(P.status, kStatusStackOverflow);
+        return no_hit();
+      }
+      for (int i = n_int - 1; i >= 1; --i) {
+        st_node[sp] = cn[i];
+        st_t[sp] = ct[i];
+        ++sp;
+      }
+      node = cn[0];
+      continue;
+    }
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      if (st_t[sp] < best.t) {
+        node = st_node[sp];
+        found = true;
+        break;
+      }
+    }
+    if (!found) {
+      break;
+    }
+  }
+  return best;
+}
+
+template <uint32_t kTrav, bool kCount>
+__device__ __forceinline__ Hit trace(const RenderParams &P, const ray &r,
+                                     Counts &cnt) {
+  if (kCount) {
+    ++cnt.rays;
+  }
+  if (kTrav == kTravWide) {
+    return trace_wide<kCount>(P, r, cnt);
+  }
+  return trace_binary<kCount>(P, r, cnt);
+}
+
+// ---------------------------------------------------------------------------
+// RNG: table-driven Sobol (include/rng/rng_from_sequence_gen.h:26-107)
+struct Rng {
+  const float *row;
+  uint32_t dim;
+  uint32_t bound;
+  __device__ __forceinline__ float next() {
+    float v = __ldg(row + dim);
+    ++dim;
+    dim = dim == bound ? 0u : dim;
+    return v;
+  }
+};
+
+__device__ __forceinline__ uint32_t fnv_hash(uint32_t in) {
+  uint32_t h = 2166136261u;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h ^= (in >> (8 * i)) & 0xffu;
+    h *= 16777619u;
+  }
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// include/lib/projection.h:9-32, rotation by Rodrigues' formula
+__device__ __forceinline__ f3 rotate(f3 v, float angle, f3 axis) {
+  float s, c;
+  pm::sincos(angle, &s, &c);
+  f3 t0 = v * c;
+  f3 t1 = cross(axis, v) * s;
+  f3 t2 = axis * ((1.f - c) * dot(axis, v));
+  return (t0 + t1) + t2;
+}
+
+__device__ __forceinline__ f3 relative_vec(f3 vec, float phi, float theta) {
+  float st, ct, sp, cp;
+  pm::sincos(theta, &st, &ct);
+  pm::sincos(phi, &sp, &cp);
+  f3 local = mk(st * cp, st * sp, ct);
+  float angle = pm::acos(vec.z);
+  f3 axis = normalize(cross(vec, mk(0.f, 0.f, 1.f)));
+  return normalize(rotate(local, -angle, axis));
+}
+
+__device__ __forceinline__ f3 reflect(f3 v, f3 n) {
+  float k = 2.0f * -dot(v, n);
+  return normalize(v + n * k);
+}
+
+__device__ f3 refract(float ior, f3 v, f3 n) {
+  float c = -dot(v, n);
+  bool exiting = c < 0.f;
+  float frac = exiting ? ior : 1.f / ior;
+  float in_sqrt = 1.f - frac * frac * (1.f - c * c);
+  f3 ne = exiting ? -n : n;
+  if (in_sqrt > 0.f) {
+    float angle = pm::acos(pm::sqrt(in_sqrt));
+    f3 axis = normalize(cross(v, ne));
+    return normalize(rotate(-ne, angle, axis));
+  }
+  return reflect(v, n);
+}
+
+// ---------------------------------------------------------------------------
+// BSDFs
+struct Mat {
+  uint32_t type;
+  rgb diffuse, specular, emission;
+  float shininess, ior, w_d, roughness, glossy_norm, inv_shininess_p1, r0,
+      cont_inclusive0;
+};
+
+__device__ __forceinline__ Mat load_mat(const DevMaterial *m) {
+  Mat o;
+  o.type = __ldg(&m->type);
+  o.diffuse = mkrgb(__ldg(&m->diffuse[0]), __ldg(&m->diffuse[1]), __ldg(&m->diffuse[2]));
+  o.specular = mkrgb(__ldg(&m->specular[0]), __ldg(&m->specular[1]), __ldg(&m->specular[2]));
+  o.emission = mkrgb(__ldg(&m->emission[0]), __ldg(&m->emission[1]), __ldg(&m->emission[2]));
+  o.shininess = __ldg(&m->shininess);
+  o.ior = __ldg(&m->ior);
+  o.w_d = __ldg(&m->w_d);
+  o.roughness = __ldg(&m->roughness);
+  o.glossy_norm = __ldg(&m->glossy_norm);
+  o.inv_shininess_p1 = __ldg(&m->inv_shininess_p1);
+  o.r0 = __ldg(&m->r0);
+  o.cont_inclusive0 = __ldg(&m->cont_inclusive0);
+  return o;
+}
+
+__device__ __forceinline__ rgb emission_of(const DevMaterial *m) {
+  return mkrgb(__ldg(&m->emission[0]), __ldg(&m->emission[1]), __ldg(&m->emission[2]));
+}
+
+enum : uint32_t {
+  kDiffuse = 0,
+  kGlossy = 1,
+  kDiffuseGlossy = 2,
+  kDiffuseMirror = 3,
+  kMirror = 4,
+  kDielectric = 5,
+  kGGX = 6,
+};
+
+__device__ __forceinline__ bool is_brdf(const Mat &m) { return m.type != kDielectric; }
+
+__device__ __forceinline__ float prob_continuous(const Mat &m) {
+  switch (m.type) {
+  case kDiffuse:
+  case kGlossy:
+  case kDiffuseGlossy:
+  case kGGX:
+    return 1.0f;
+  case kMirror:
+  case kDielectric:
+    return 0.0f;
+  default:
+    return m.w_d;
+  }
+}
+
+// (float)(1 / M_PI)
+constexpr float kInvPi = 0x1.45f306p-2f;
+constexpr double kTwoPi = 6.283185307179586;
+
+__device__ __forceinline__ rgb glossy_eval(const Mat &m, f3 in, f3 out, f3 n) {
+  float c = fmax2(dot(reflect(in, n), out), 0.0f);
+  return (m.specular * m.glossy_norm) * pm::pow(c, m.shininess);
+}
+
+__device__ __forceinline__ float ggx_g1(float c, float a2) {
+  return (2.f * c) / (c + pm::sqrt(a2 + (1.f - a2) * (c * c)));
+}
+
+__device__ __forceinline__ rgb schlick(rgb f0, float c) {
+  float m = 1.f - c;
+  float m2 = m * m;
+  float m5 = (m2 * m2) * m;
+  return mkrgb(f0.r + (1.f - f0.r) * m5, f0.g + (1.f - f0.g) * m5,
+               f0.b + (1.f - f0.b) * m5);
+}
+
+// GGX microfacet reflection (Walter et al. 2007): D GGX, separable Smith G,
+// Schlick Fresnel
+__device__ rgb ggx_eval(const Mat &m, f3 in, f3 out, f3 n) {
+  f3 wo = -in;
+  if (dot(wo, n) < 0.f) {
+    n = -n;
+  }
+  float co = dot(wo, n);
+  float ci = dot(out, n);
+  if (!(co > 0.f) || !(ci > 0.f)) {
+    return zero_rgb();
+  }
+  float a2 = m.roughness * m.roughness;
+  f3 h = normalize(wo + out);
+  float ch = dot(h, n);
+  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
+  float d = a2 / ((0x1.921fb6p+1f * dd) * dd); // (float)M_PI
+  float g = ggx_g1(co, a2) * ggx_g1(ci, a2);
+  rgb f = schlick(m.specular, dot(wo, h));
+  float scale = (d * g) / ((4.f * ci) * co);
+  return f * scale;
+}
+
+__device__ rgb continuous_eval(const Mat &m, f3 in, f3 out, f3 n) {
+  switch (m.type) {
+  case kDiffuse:
+    return m.diffuse * kInvPi;
+  case kGlossy:
+    return glossy_eval(m, in, out, n);
+  case kDiffuseGlossy: {
+    float w0 = m.cont_inclusive0 - 0.f;
+    float w1 = 1.f - m.cont_inclusive0;
+    return (m.diffuse * kInvPi) * w0 + glossy_eval(m, in, out, n) * w1;
+  }
+  case kDiffuseMirror:
+    return (m.diffuse * kInvPi) * (1.f - 0.f);
+  case kGGX:
+    return ggx_eval(m, in, out, n);
+  default:
+    return zero_rgb();
+  }
+}
+
+struct Sample {
+  f3 dir;
+  rgb mult;
+};
+
+__device__ __forceinline__ Sample diffuse_sample(rgb albedo, f3 in, f3 n, Rng &rng) {
+  float v0 = rng.next();
+  float v1 = rng.next();
+  float phi = (float)(kTwoPi * (double)v0);
+  float theta = pm::asin(pm::sqrt(v1));
+  f3 aligned = dot(in, n) > 0.f ? -n : n;
+  Sample s;
+  s.dir = relative_vec(aligned, phi, theta);
+  s.mult = albedo;
+  return s;
+}
+
+__device__ Sample glossy_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+  float v0 = rng.next();
+  float v1 = rng.next();
+  f3 refl = reflect(in, n);
+  float phi = (float)(kTwoPi * (double)v0);
+  float psi = pm::acos(pm::pow(v1, m.inv_shininess_p1));
+  Sample s;
+  s.dir = relative_vec(refl, phi, psi);
+  s.mult = m.specular;
+  return s;
+}
+
+// orthonormal basis (Duff et al. 2017, "Building an Orthonormal Basis,
+// Revisited")
+__device__ __forceinline__ void onb(f3 n, f3 &b1, f3 &b2) {
+  float sign = n.z >= 0.f ? 1.f : -1.f;
+  float a = -1.f / (sign + n.z);
+  float b = n.x * n.y * a;
+  b1 = mk(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  b2 = mk(b, sign + n.y * n.y * a, -n.y);
+}
+
+__device__ Sample ggx_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+  float u0 = rng.next();
+  float u1 = rng.next();
+  f3 wo = -in;
+  if (dot(wo, n) < 0.f) {
+    n = -n;
+  }
+  float a2 = m.roughness * m.roughness;
+  float phi = (float)(kTwoPi * (double)u0);
+  float tan2 = (a2 * u1) / (1.f - u1);
+  float cos_t = 1.f / pm::sqrt(1.f + tan2);
+  float sin_t = pm::sqrt(fmax2(0.f, 1.f - cos_t * cos_t));
+  f3 b1, b2;
+  onb(n, b1, b2);
+  float sp, cp;
+  pm::sincos(phi, &sp, &cp);
+  f3 h = normalize((b1 * (sin_t * cp) + b2 * (sin_t * sp)) + n * cos_t);
+  float k = 2.f * dot(wo, h);
+  f3 wi = normalize(h * k - wo);
+  float co = dot(wo, n);
+  float ci = dot(wi, n);
+  float ch = dot(h, n);
+  float oh = dot(wo, h);
+  Sample s;
+  s.dir = wi;
+  if (!(ci > 0.f) || !(co > 0.f) || !(ch > 0.f) || !(oh > 0.f)) {
+    s.mult = zero_rgb();
+    return s;
+  }
+  float g = ggx_g1(co, a2) * ggx_g1(ci, a2);
+  rgb f = schlick(m.specular, oh);
+  float w = (g * oh) / (co * ch);
+  s.mult = f * w;
+  return s;
+}
+
+__device__ Sample continuous_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+  switch (m.type) {
+  case kDiffuse:
+    return diffuse_sample(m.diffuse, in, n, rng);
+  case kGlossy:
+    return glossy_sample(m, in, n, rng);
+  case kDiffuseGlossy: {
+    float loc = rng.next();
+    if (loc <= m.cont_inclusive0) {
+      return diffuse_sample(m.diffuse, in, n, rng);
+    }
+    return glossy_sample(m, in, n, rng);
+  }
+  case kDiffuseMirror:
+    (void)rng.next();
+    return diffuse_sample(m.diffuse, in, n, rng);
+  case kGGX:
+    return ggx_sample(m, in, n, rng);
+  default: {
+    Sample s;
+    s.dir = in;
+    s.mult = zero_rgb();
+    return s;
+  }
+  }
+}
+
+__device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+  Sample s;
+  s.mult = m.specular;
+  switch (m.type) {
+  case kMirror:
+    s.dir = reflect(in, n);
+    return s;
+  case kDiffuseMirror:
+    (void)rng.next();
+    s.dir = reflect(in, n);
+    return s;
+  case kDielectric: {
+    float c = pm::fabs(dot(in, n));
+    double x = (double)(1.f - c);
+    double x2 = x * x;
+    double p5 = (x2 * x2) * x;
+    float prop = (float)((double)m.r0 + (double)(1.f - m.r0) * p5);
+    if (rng.next() < prop) {
+      s.dir = reflect(in, n);
+    } else {
+      s.dir = refract(m.ior, in, n);
+    }
+    return s;
+  }
+  default:
+    s.dir = in;
+    s.mult = zero_rgb();
+    return s;
+  }
+}
+
+__device__ Sample uniform_dir_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+  float v0 = rng.next();
+  float v1 = rng.next();
+  bool whole = !is_brdf(m);
+  float phi = (float)(kTwoPi * (double)v0);
+  float theta = pm::acos(whole ? 2.f * v1 - 1.f : v1);
+  Sample s;
+  s.dir = relative_vec(n, phi, theta);
+  float inv_prob = whole ? 0x1.921fb6p+3f : 0x1.921fb6p+2f; // (float)(4 pi), (float)(2 pi)
+  rgb f = continuous_eval(m, in, s.dir, n);
+  s.mult = (f * dot(s.dir, n)) * inv_prob;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// RandomTriangle light sample (random_triangle.h:35-90).  |n.d| |N_A.d| <
+// 1e-8 in double equals <= 1e-8f in float for float operands.
+struct LightSample {
+  f3 dir;
+  float mult;
+  float target;
+};
+
+__device__ bool sample_light(const RenderParams &P, f3 pos, const Mat &m, f3 normal,
+                             Rng &rng, LightSample &out) {
+  if (P.n_lights == 0) {
+    return false;
+  }
+  float search = rng.next();
+  uint32_t idx = 0;
+  for (; idx < P.n_lights; ++idx) {
+    if (__ldg(P.light_cdf + idx) >= search) {
+      break;
+    }
+  }
+  if (idx >= P.n_lights) {
+    idx = P.n_lights - 1; // unreachable for a normalised table
+  }
+  float4 a = __ldg(P.light_tris + 3 * idx);
+  float4 b = __ldg(P.light_tris + 3 * idx + 1);
+  float4 c = __ldg(P.light_tris + 3 * idx + 2);
+  f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+  float s = rng.next();
+  float t = rng.next();
+  if (s + t > 1.f) {
+    s = 1.f - s;
+    t = 1.f - t;
+  }
+  f3 point = (e0 * s + e1 * t) + v0;
+  f3 dir_un = point - pos;
+  if (is_brdf(m) && dot(dir_un, normal) <= 0.f) {
+    return false;
+  }
+  f3 dir = normalize(dir_un);
+  f3 tn = cross(e0, e1) * 0.5f;
+  float prob = __ldg(P.light_cdf + idx) - (idx == 0 ? 0.f : __ldg(P.light_cdf + idx - 1));
+  float nw = pm::fabs(dot(normal, dir) * dot(tn, dir));
+  if (nw <= 1e-8f) {
+    return false;
+  }
+  float weight = nw / sqnorm(dir_un);
+  out.dir = dir;
+  out.mult = prob / weight;
+  out.target = length(dir_un);
+  return true;
+}
+
+// include/integrate/term_prob/*
+__device__ __forceinline__ float term_prob(const RenderParams &P, uint32_t iters,
+                                           rgb mult) {
+  switch (P.term_prob) {
+  case 0:
+    return P.term_prob_prob;
+  case 1:
+    return iters >= P.term_iters ? 1.0f : 0.0f;
+  case 2: {
+    rgb q = mkrgb(mult.r / (mult.r + 1.f), mult.g / (mult.g + 1.f),
+                  mult.b / (mult.b + 1.f));
+    q = q * 0.57f;
+    float sq = (q.r * q.r + q.g * q.g) + q.b * q.b;
+    sq = fmin2(fmax2(sq, 0.0f), 1.0f);
+    float p = pm::fabs(pm::pow(1.f - sq, P.term_exp));
+    return fmax2(p, P.term_min_prob);
+  }
+  default: {
+    float p = 1.f - 1.f / (sum(mult) / 3.f);
+    return fmin2(fmax2(p, P.term_min_prob), 1.f);
+  }
+  }
+}
+
+// camera ray (initial_ray_sample.h:16-56)
+__device__ __forceinline__ ray camera_ray(const RenderParams &P, float x, float y) {
+  f3 film = mk((2.0f * x) / (float)P.x_dim - 1.0f, (-2.0f * y) / (float)P.y_dim + 1.0f,
+               -1.0f);
+  const float *m = P.f2w;
+  f3 world = mk(((m[0] * film.x + m[1] * film.y) + m[2] * film.z) + m[3],
+                ((m[4] * film.x + m[5] * film.y) + m[6] * film.z) + m[7],
+                ((m[8] * film.x + m[9] * film.y) + m[10] * film.z) + m[11]);
+  ray r;
+  r.o = mk(m[3], m[7], m[11]);
+  r.d = normalize(world - r.o);
+  return r;
+}
+
+__device__ __forceinline__ f3 shading_normal(const RenderParams &P, uint32_t idx,
+                                             f3 point, uint32_t &material) {
+  float4 a = __ldg(P.tri_data + 3 * idx);
+  float4 b = __ldg(P.tri_data + 3 * idx + 1);
+  float4 c = __ldg(P.tri_data + 3 * idx + 2);
+  material = __float_as_uint(c.w);
+  f3 n0 = mk(a.x, a.y, a.z), n1 = mk(a.w, b.x, b.y), n2 = mk(b.z, b.w, c.x);
+  f3 v0, e1, e2;
+  load_tri(P.tris, idx, v0, e1, e2);
+  float w[3];
+  barycentric(e1, e2, point - v0, w);
+  return normalize((n0 * w[0] + n1 * w[1]) + n2 * w[2]);
+}
+
+// one camera sample of rendering_equation, with at most one light sample
+// per vertex
+template <uint32_t kTrav, bool kCount>
+__device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
+                                uint32_t x, uint32_t y, Counts &cnt) {
+  const uint32_t location = x + y * P.x_dim;
+  Rng rng;
+  rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
+  rng.bound = P.dim_bound;
+  rng.dim = fnv_hash(location) % P.init_dim_bound;
+  float xo = rng.next();
+  float yo = rng.next();
+  ray r = camera_ray(P, (float)x + xo, (float)y + yo);
+
+  uint32_t iters = 0;
+  bool count_emission = true;
+  bool has_next = true;
+  rgb multiplier = mkrgb(1.f, 1.f, 1.f);
+  bool has_light = false;
+  ray light_ray;
+  light_ray.o = mk(0.f, 0.f, 0.f);
+  light_ray.d = mk(0.f, 0.f, 0.f);
+  rgb light_mult = zero_rgb();
+  float light_target = 0.f;
+  rgb total = zero_rgb();
+  const bool performs_samples = P.light_sampler == 0;
+  const bool cull = P.back_cull != 0;
+
+  while (true) {
+    Hit lh = no_hit(), nh = no_hit();
+    if (has_light) {
+      lh = trace<kTrav, kCount>(P, light_ray, cnt);
+    }
+    if (has_next) {
+      nh = trace<kTrav, kCount>(P, r, cnt);
+    }
+    if (has_light && lh.ok && pm::fabs(light_target - lh.t) <= 1e-6f &&
+        (!cull || !lh.back)) {
+      float4 c = __ldg(P.tri_data + 3 * lh.idx + 2);
+      total = total + emission_of(P.materials + __float_as_uint(c.w)) * light_mult;
+    }
+    if (!has_next || !nh.ok) {
+      return total;
+    }
+    f3 point = r.o + r.d * nh.t;
+    uint32_t mi;
+    f3 normal = shading_normal(P, nh.idx, point, mi);
+    const Mat mat = load_mat(P.materials + mi);
+    if ((!performs_samples || count_emission) && (!cull || !nh.back)) {
+      total = total + multiplier * mat.emission;
+    }
+    bool new_has_light = false;
+    rgb new_light_mult = zero_rgb();
+    float new_light_target = 0.f;
+    ray new_light_ray = light_ray;
+    float pc = prob_continuous(mat);
+    if (pc > 0.f && performs_samples) {
+      LightSample ls;
+      if (sample_light(P, point, mat, normal, rng, ls)) {
+        rgb f = continuous_eval(mat, r.d, ls.dir, normal);
+        new_light_mult = ((multiplier * f) * pc) / ls.mult;
+        new_light_target = ls.target;
+        new_light_ray.o = point;
+        new_light_ray.d = ls.dir;
+        new_has_light = true;
+      }
+    }
+    bool take_discrete;
+    if (pc == 0.f) {
+      take_discrete = true;
+    } else if (pc == 1.f) {
+      take_discrete = false;
+    } else {
+      take_discrete = pc < rng.next();
+    }
+    Sample smp;
+    if (take_discrete) {
+      smp = discrete_sample(mat, r.d, normal, rng);
+    } else if (P.dir_sampler == 0) {
+      smp = continuous_sample(mat, r.d, normal, rng);
+    } else {
+      smp = uniform_dir_sample(mat, r.d, normal, rng);
+    }
+    rgb new_multiplier = multiplier * smp.mult;
+    float p = term_prob(P, iters, new_multiplier);
+    bool next = rng.next() > p;
+    iters += 1;
+    count_emission = take_discrete;
+    has_light = new_has_light;
+    light_mult = new_light_mult;
+    light_target = new_light_target;
+    light_ray = new_light_ray;
+    if (next) {
+      multiplier = new_multiplier / (1.0f - p);
+      r.o = point;
+      r.d = smp.dir;
+      has_next = true;
+    } else {
+      has_next = false;
+      if (!has_light) {
+        return total;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// reduction over sample_block_size lanes (include/lib/cuda/reduce.cuh:35-102)
+__device__ __forceinline__ rgb warp_reduce(rgb v, uint32_t width) {
+  for (uint32_t off = width / 2; off > 0; off /= 2) {
+    float r = __shfl_down_sync(0xffffffffu, v.r, off, width);
+    float g = __shfl_down_sync(0xffffffffu, v.g, off, width);
+    float b = __shfl_down_sync(0xffffffffu, v.b, off, width);
+    v = mkrgb(r + v.r, g + v.g, b + v.b);
+  }
+  return v;
+}
+
+__device__ __forceinline__ rgb sub_block_reduce(rgb v, uint32_t tid, uint32_t sbs) {
+  v = warp_reduce(v, sbs < 32u ? sbs : 32u);
+  if (sbs <= 32) {
+    return v;
+  }
+  __shared__ float sh[32][3];
+  uint32_t lane = tid % 32, warp = tid / 32;
+  if (lane == 0) {
+    sh[warp][0] = v.r;
+    sh[warp][1] = v.g;
+    sh[warp][2] = v.b;
+  }
+  __syncthreads();
+  uint32_t per_group = sbs / 32;
+  if (tid % sbs < per_group) {
+    uint32_t k = lane + (tid / sbs) * per_group;
+    v = mkrgb(sh[k][0], sh[k][1], sh[k][2]);
+  }
+  return warp_reduce(v, per_group);
+}
+
+// assign_output (include/render/detail/integrate_image/assign_output.h:11-24)
+// and float_rgb_to_bgra_32 (include/lib/bgra_32.h:12-31)
+__device__ __forceinline__ void write_pixel(float *out_rgb, uint8_t *out_bgra,
+                                            bool bgra, size_t idx, rgb v) {
+  if (bgra) {
+    float tr = v.r / (v.r + 1.f), tg = v.g / (v.g + 1.f), tb = v.b / (v.b + 1.f);
+    uchar4 o;
+    o.x = (unsigned char)(tb * 255.0f);
+    o.y = (unsigned char)(tg * 255.0f);
+    o.z = (unsigned char)(tr * 255.0f);
+    o.w = 0;
+    reinterpret_cast<uchar4 *>(out_bgra)[idx] = o;
+  } else {
+    out_rgb[3 * idx] = v.r;
+    out_rgb[3 * idx + 1] = v.g;
+    out_rgb[3 * idx + 2] = v.b;
+  }
+}
+
+} // namespace dev
+} // namespace pg

@@ -1,0 +1,80 @@
+// Launch interface between the host orchestration and the CUDA kernels.
+#pragma once
+
+#include "devtypes.h"
+#include "workdiv.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pg {
+
+struct RenderParams {
+  // geometry (device pointers)
+  const float4 *tris;       // BVH order, 3 float4 per triangle
+  const float4 *tri_data;   // normals + material, 3 float4 per triangle
+  const uint4 *bin_nodes;   // 2 uint4 per binary node
+  const uint32_t *extra_idxs;
+  const uint4 *wide_nodes;  // 5 uint4 per wide node
+  const float4 *wide_tris;  // 3 float4 per wide-leaf triangle
+  uint32_t n_tris, n_bin_nodes, n_wide_nodes;
+  const DevMaterial *materials;
+  const float4 *light_tris; // 3 float4 per light triangle: v0, e0, e1
+  const float *light_cdf;
+  uint32_t n_lights;
+  // rng: Sobol table [spp][dim_bound]
+  const float *sobol;
+  uint32_t dim_bound, init_dim_bound;
+  // integrator settings
+  uint32_t light_sampler, dir_sampler, term_prob, term_iters;
+  float term_prob_prob, term_exp, term_min_prob;
+  uint32_t back_cull, target_objects;
+  // image
+  float f2w[12];
+  uint32_t x_dim, y_dim, spp;
+  WorkDiv wd;
+  // outputs
+  float *out_rgb;     // [nsb * x_dim * y_dim][3]
+  uint8_t *out_bgra;  // [x_dim * y_dim][4] when output_bgra and nsb == 1
+  uint32_t output_bgra;
+  uint32_t *status;   // first in-kernel error code
+  unsigned long long *counters; // [3] rays, nodes, triangles (counting runs)
+  uint32_t start_block;
+};
+
+enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
+
+// integration megakernel over blocks [start_block, start_block + n_blocks)
+cudaError_t launch_render(const RenderParams &p, uint32_t traversal,
+                          uint32_t n_blocks, bool counting, cudaStream_t s);
+
+// one ReduceFloatRGB pass (reduce_float_rgb_impl.h:17-63)
+struct ReduceParams {
+  const float *in;
+  float *out;
+  uint8_t *out_bgra;
+  uint32_t reduction_factor;
+  uint32_t spp;
+  uint32_t output_bgra;
+  WorkDiv wd;
+};
+cudaError_t launch_reduce(const ReduceParams &p, cudaStream_t s);
+
+// closest hit for a batch of rays: idx = original triangle index or -1
+cudaError_t launch_intersect(const RenderParams &p, uint32_t traversal,
+                             const float *rays, uint32_t n_rays,
+                             const uint32_t *bvh_to_orig, int32_t *idx_out,
+                             float *t_out, cudaStream_t s);
+
+// Sobol table from direction vectors [dim][32] and scrambles [dim]
+cudaError_t launch_sobol_table(const uint32_t *dirs, const uint32_t *scramble,
+                               uint32_t dimension_bound, uint32_t count,
+                               float *out, cudaStream_t s);
+cudaError_t launch_sobol_curand(const uint32_t *dirs, const uint32_t *scramble,
+                                uint32_t dimension_bound, uint32_t count,
+                                float *out, cudaStream_t s);
+
+cudaError_t launch_pmath(uint32_t fn, const float *x, const float *y,
+                         float *out, uint32_t n, cudaStream_t s);
+
+} // namespace pg

@@ -1,0 +1,602 @@
+// render::Renderer for the GPU execution model (see renderer.h).
+#include "renderer.h"
+
+#include <curand.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace pg {
+
+cudaError_t DeviceBuffer::ensure(size_t bytes) {
+  if (bytes <= size_ && ptr_ != nullptr) {
+    return cudaSuccess;
+  }
+  release();
+  if (bytes == 0) {
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMalloc(&ptr_, bytes);
+  if (e != cudaSuccess) {
+    ptr_ = nullptr;
+    size_ = 0;
+    return e;
+  }
+  size_ = bytes;
+  return cudaSuccess;
+}
+
+cudaError_t DeviceBuffer::upload(const void *src, size_t bytes, cudaStream_t s) {
+  cudaError_t e = ensure(bytes);
+  if (e != cudaSuccess || bytes == 0) {
+    return e;
+  }
+  return cudaMemcpyAsync(ptr_, src, bytes, cudaMemcpyHostToDevice, s);
+}
+
+void DeviceBuffer::release() {
+  if (ptr_ != nullptr) {
+    cudaFree(ptr_);
+  }
+  ptr_ = nullptr;
+  size_ = 0;
+}
+
+cudaError_t PinnedBuffer::ensure(size_t n) {
+  bytes = n;
+  if (n <= cap_ && ptr_ != nullptr) {
+    return cudaSuccess;
+  }
+  release();
+  bytes = n;
+  if (n == 0) {
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMallocHost(&ptr_, n);
+  if (e != cudaSuccess) {
+    ptr_ = nullptr;
+    cap_ = 0;
+    bytes = 0;
+    return e;
+  }
+  cap_ = n;
+  return cudaSuccess;
+}
+
+void PinnedBuffer::release() {
+  if (ptr_ != nullptr) {
+    cudaFreeHost(ptr_);
+  }
+  ptr_ = nullptr;
+  cap_ = 0;
+  bytes = 0;
+}
+
+Status cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) {
+    return Status::ok();
+  }
+  path_status code = e == cudaErrorMemoryAllocation ? PATH_ERR_OOM : PATH_ERR_CUDA;
+  return Status::err(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PG_TRY_CUDA(expr, what)                                                \
+  do {                                                                         \
+    Status st_ = cuda_status((expr), what);                                    \
+    if (!st_.good()) {                                                         \
+      return st_;                                                              \
+    }                                                                          \
+  } while (0)
+
+Renderer::Renderer() = default;
+
+Renderer::~Renderer() {
+  if (initialised_) {
+    cudaStreamSynchronize(stream_);
+    cudaEventDestroy(ev_start_);
+    cudaEventDestroy(ev_stop_);
+    cudaStreamDestroy(stream_);
+  }
+}
+
+Status Renderer::init() {
+  if (initialised_) {
+    return Status::ok();
+  }
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    return Status::err(PATH_ERR_CUDA, std::string("no CUDA device available: ") +
+                                          cudaGetErrorString(e));
+  }
+  PG_TRY_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  PG_TRY_CUDA(cudaEventCreate(&ev_start_), "event");
+  PG_TRY_CUDA(cudaEventCreate(&ev_stop_), "event");
+  initialised_ = true;
+  return Status::ok();
+}
+
+static DevMaterial to_dev(const path_material &m) {
+  DevMaterial d;
+  std::memset(&d, 0, sizeof(d));
+  d.type = m.type;
+  for (int i = 0; i < 3; ++i) {
+    d.diffuse[i] = m.diffuse[i];
+    d.specular[i] = m.specular[i];
+    d.emission[i] = m.emission[i];
+  }
+  d.shininess = m.shininess;
+  d.ior = m.ior;
+  d.w_d = m.diffuse_weight;
+  d.w_g = m.glossy_weight;
+  d.roughness = m.roughness;
+  d.glossy_norm = (m.shininess + 2.f) / (2.f * (float)M_PI);
+  d.inv_shininess_p1 = 1.f / (m.shininess + 1.f);
+  float r0 = (m.ior - 1) / (m.ior + 1);
+  d.r0 = r0 * r0;
+  d.cont_inclusive0 = m.diffuse_weight / (m.diffuse_weight + m.glossy_weight);
+  return d;
+}
+
+static void put_tri(float *dst, f3 v0, f3 v1, f3 v2, uint32_t extra_bits) {
+  f3 e1 = v1 - v0, e2 = v2 - v0;
+  float vals[12] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z, 0.f, 0.f, 0.f};
+  std::memcpy(&vals[10], &extra_bits, sizeof(extra_bits));
+  std::memcpy(dst, vals, sizeof(vals));
+}
+
+Status Renderer::upload_geometry(const FlatScene &flat,
+                                 const std::vector<path_material> &mats) {
+  const BinaryBVH &bvh = prep_.bvh;
+  const WideBVH &wide = prep_.wide;
+  const size_t n = flat.v0.size();
+  PG_TRY_CUDA(st_tris_.ensure(n * 48), "staging");
+  PG_TRY_CUDA(st_data_.ensure(n * 48), "staging");
+  PG_TRY_CUDA(st_nodes_.ensure(bvh.nodes.size() * 32), "staging");
+  PG_TRY_CUDA(st_extra_.ensure(bvh.extra_idxs.size() * 4), "staging");
+  PG_TRY_CUDA(st_wnodes_.ensure(wide.nodes.size() * sizeof(WideNode)), "staging");
+  PG_TRY_CUDA(st_wtris_.ensure(wide.tri_index.size() * 48), "staging");
+  PG_TRY_CUDA(st_mats_.ensure(mats.size() * sizeof(DevMaterial)), "staging");
+  PG_TRY_CUDA(st_lights_.ensure(flat.light_v0.size() * 48), "staging");
+  PG_TRY_CUDA(st_cdf_.ensure(flat.light_cdf.size() * 4), "staging");
+  PG_TRY_CUDA(st_perm_.ensure(bvh.permutation.size() * 4), "staging");
+  float *tris = st_tris_.as<float>();
+  float *data = st_data_.as<float>();
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t o = bvh.permutation[i];
+    put_tri(&tris[12 * i], flat.v0[o], flat.v1[o], flat.v2[o], 0);
+    float d[12] = {flat.n0[o].x, flat.n0[o].y, flat.n0[o].z, flat.n1[o].x,
+                   flat.n1[o].y, flat.n1[o].z, flat.n2[o].x, flat.n2[o].y,
+                   flat.n2[o].z, 0.f, 0.f, 0.f};
+    std::memcpy(&d[11], &flat.material[o], sizeof(uint32_t));
+    std::memcpy(&data[12 * i], d, sizeof(d));
+  }
+  uint32_t *nodes = st_nodes_.as<uint32_t>();
+  for (size_t i = 0; i < bvh.nodes.size(); ++i) {
+    const BinaryNode &b = bvh.nodes[i];
+    float bx[6] = {b.aabb.lo.x, b.aabb.lo.y, b.aabb.lo.z,
+                   b.aabb.hi.x, b.aabb.hi.y, b.aabb.hi.z};
+    nodes[8 * i] = b.w0;
+    nodes[8 * i + 1] = b.w1;
+    std::memcpy(&nodes[8 * i + 2], bx, sizeof(bx));
+  }
+  if (!bvh.extra_idxs.empty()) {
+    std::memcpy(st_extra_.get(), bvh.extra_idxs.data(), bvh.extra_idxs.size() * 4);
+  }
+  if (!wide.nodes.empty()) {
+    std::memcpy(st_wnodes_.get(), wide.nodes.data(), wide.nodes.size() * sizeof(WideNode));
+  }
+  float *wtris = st_wtris_.as<float>();
+  for (size_t k = 0; k < wide.tri_index.size(); ++k) {
+    uint32_t b = wide.tri_index[k];
+    uint32_t o = bvh.permutation[b];
+    put_tri(&wtris[12 * k], flat.v0[o], flat.v1[o], flat.v2[o], 0);
+    std::memcpy(&wtris[12 * k + 9], &b, sizeof(b));
+  }
+  DevMaterial *dm = st_mats_.as<DevMaterial>();
+  for (size_t i = 0; i < mats.size(); ++i) {
+    dm[i] = to_dev(mats[i]);
+  }
+  float *lt = st_lights_.as<float>();
+  for (size_t i = 0; i < flat.light_v0.size(); ++i) {
+    put_tri(&lt[12 * i], flat.light_v0[i], flat.light_v1[i], flat.light_v2[i], 0);
+  }
+  if (!flat.light_cdf.empty()) {
+    std::memcpy(st_cdf_.get(), flat.light_cdf.data(), flat.light_cdf.size() * 4);
+  }
+  if (!bvh.permutation.empty()) {
+    std::memcpy(st_perm_.get(), bvh.permutation.data(), bvh.permutation.size() * 4);
+  }
+  uint64_t bytes = 0;
+  Status sc = copy_staged(&bytes);
+  if (!sc.good()) {
+    return sc;
+  }
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "upload sync");
+  prep_.n_tris = (uint32_t)n;
+  prep_.n_lights = (uint32_t)flat.light_v0.size();
+  return Status::ok();
+}
+
+// host -> device copies of every staged scene array (asynchronous)
+Status Renderer::copy_staged(uint64_t *bytes) {
+  struct Pair {
+    DeviceBuffer *dev;
+    PinnedBuffer *host;
+  };
+  Pair pairs[] = {{&tris_, &st_tris_},       {&tri_data_, &st_data_},
+                  {&bin_nodes_, &st_nodes_}, {&extra_, &st_extra_},
+                  {&wide_nodes_, &st_wnodes_}, {&wide_tris_, &st_wtris_},
+                  {&materials_, &st_mats_},  {&light_tris_, &st_lights_},
+                  {&light_cdf_, &st_cdf_},   {&perm_, &st_perm_}};
+  uint64_t total = 0;
+  for (const Pair &p : pairs) {
+    PG_TRY_CUDA(p.dev->upload(p.host->get(), p.host->bytes, stream_), "scene upload");
+    total += p.host->bytes;
+  }
+  *bytes = total;
+  return Status::ok();
+}
+
+Status Renderer::prepare_scene(const FlatScene &flat, uint64_t id, uint64_t version,
+                               const SBVHSettings &sbvh, bool force) {
+  if (!force && prep_.valid && prep_.scene_id == id && prep_.scene_version == version &&
+      prep_.sbvh.overlap_threshold == sbvh.overlap_threshold &&
+      prep_.sbvh.use_spatial_splits == sbvh.use_spatial_splits &&
+      prep_.sbvh.traversal_per_intersect_cost == sbvh.traversal_per_intersect_cost &&
+      prep_.sbvh.target_objects == sbvh.target_objects) {
+    return Status::ok();
+  }
+  prep_.valid = false;
+  auto t0 = std::chrono::steady_clock::now();
+  prep_.bvh = build_sbvh(flat.v0.data(), flat.v1.data(), flat.v2.data(), flat.v0.size(), sbvh);
+  prep_.wide = build_wide(prep_.bvh);
+  auto t1 = std::chrono::steady_clock::now();
+  prep_.build_seconds = std::chrono::duration<double>(t1 - t0).count();
+  prep_.scene_id = id;
+  prep_.scene_version = version;
+  prep_.sbvh = sbvh;
+  return Status::ok();
+}
+
+Status Renderer::prepare_sobol(uint32_t dim_bound, uint32_t count) {
+  if (sobol_bound_ == dim_bound && sobol_count_ == count && sobol_table_.get()) {
+    return Status::ok();
+  }
+  curandDirectionVectors32_t *vecs = nullptr;
+  unsigned *scr = nullptr;
+  if (curandGetDirectionVectors32(&vecs, CURAND_SCRAMBLED_DIRECTION_VECTORS_32_JOEKUO6) !=
+          CURAND_STATUS_SUCCESS ||
+      curandGetScrambleConstants32(&scr) != CURAND_STATUS_SUCCESS) {
+    return Status::err(PATH_ERR_CUDA, "cuRAND direction vectors unavailable");
+  }
+  if (dim_bound > 20000) {
+    return Status::err(PATH_ERR_ARGUMENT, "max_sample_size above the 20000 Sobol dimensions");
+  }
+  PG_TRY_CUDA(sobol_dirs_.upload(vecs, (size_t)dim_bound * 32 * 4, stream_), "sobol dirs");
+  PG_TRY_CUDA(sobol_scramble_.upload(scr, (size_t)dim_bound * 4, stream_), "sobol scramble");
+  PG_TRY_CUDA(sobol_table_.ensure((size_t)dim_bound * count * 4), "sobol table");
+  PG_TRY_CUDA(launch_sobol_table(sobol_dirs_.as<uint32_t>(), sobol_scramble_.as<uint32_t>(),
+                                 dim_bound, count, sobol_table_.as<float>(), stream_),
+              "sobol kernel");
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "sobol sync");
+  sobol_bound_ = dim_bound;
+  sobol_count_ = count;
+  return Status::ok();
+}
+
+void Renderer::fill_params(RenderParams &p) const {
+  std::memset(&p, 0, sizeof(p));
+  p.tris = tris_.as<const float4>();
+  p.tri_data = tri_data_.as<const float4>();
+  p.bin_nodes = bin_nodes_.as<const uint4>();
+  p.extra_idxs = extra_.as<const uint32_t>();
+  p.wide_nodes = wide_nodes_.as<const uint4>();
+  p.wide_tris = wide_tris_.as<const float4>();
+  p.n_tris = prep_.n_tris;
+  p.n_bin_nodes = (uint32_t)prep_.bvh.nodes.size();
+  p.n_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  p.materials = materials_.as<const DevMaterial>();
+  p.light_tris = light_tris_.as<const float4>();
+  p.light_cdf = light_cdf_.as<const float>();
+  p.n_lights = prep_.n_lights;
+  p.status = status_.as<uint32_t>();
+  p.counters = counters_.as<unsigned long long>();
+}
+
+static Status check_settings(const path_settings &s) {
+  if (s.kernel_approach != PATH_KERNEL_MEGA && s.kernel_approach != PATH_KERNEL_STREAMING) {
+    return Status::err(PATH_ERR_ARGUMENT, "unknown kernel_approach");
+  }
+  if (s.rng != PATH_RNG_SOBEL) {
+    return Status::err(PATH_ERR_UNSUPPORTED,
+                       "only the Sobel RNG is built (Uniform draws cuRAND XORWOW / "
+                       "mt19937 streams that differ between the reference's CPU and GPU)");
+  }
+  if (s.light_sampler > PATH_LIGHT_NONE || s.dir_sampler > PATH_DIR_UNIFORM ||
+      s.term_prob > PATH_TERM_NORMALIZE || s.traversal > PATH_TRAVERSAL_WIDE8) {
+    return Status::err(PATH_ERR_ARGUMENT, "unknown sampler / term_prob / traversal value");
+  }
+  if (s.max_sample_size == 0) {
+    return Status::err(PATH_ERR_ARGUMENT, "max_sample_size must be positive");
+  }
+  if (s.target_objects == 0 || s.target_objects > 10) {
+    return Status::err(PATH_ERR_ARGUMENT, "target_objects must be in [1, 10]");
+  }
+  return Status::ok();
+}
+
+Status Renderer::render(const path_sample_spec &spec, const path_output &output,
+                        const Scene &scene, uint32_t spp, const path_settings &st,
+                        double *seconds) {
+  Status sc = check_settings(st);
+  if (!sc.good()) {
+    return sc;
+  }
+  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "only SquareImage sample specs are built");
+  }
+  if (spec.x_dim == 0 || spec.y_dim == 0 || spp == 0) {
+    return Status::err(PATH_ERR_ARGUMENT, "image size and samples_per must be positive");
+  }
+  if (output.data == nullptr ||
+      (output.type != PATH_OUTPUT_BGRA && output.type != PATH_OUTPUT_FLOAT_RGB)) {
+    return Status::err(PATH_ERR_ARGUMENT, "output buffer missing or unknown output type");
+  }
+  for (size_t i = 0; i < scene.tri_material.size(); ++i) {
+    if (scene.tri_material[i] >= scene.materials.size()) {
+      return Status::err(PATH_ERR_ARGUMENT, "triangle material index out of range");
+    }
+  }
+  Status s0 = init();
+  if (!s0.good()) {
+    return s0;
+  }
+  SBVHSettings sb;
+  sb.overlap_threshold = st.overlap_threshold;
+  sb.use_spatial_splits = st.use_spatial_splits != 0;
+  sb.traversal_per_intersect_cost = st.traversal_per_intersect_cost;
+  sb.target_objects = st.target_objects;
+  bool rebuilt = !(prep_.valid && prep_.scene_id == scene.id &&
+                   prep_.scene_version == scene.version &&
+                   prep_.sbvh.overlap_threshold == sb.overlap_threshold &&
+                   prep_.sbvh.use_spatial_splits == sb.use_spatial_splits &&
+                   prep_.sbvh.traversal_per_intersect_cost == sb.traversal_per_intersect_cost &&
+                   prep_.sbvh.target_objects == sb.target_objects);
+  if (rebuilt) {
+    FlatScene flat = flatten(scene);
+    Status sp = prepare_scene(flat, scene.id, scene.version, sb, true);
+    if (!sp.good()) {
+      return sp;
+    }
+    Status su = upload_geometry(flat, scene.materials);
+    if (!su.good()) {
+      return su;
+    }
+    prep_.valid = true;
+  }
+  if (st.traversal == PATH_TRAVERSAL_BINARY) {
+    if (prep_.bvh.depth + 2 > 64) {
+      return Status::err(PATH_ERR_UNSUPPORTED, "SBVH deeper than the 64-entry traversal stack");
+    }
+    if (st.target_objects + prep_.bvh.max_leaf_size - 1 > 10) {
+      return Status::err(PATH_ERR_UNSUPPORTED,
+                         "target_objects + max leaf size - 1 exceeds the 10 candidates");
+    }
+  }
+  uint64_t h2d = 0;
+  if (!rebuilt && st.upload_scene_every_render) {
+    Status sr = copy_staged(&h2d);
+    if (!sr.good()) {
+      return sr;
+    }
+  }
+  Status ss = prepare_sobol(st.max_sample_size, spp);
+  if (!ss.good()) {
+    return ss;
+  }
+  WorkDiv wd;
+  if (!make_workdiv(st.render_work_division, spp, spec.x_dim, spec.y_dim, wd)) {
+    return Status::err(PATH_ERR_ARGUMENT, "invalid render work division settings");
+  }
+  if (wd.block_size > 256) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "render block_size above 256");
+  }
+  const size_t n_pix = (size_t)spec.x_dim * spec.y_dim;
+  const bool bgra = output.type == PATH_OUTPUT_BGRA;
+  const uint32_t nsb = wd.num_sample_blocks;
+  float *direct_rgb = nullptr;
+  if (!bgra && nsb == 1 && output.on_device) {
+    direct_rgb = static_cast<float *>(output.data);
+  } else {
+    PG_TRY_CUDA(out_a_.ensure((size_t)nsb * n_pix * 3 * 4), "output buffer");
+  }
+  if (nsb > 1) {
+    PG_TRY_CUDA(out_b_.ensure((size_t)nsb * n_pix * 3 * 4), "reduce buffer");
+  }
+  if (bgra && !output.on_device) {
+    PG_TRY_CUDA(bgra_.ensure(n_pix * 4), "bgra buffer");
+  }
+  PG_TRY_CUDA(status_.ensure(4), "status word");
+  PG_TRY_CUDA(counters_.ensure(3 * 8), "counters");
+  PG_TRY_CUDA(cudaMemsetAsync(status_.get(), 0, 4, stream_), "status reset");
+  PG_TRY_CUDA(cudaMemsetAsync(counters_.get(), 0, 24, stream_), "counter reset");
+
+  RenderParams p;
+  fill_params(p);
+  p.sobol = sobol_table_.as<const float>();
+  p.dim_bound = st.max_sample_size;
+  p.init_dim_bound = std::min(64u, st.max_sample_size);
+  p.light_sampler = st.light_sampler;
+  p.dir_sampler = st.dir_sampler;
+  p.term_prob = st.term_prob;
+  p.term_iters = st.term_prob_iters;
+  p.term_prob_prob = st.term_prob_prob;
+  p.term_exp = st.term_prob_exp;
+  p.term_min_prob = st.term_prob_min_prob;
+  p.back_cull = st.back_cull_emission;
+  p.target_objects = st.target_objects;
+  std::memcpy(p.f2w, spec.film_to_world, sizeof(p.f2w));
+  p.x_dim = spec.x_dim;
+  p.y_dim = spec.y_dim;
+  p.spp = spp;
+  p.wd = wd;
+  p.out_rgb = direct_rgb ? direct_rgb : out_a_.as<float>();
+  uint8_t *bgra_dev = bgra ? (output.on_device ? static_cast<uint8_t *>(output.data)
+                                               : bgra_.as<uint8_t>())
+                           : nullptr;
+  p.out_bgra = bgra_dev;
+  p.output_bgra = bgra ? 1 : 0;
+  p.start_block = 0;
+
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "pre-render sync");
+  auto t0 = std::chrono::steady_clock::now();
+  uint32_t launches = 0;
+  PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
+  PG_TRY_CUDA(launch_render(p, st.traversal, wd.total_blocks(), st.count_work != 0, stream_),
+              "render kernel");
+  ++launches;
+  // ReduceFloatRGB passes
+  uint32_t factor = nsb;
+  float *in = p.out_rgb;
+  float *other = out_b_.as<float>();
+  size_t elems = (size_t)nsb * n_pix;
+  while (factor != 1) {
+    ReduceParams rp;
+    std::memset(&rp, 0, sizeof(rp));
+    uint32_t xd = (uint32_t)(elems / factor);
+    if (!make_workdiv(st.reduce_work_division, factor, xd, 1, rp.wd)) {
+      return Status::err(PATH_ERR_ARGUMENT, "invalid reduce work division settings");
+    }
+    rp.in = in;
+    rp.out = other;
+    rp.reduction_factor = factor;
+    rp.spp = spp;
+    rp.output_bgra = bgra ? 1 : 0;
+    rp.out_bgra = bgra_dev;
+    PG_TRY_CUDA(launch_reduce(rp, stream_), "reduce kernel");
+    ++launches;
+    factor = rp.wd.num_sample_blocks;
+    elems = (size_t)xd * factor;
+    std::swap(in, other);
+  }
+  PG_TRY_CUDA(cudaEventRecord(ev_stop_, stream_), "event");
+  if (bgra) {
+    if (!output.on_device) {
+      PG_TRY_CUDA(cudaMemcpyAsync(output.data, bgra_dev, n_pix * 4, cudaMemcpyDeviceToHost,
+                                  stream_),
+                  "output copy");
+    }
+  } else if (in != output.data) {
+    PG_TRY_CUDA(cudaMemcpyAsync(output.data, in, n_pix * 12,
+                                output.on_device ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyDeviceToHost,
+                                stream_),
+                "output copy");
+  }
+  uint64_t d2h = 0;
+  if (!output.on_device) {
+    d2h = bgra ? n_pix * 4 : n_pix * 12;
+  }
+  uint32_t status = 0;
+  unsigned long long counts[3] = {0, 0, 0};
+  PG_TRY_CUDA(cudaMemcpyAsync(&status, status_.get(), 4, cudaMemcpyDeviceToHost, stream_),
+              "status copy");
+  if (st.count_work) {
+    PG_TRY_CUDA(cudaMemcpyAsync(counts, counters_.get(), 24, cudaMemcpyDeviceToHost, stream_),
+                "counter copy");
+  }
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "render sync");
+  auto t1 = std::chrono::steady_clock::now();
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev_start_, ev_stop_);
+  stats_ = path_render_stats{};
+  stats_.seconds = std::chrono::duration<double>(t1 - t0).count();
+  stats_.kernel_ms = ms;
+  stats_.bvh_build_seconds = prep_.build_seconds;
+  stats_.rays_traced = counts[0];
+  stats_.nodes_visited = counts[1];
+  stats_.triangles_tested = counts[2];
+  stats_.gpu_launches = launches;
+  stats_.device_status = status;
+  stats_.num_bvh_nodes = (uint32_t)prep_.bvh.nodes.size();
+  stats_.num_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  stats_.h2d_bytes = h2d;
+  stats_.d2h_bytes = d2h;
+  if (seconds) {
+    *seconds = stats_.seconds;
+  }
+  if (status != 0) {
+    return Status::err(PATH_ERR_DEVICE_TIMEOUT,
+                       "kernel reported device status " + std::to_string(status) +
+                           " (1 stack overflow, 2 candidate overflow, 3 bad node)");
+  }
+  return Status::ok();
+}
+
+Status Renderer::intersect(const float *tris, uint32_t n_tris, const float *rays,
+                           uint32_t n_rays, const path_settings &st, int32_t *idx,
+                           float *t) {
+  Status s0 = init();
+  if (!s0.good()) {
+    return s0;
+  }
+  FlatScene flat;
+  for (uint32_t i = 0; i < n_tris; ++i) {
+    const float *p = tris + 9 * (size_t)i;
+    flat.v0.push_back(mk(p[0], p[1], p[2]));
+    flat.v1.push_back(mk(p[3], p[4], p[5]));
+    flat.v2.push_back(mk(p[6], p[7], p[8]));
+    flat.n0.push_back(mk(0.f, 0.f, 1.f));
+    flat.n1.push_back(mk(0.f, 0.f, 1.f));
+    flat.n2.push_back(mk(0.f, 0.f, 1.f));
+    flat.material.push_back(0);
+  }
+  SBVHSettings sb;
+  sb.overlap_threshold = st.overlap_threshold;
+  sb.use_spatial_splits = st.use_spatial_splits != 0;
+  sb.traversal_per_intersect_cost = st.traversal_per_intersect_cost;
+  sb.target_objects = st.target_objects;
+  prep_.valid = false;
+  Status sp = prepare_scene(flat, 0, 0, sb, true);
+  if (!sp.good()) {
+    return sp;
+  }
+  std::vector<path_material> mats(1);
+  std::memset(mats.data(), 0, sizeof(path_material));
+  Status su = upload_geometry(flat, mats);
+  if (!su.good()) {
+    return su;
+  }
+  DeviceBuffer d_rays, d_idx, d_t;
+  PG_TRY_CUDA(d_rays.upload(rays, (size_t)n_rays * 24, stream_), "rays");
+  PG_TRY_CUDA(d_idx.ensure((size_t)n_rays * 4), "idx");
+  PG_TRY_CUDA(d_t.ensure((size_t)n_rays * 4), "t");
+  PG_TRY_CUDA(status_.ensure(4), "status word");
+  PG_TRY_CUDA(counters_.ensure(24), "counters");
+  PG_TRY_CUDA(cudaMemsetAsync(status_.get(), 0, 4, stream_), "status reset");
+  RenderParams p;
+  fill_params(p);
+  p.target_objects = st.target_objects;
+  PG_TRY_CUDA(launch_intersect(p, st.traversal, d_rays.as<float>(), n_rays,
+                               perm_.as<uint32_t>(), d_idx.as<int32_t>(), d_t.as<float>(),
+                               stream_),
+              "intersect kernel");
+  uint32_t status = 0;
+  PG_TRY_CUDA(cudaMemcpyAsync(idx, d_idx.get(), (size_t)n_rays * 4, cudaMemcpyDeviceToHost,
+                              stream_),
+              "idx copy");
+  PG_TRY_CUDA(cudaMemcpyAsync(t, d_t.get(), (size_t)n_rays * 4, cudaMemcpyDeviceToHost, stream_),
+              "t copy");
+  PG_TRY_CUDA(cudaMemcpyAsync(&status, status_.get(), 4, cudaMemcpyDeviceToHost, stream_),
+              "status copy");
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "intersect sync");
+  if (status != 0) {
+    return Status::err(PATH_ERR_DEVICE_TIMEOUT,
+                       "kernel reported device status " + std::to_string(status));
+  }
+  return Status::ok();
+}
+
+} // namespace pg

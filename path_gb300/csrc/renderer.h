@@ -1,0 +1,115 @@
+// render::Renderer for the GPU execution model (host side).
+//
+// Owns a CUDA stream and device buffers, and caches the uploaded scene
+// (flattened triangles, SBVH, wide BVH, materials, light table) and the
+// Sobol table across calls, as Renderer::Impl caches its generators and
+// vectors (include/render/detail/renderer_impl.h:42-96).
+#pragma once
+
+#include "kernels.h"
+#include "scene.h"
+#include "sbvh.h"
+#include "wide.h"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace pg {
+
+class DeviceBuffer {
+public:
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  ~DeviceBuffer() { release(); }
+  cudaError_t ensure(size_t bytes);
+  cudaError_t upload(const void *src, size_t bytes, cudaStream_t s);
+  void release();
+  void *get() const { return ptr_; }
+  template <typename T> T *as() const { return static_cast<T *>(ptr_); }
+  size_t size() const { return size_; }
+
+private:
+  void *ptr_ = nullptr;
+  size_t size_ = 0;
+};
+
+// page-locked host staging buffer (fast host -> device copies)
+class PinnedBuffer {
+public:
+  PinnedBuffer() = default;
+  PinnedBuffer(const PinnedBuffer &) = delete;
+  PinnedBuffer &operator=(const PinnedBuffer &) = delete;
+  ~PinnedBuffer() { release(); }
+  cudaError_t ensure(size_t bytes);
+  void release();
+  void *get() const { return ptr_; }
+  template <typename T> T *as() const { return static_cast<T *>(ptr_); }
+  size_t bytes = 0; // bytes in use
+
+private:
+  void *ptr_ = nullptr;
+  size_t cap_ = 0;
+};
+
+struct Status {
+  path_status code = PATH_OK;
+  std::string message;
+  static Status ok() { return {}; }
+  static Status err(path_status c, std::string m) { return {c, std::move(m)}; }
+  bool good() const { return code == PATH_OK; }
+};
+
+Status cuda_status(cudaError_t e, const char *what);
+
+// host copies of the scene's device arrays (kept for tests and reuse)
+struct PreparedScene {
+  uint64_t scene_id = 0, scene_version = 0;
+  SBVHSettings sbvh;
+  bool valid = false;
+  BinaryBVH bvh;
+  WideBVH wide;
+  uint32_t n_tris = 0, n_lights = 0;
+  double build_seconds = 0.0;
+};
+
+class Renderer {
+public:
+  Renderer();
+  ~Renderer();
+
+  Status render(const path_sample_spec &spec, const path_output &output,
+                const Scene &scene, uint32_t spp, const path_settings &settings,
+                double *seconds);
+  Status intersect(const float *tris, uint32_t n_tris, const float *rays,
+                   uint32_t n_rays, const path_settings &settings, int32_t *idx,
+                   float *t);
+  const path_render_stats &stats() const { return stats_; }
+
+private:
+  Status init();
+  Status prepare_scene(const FlatScene &flat, uint64_t id, uint64_t version,
+                       const SBVHSettings &sbvh, bool force);
+  Status upload_geometry(const FlatScene &flat, const std::vector<path_material> &mats);
+  Status copy_staged(uint64_t *bytes);
+  Status prepare_sobol(uint32_t dim_bound, uint32_t count);
+  void fill_params(RenderParams &p) const;
+
+  bool initialised_ = false;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
+  PreparedScene prep_;
+  DeviceBuffer tris_, tri_data_, bin_nodes_, extra_, wide_nodes_, wide_tris_,
+      materials_, light_tris_, light_cdf_, perm_;
+  // pinned host copies of the device arrays above, in the same order
+  PinnedBuffer st_tris_, st_data_, st_nodes_, st_extra_, st_wnodes_, st_wtris_, st_mats_,
+      st_lights_, st_cdf_, st_perm_;
+  DeviceBuffer sobol_dirs_, sobol_scramble_, sobol_table_;
+  uint32_t sobol_bound_ = 0, sobol_count_ = 0;
+  DeviceBuffer out_a_, out_b_, bgra_, status_, counters_;
+  path_render_stats stats_{};
+};
+
+} // namespace pg

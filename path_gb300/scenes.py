@@ -1,0 +1,257 @@
+"""Seeded synthetic scenes of the render-path workloads.
+
+* ``cornell_box``: the small Cornell box -- 36 triangles: five walls of two
+  triangles over [-1, 1]^3 with the front (+z) open, a 0.5 x 0.5 ceiling light
+  (emission 15) facing down, and two boxes 0.6 and 1.2 tall rotated +-18
+  degrees about y; Lambertian white 0.73, red (0.65, 0.05, 0.05) and green
+  (0.12, 0.45, 0.15); pinhole camera at z = 3.5 with a 40 degree vertical
+  field of view.
+* ``large_mesh_room``: the same room and light holding an icosphere
+  subdivided ``subdivisions`` times (8 -> 1,310,720 triangles) with radial
+  displacement by 4-octave value noise (amplitude 0.08, seed 1) and a GGX
+  material (roughness 0.2, F0 0.04), beside a latitude-longitude glass
+  sphere of about 20k triangles (dielectric, IOR 1.5).
+
+Triangles are wound so that face normals point into the room (walls) or out
+of the objects; the light faces down so back-face culled emission is seen
+from below.  All geometry is generated here; no third-party asset is used.
+"""
+
+import math
+
+import numpy as np
+
+from . import api
+
+WHITE = (0.73, 0.73, 0.73)
+RED = (0.65, 0.05, 0.05)
+GREEN = (0.12, 0.45, 0.15)
+LIGHT_EMISSION = (15.0, 15.0, 15.0)
+
+
+def _quad(a, b, c, d):
+    """Two triangles (a, b, c), (a, c, d); normal = (b - a) x (c - a)."""
+    return [np.array([a, b, c], np.float32), np.array([a, c, d], np.float32)]
+
+
+def room_triangles():
+    """Walls [-1, 1]^3 (front open) and the ceiling light, inward facing."""
+    p = lambda x, y, z: (x, y, z)  # noqa: E731
+    walls = {
+        "floor": _quad(p(-1, -1, -1), p(-1, -1, 1), p(1, -1, 1), p(1, -1, -1)),
+        "ceiling": _quad(p(-1, 1, -1), p(1, 1, -1), p(1, 1, 1), p(-1, 1, 1)),
+        "back": _quad(p(-1, -1, -1), p(1, -1, -1), p(1, 1, -1), p(-1, 1, -1)),
+        "left": _quad(p(-1, -1, -1), p(-1, 1, -1), p(-1, 1, 1), p(-1, -1, 1)),
+        "right": _quad(p(1, -1, -1), p(1, -1, 1), p(1, 1, 1), p(1, 1, -1)),
+    }
+    h = 0.25
+    y = 0.999
+    light = _quad(p(-h, y, -h), p(h, y, -h), p(h, y, h), p(-h, y, h))
+    return walls, light
+
+
+def _box(width, height, depth, angle_deg, centre_xz):
+    """Axis box on the floor (y = -1) rotated about y; outward normals."""
+    w, d = width / 2, depth / 2
+    y0, y1 = -1.0, -1.0 + height
+    a = math.radians(angle_deg)
+    ca, sa = math.cos(a), math.sin(a)
+    cx, cz = centre_xz
+
+    def v(x, y, z):
+        return (cx + ca * x + sa * z, y, cz - sa * x + ca * z)
+
+    c = [v(-w, y0, -d), v(w, y0, -d), v(w, y0, d), v(-w, y0, d),
+         v(-w, y1, -d), v(w, y1, -d), v(w, y1, d), v(-w, y1, d)]
+    faces = [
+        (c[0], c[1], c[2], c[3]),  # bottom, normal -y
+        (c[4], c[7], c[6], c[5]),  # top, +y
+        (c[0], c[4], c[5], c[1]),  # -z
+        (c[3], c[2], c[6], c[7]),  # +z
+        (c[0], c[3], c[7], c[4]),  # -x
+        (c[1], c[5], c[6], c[2]),  # +x
+    ]
+    out = []
+    for f in faces:
+        out += _quad(*f)
+    return np.stack(out)
+
+
+def cornell_camera(x_dim, y_dim):
+    return api.camera_transform((0, 0, -1), (0, 1, 0), (0, 0, 3.5), 40.0, x_dim / y_dim)
+
+
+def _add_room(scene, with_boxes):
+    white = scene.add_material(api.material("Diffuse", diffuse=WHITE))
+    red = scene.add_material(api.material("Diffuse", diffuse=RED))
+    green = scene.add_material(api.material("Diffuse", diffuse=GREEN))
+    light = scene.add_material(api.material("Diffuse", diffuse=(0.78, 0.78, 0.78),
+                                            emission=LIGHT_EMISSION))
+    walls, light_tris = room_triangles()
+    tris, mats = [], []
+    for name, ts in walls.items():
+        m = red if name == "left" else green if name == "right" else white
+        tris += ts
+        mats += [m] * len(ts)
+    tris += light_tris
+    mats += [light] * len(light_tris)
+    if with_boxes:
+        short = _box(0.6, 0.6, 0.6, -18.0, (0.33, 0.37))
+        tall = _box(0.6, 1.2, 0.6, 18.0, (-0.33, -0.3))
+        for b in (short, tall):
+            tris += list(b)
+            mats += [white] * len(b)
+    scene.add_mesh(np.stack(tris).reshape(-1, 9), np.array(mats, np.uint32))
+    return white
+
+
+def cornell_box():
+    """The 36-triangle Cornell box; returns (scene, camera builder)."""
+    scene = api.Scene()
+    _add_room(scene, with_boxes=True)
+    return scene
+
+
+# ---------------------------------------------------------------------------
+# procedural meshes
+
+def icosphere(subdivisions):
+    """Unit icosphere by repeated midpoint subdivision (20 * 4^n triangles)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0],
+                      [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                      [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    verts /= np.linalg.norm(verts, axis=1, keepdims=True)
+    faces = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
+                      [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
+                      [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
+                      [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], np.int64)
+    for _ in range(subdivisions):
+        a, b, c = faces[:, 0], faces[:, 1], faces[:, 2]
+        edges = np.concatenate([np.stack([a, b], 1), np.stack([b, c], 1), np.stack([c, a], 1)])
+        key = np.sort(edges, axis=1)
+        uniq, inv = np.unique(key[:, 0] * (len(verts) + 1) + key[:, 1], return_inverse=True)
+        e0 = uniq // (len(verts) + 1)
+        e1 = uniq % (len(verts) + 1)
+        mids = verts[e0] + verts[e1]
+        mids /= np.linalg.norm(mids, axis=1, keepdims=True)
+        base = len(verts)
+        verts = np.concatenate([verts, mids])
+        nf = len(faces)
+        ab = base + inv[:nf]
+        bc = base + inv[nf:2 * nf]
+        ca = base + inv[2 * nf:]
+        faces = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1),
+                                np.stack([c, ca, bc], 1), np.stack([ab, bc, ca], 1)])
+    return verts, faces
+
+
+def _hash3(ix, iy, iz, seed):
+    """Integer lattice hash to [-1, 1] (MurmurHash3's 32-bit finaliser)."""
+    h = (ix.astype(np.uint32) * np.uint32(0x8DA6B343)) ^ \
+        (iy.astype(np.uint32) * np.uint32(0xD8163841)) ^ \
+        (iz.astype(np.uint32) * np.uint32(0xCB1AB31F)) ^ np.uint32(seed * 0x9E3779B9 & 0xffffffff)
+    h ^= h >> np.uint32(16)
+    h *= np.uint32(0x85EBCA6B)
+    h ^= h >> np.uint32(13)
+    h *= np.uint32(0xC2B2AE35)
+    h ^= h >> np.uint32(16)
+    return h.astype(np.float64) / 4294967295.0 * 2.0 - 1.0
+
+
+def value_noise(p, seed, octaves=4, base_frequency=2.0):
+    """Fractal value noise in [-1, 1]: smoothstep-interpolated lattice values,
+    frequency doubling and amplitude halving per octave."""
+    total = np.zeros(len(p))
+    norm = 0.0
+    amp = 1.0
+    freq = base_frequency
+    with np.errstate(over="ignore"):
+        for o in range(octaves):
+            q = p * freq
+            i = np.floor(q).astype(np.int64)
+            f = q - i
+            w = f * f * (3.0 - 2.0 * f)
+            acc = np.zeros(len(p))
+            for dx in (0, 1):
+                for dy in (0, 1):
+                    for dz in (0, 1):
+                        val = _hash3(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz, seed + 7919 * o)
+                        wx = w[:, 0] if dx else 1 - w[:, 0]
+                        wy = w[:, 1] if dy else 1 - w[:, 1]
+                        wz = w[:, 2] if dz else 1 - w[:, 2]
+                        acc += val * wx * wy * wz
+            total += amp * acc
+            norm += amp
+            amp *= 0.5
+            freq *= 2.0
+    return total / norm
+
+
+def _vertex_normals(verts, faces):
+    fn = np.cross(verts[faces[:, 1]] - verts[faces[:, 0]], verts[faces[:, 2]] - verts[faces[:, 0]])
+    vn = np.zeros_like(verts)
+    for k in range(3):
+        np.add.at(vn, faces[:, k], fn)
+    return vn / np.linalg.norm(vn, axis=1, keepdims=True)
+
+
+def displaced_icosphere(subdivisions=8, radius=0.5, centre=(0.35, -0.4, -0.25),
+                        amplitude=0.08, seed=1):
+    verts, faces = icosphere(subdivisions)
+    disp = radius + amplitude * value_noise(verts, seed)
+    pos = verts * disp[:, None] + np.asarray(centre)
+    normals = _vertex_normals(pos, faces)
+    tris = pos[faces].reshape(-1, 9).astype(np.float32)
+    nrm = normals[faces].reshape(-1, 9).astype(np.float32)
+    return tris, nrm
+
+
+def uv_sphere(n_lat=100, n_lon=100, radius=0.3, centre=(-0.45, -0.7, 0.3)):
+    """Latitude-longitude sphere with analytic vertex normals (outward)."""
+    th = np.linspace(0, np.pi, n_lat + 1)
+    ph = np.linspace(0, 2 * np.pi, n_lon + 1)
+    tris, nrm = [], []
+    c = np.asarray(centre)
+
+    def unit(t, p):
+        return np.array([np.sin(t) * np.cos(p), np.cos(t), np.sin(t) * np.sin(p)])
+
+    for i in range(n_lat):
+        for j in range(n_lon):
+            a, b = unit(th[i], ph[j]), unit(th[i], ph[j + 1])
+            cc, d = unit(th[i + 1], ph[j + 1]), unit(th[i + 1], ph[j])
+            if i > 0:
+                tris.append([a, b, d])
+            if i < n_lat - 1:
+                tris.append([b, cc, d])
+    n = np.array(tris)
+    # wind outward: normal must agree with the position direction
+    fn = np.cross(n[:, 1] - n[:, 0], n[:, 2] - n[:, 0])
+    flip = np.einsum("ij,ij->i", fn, n.mean(axis=1)) < 0
+    n[flip] = n[flip][:, ::-1]
+    pos = n * radius + c
+    return pos.reshape(-1, 9).astype(np.float32), n.reshape(-1, 9).astype(np.float32)
+
+
+def large_mesh_room(subdivisions=8, glass_lat=100, glass_lon=100):
+    """Room + light, displaced GGX icosphere and a glass sphere."""
+    scene = api.Scene()
+    _add_room(scene, with_boxes=False)
+    ggx = scene.add_material(api.material("GGX", specular=(0.04, 0.04, 0.04), roughness=0.2))
+    glass = scene.add_material(api.material("DielectricRefractive", specular=(1, 1, 1), ior=1.5))
+    tris, nrm = displaced_icosphere(subdivisions)
+    scene.add_mesh(tris, np.full(len(tris), ggx, np.uint32), normals=nrm)
+    gt, gn = uv_sphere(glass_lat, glass_lon)
+    scene.add_mesh(gt, np.full(len(gt), glass, np.uint32), normals=gn)
+    return scene
+
+
+def path_settings(max_depth, traversal="wide"):
+    """Settings for 'max depth D, no Russian roulette, Sobol': NIters{D-1}."""
+    s = api.Settings()
+    s.set_term_prob("NIters", iters=max_depth - 1)
+    s.max_sample_size = 256
+    s.back_cull_emission = 1
+    s.traversal = 1 if traversal == "wide" else 0
+    return s

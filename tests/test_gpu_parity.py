@@ -1,0 +1,236 @@
+"""Parity of the CUDA render path with the CPU oracle (GPU tests).
+
+Tolerances: Sobol values, transcendental functions, closest-hit ids (except
+exact-distance ties) and images rendered with the binary traversal are
+compared bit for bit; images through the 8-wide traversal may differ only
+where two triangles are hit at exactly the same distance, and must stay
+within 1e-4 relative RMSE (||gpu - oracle||_2 / ||oracle||_2 over all
+pixel channels), the bar the render path is held to.
+"""
+
+import numpy as np
+import pytest
+
+from path_gb300 import api, scenes
+from oracle import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+RMSE_TOL = 1e-4
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.mark.parametrize("count", [16, 64, 1024, 4096])
+def test_sobol_bit_exact_against_curand_and_oracle(lib, oracle, count):
+    ours = api.sobol_table(256, count)
+    curand = api.sobol_table(256, count, use_curand=True)
+    host = ol.sobol_table(256, count)
+    assert np.array_equal(bits(ours), bits(curand))
+    assert np.array_equal(bits(ours), bits(host))
+
+
+def test_pmath_gpu_equals_host(lib, oracle):
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.uniform(-7, 7, 200000), [0.0, -0.0, np.pi, -np.pi, 1e-30]]).astype(np.float32)
+    a = np.concatenate([rng.uniform(-1, 1, 200000), [1.0, -1.0, 0.5, -0.5, 0.0]]).astype(np.float32)
+    b = rng.uniform(0, 1, a.size).astype(np.float32)
+    e = rng.uniform(0, 100, a.size).astype(np.float32)
+    for fn in (0, 1):
+        assert np.array_equal(bits(api.debug_pmath(fn, x)), bits(ol.pmath(fn, x)))
+    for fn in (2, 3):
+        assert np.array_equal(bits(api.debug_pmath(fn, a)), bits(ol.pmath(fn, a)))
+    assert np.array_equal(bits(api.debug_pmath(4, b, e)), bits(ol.pmath(4, b, e)))
+
+
+def _random_rays(rng, lo, hi, n):
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.uniform(lo, hi, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_closest_hit_matches_oracle(lib, oracle, traversal):
+    rng = np.random.default_rng(21)
+    r = api.Renderer()
+    s = api.Settings()
+    s.traversal = traversal
+    cases = []
+    for n in (1, 4, 37, 100, 5000):
+        cases.append((rng.uniform(-1, 1, (n, 9)).astype(np.float32),
+                      _random_rays(rng, -1, 1, 4096)))
+    tris, _ = scenes.displaced_icosphere(5)
+    o = np.tile([0.0, 0.0, 3.5], (20000, 1))
+    d = rng.normal(size=(20000, 3)) * [0.3, 0.3, 0.0] + [0.35, -0.4, -3.75]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    cases.append((tris, np.concatenate([o, d], 1).astype(np.float32)))
+    for tris, rays in cases:
+        want, wt = ol.loop_all(tris, rays)
+        got, gt = r.intersect(tris, rays, s)
+        assert np.array_equal(want >= 0, got >= 0)
+        hit = want >= 0
+        tie = np.abs(wt - gt) <= 1e-6
+        assert np.all((want == got) | (hit & tie))
+        assert np.array_equal(bits(wt[hit]), bits(gt[hit]))
+
+
+def _render_gpu(scene, settings, spp, w, h, f2w, bgra=False):
+    out = np.zeros((h, w, 4), np.uint8) if bgra else np.zeros((h, w, 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), out, scene, spp, settings)
+    assert r.stats()["device_status"] == 0
+    return out
+
+
+def _render_oracle(scene, settings, spp, w, h, f2w, rows=None):
+    arr = ol.SceneArrays(scene.export())
+    img, _ = ol.render(arr, ol.settings_from(settings, reduce_order=1), spp, w, h, f2w, rows)
+    return img
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_cornell_bit_exact(lib, oracle, traversal):
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "wide" if traversal else "binary")
+    f2w = scenes.cornell_camera(64, 64)
+    gpu = _render_gpu(sc, s, 16, 64, 64, f2w)
+    ref = _render_oracle(sc, s, 16, 64, 64, f2w)
+    assert rel_rmse(gpu, ref) <= RMSE_TOL
+    if traversal == 0:
+        assert np.array_equal(bits(gpu), bits(ref))
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_cornell_full_size(lib, oracle, traversal):
+    # the small-Cornell workload: 256 x 256, 16 spp, max depth 5
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "wide" if traversal else "binary")
+    f2w = scenes.cornell_camera(256, 256)
+    gpu = _render_gpu(sc, s, 16, 256, 256, f2w)
+    ref = _render_oracle(sc, s, 16, 256, 256, f2w)
+    err = rel_rmse(gpu, ref)
+    print(f"cornell 256x256x16 traversal={traversal} rel RMSE vs oracle {err:.3e}")
+    assert err <= RMSE_TOL
+    assert 0.15 < float(gpu.mean()) < 0.6
+
+
+def test_cornell_bgra(lib, oracle):
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "binary")
+    f2w = scenes.cornell_camera(48, 40)
+    gpu = _render_gpu(sc, s, 8, 48, 40, f2w, bgra=True)
+    arr = ol.SceneArrays(sc.export())
+    ref = ol.render_bgra(arr, ol.settings_from(s, reduce_order=1), 8, 48, 40, f2w)
+    assert np.array_equal(gpu, ref)
+
+
+def _settings_variants():
+    out = []
+    s = scenes.path_settings(5, "binary")
+    s.set_term_prob("MultiplierFunc", exp=50.0, min_prob=0.1)
+    out.append(("multiplier_func", s))
+    s = scenes.path_settings(4, "binary")
+    s.set_term_prob("Normalize", min_prob=0.1)
+    out.append(("normalize", s))
+    s = scenes.path_settings(4, "binary")
+    s.set_term_prob("Constant", prob=0.3)
+    out.append(("constant", s))
+    s = scenes.path_settings(5, "binary")
+    s.light_sampler = 1
+    out.append(("no_light_sampling", s))
+    s = scenes.path_settings(5, "binary")
+    s.dir_sampler = 1
+    out.append(("uniform_dir", s))
+    s = scenes.path_settings(5, "binary")
+    s.back_cull_emission = 0
+    out.append(("no_back_cull", s))
+    # several sample blocks per pixel: exercises the second reduction stage
+    s = scenes.path_settings(5, "binary")
+    s.render_work_division.block_size = 32
+    s.render_work_division.force_target_samples = 1
+    s.render_work_division.forced_target_samples_per_thread = 1
+    out.append(("sample_blocks", s))
+    return out
+
+
+@pytest.mark.parametrize("name,settings", _settings_variants())
+def test_settings_variants_match(lib, oracle, name, settings):
+    sc = scenes.cornell_box()
+    f2w = scenes.cornell_camera(32, 32)
+    spp = 128 if name == "sample_blocks" else 16
+    gpu = _render_gpu(sc, settings, spp, 32, 32, f2w)
+    ref = _render_oracle(sc, settings, spp, 32, 32, f2w)
+    assert np.array_equal(bits(gpu), bits(ref)), (name, rel_rmse(gpu, ref))
+
+
+def _material_zoo_scene():
+    sc = api.Scene()
+    mats = [
+        api.material("Diffuse", diffuse=(0.7, 0.7, 0.7)),
+        api.material("Glossy", specular=(0.8, 0.6, 0.4), shininess=40.0),
+        api.material("DiffuseGlossy", diffuse=(0.5, 0.3, 0.3), specular=(0.4, 0.4, 0.4),
+                     shininess=20.0, diffuse_weight=0.6, glossy_weight=0.4),
+        api.material("DiffuseMirror", diffuse=(0.3, 0.5, 0.3), specular=(0.9, 0.9, 0.9),
+                     diffuse_weight=0.5, glossy_weight=0.5),
+        api.material("Mirror", specular=(0.9, 0.9, 0.9)),
+        api.material("DielectricRefractive", specular=(1, 1, 1), ior=1.5),
+        api.material("GGX", specular=(0.9, 0.6, 0.3), roughness=0.3),
+        api.material("Diffuse", diffuse=(0.78, 0.78, 0.78), emission=(12, 12, 12)),
+    ]
+    ids = [sc.add_material(m) for m in mats]
+    walls, light = scenes.room_triangles()
+    tris = np.stack([t for ts in walls.values() for t in ts] + light).reshape(-1, 9)
+    mat = np.array([ids[0]] * 10 + [ids[7]] * 2, np.uint32)
+    sc.add_mesh(tris, mat)
+    for k, m in enumerate(ids[1:7]):
+        cx = -0.6 + 0.4 * (k % 4)
+        cz = -0.4 + 0.6 * (k // 4)
+        gt, gn = scenes.uv_sphere(12, 16, radius=0.17, centre=(cx, -0.8, cz))
+        sc.add_mesh(gt, np.full(len(gt), m, np.uint32), normals=gn)
+    return sc
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_material_zoo_matches(lib, oracle, traversal):
+    sc = _material_zoo_scene()
+    s = scenes.path_settings(6, "wide" if traversal else "binary")
+    f2w = scenes.cornell_camera(48, 48)
+    gpu = _render_gpu(sc, s, 16, 48, 48, f2w)
+    ref = _render_oracle(sc, s, 16, 48, 48, f2w)
+    assert rel_rmse(gpu, ref) <= RMSE_TOL
+    if traversal == 0:
+        assert np.array_equal(bits(gpu), bits(ref))
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_large_mesh_small_case(lib, oracle, traversal):
+    sc = scenes.large_mesh_room(subdivisions=5, glass_lat=40, glass_lon=40)
+    s = scenes.path_settings(8, "wide" if traversal else "binary")
+    f2w = scenes.cornell_camera(64, 64)
+    gpu = _render_gpu(sc, s, 8, 64, 64, f2w)
+    ref = _render_oracle(sc, s, 8, 64, 64, f2w)
+    err = rel_rmse(gpu, ref)
+    print(f"large mesh (20480 tris) traversal={traversal} rel RMSE {err:.3e}")
+    assert err <= RMSE_TOL
+
+
+def test_device_output_equals_host_output(lib):
+    torch = pytest.importorskip("torch")
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5)
+    f2w = scenes.cornell_camera(64, 64)
+    host = _render_gpu(sc, s, 16, 64, 64, f2w)
+    dev = torch.zeros((64, 64, 3), dtype=torch.float32, device="cuda")
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.SquareImage(64, 64, f2w), dev, sc, 16, s)
+    torch.cuda.synchronize()
+    assert np.array_equal(bits(dev.cpu().numpy()), bits(host))
