@@ -1395,6 +1395,11 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
   };
 
   while (true) {
+    // safety bound shared with the kernels (no counterpart in the reference;
+    // no path of the tested settings reaches it)
+    if (iters >= 4096) {
+      return total;
+    }
     // intersect all pending rays (light ray first, then the next ray)
     Hit light_hit, next_hit;
     if (has_light) {

@@ -66,6 +66,13 @@ enum DeviceStatus : uint32_t {
   kStatusStackOverflow = 1,
   kStatusObjectsOverflow = 2,
   kStatusBadNode = 3,
+  kStatusPathTooLong = 4,
 };
+
+// Safety bound on the vertices of one path.  The reference loops until the
+// termination draw ends the path; a bound keeps a kernel from spinning if a
+// termination setting never ends a path.  No path of the built settings
+// comes near it (NIters ends a path after iters + 1 vertices).
+constexpr uint32_t kMaxPathVertices = 4096;
 
 } // namespace pg

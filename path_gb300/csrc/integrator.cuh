@@ -760,6 +760,10 @@ __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
   const bool cull = P.back_cull != 0;
 
   while (true) {
+    if (iters >= kMaxPathVertices) {
+      set_status(P.status, kStatusPathTooLong);
+      return total;
+    }
     Hit lh = no_hit(), nh = no_hit();
     if (has_light) {
       lh = trace<kTrav, kCount>(P, light_ray, cnt);

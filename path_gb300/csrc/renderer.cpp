@@ -530,7 +530,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   if (status != 0) {
     return Status::err(PATH_ERR_DEVICE_TIMEOUT,
                        "kernel reported device status " + std::to_string(status) +
-                           " (1 stack overflow, 2 candidate overflow, 3 bad node)");
+                           " (1 stack overflow, 2 candidate overflow, 3 bad node, 4 path too long)");
   }
   return Status::ok();
 }
