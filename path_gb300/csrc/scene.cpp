@@ -139,10 +139,4 @@ affine camera_transform(f3 look, f3 up, f3 pos, float height_angle_deg,
   return out;
 }
 
-bool load_scene_xml(const std::string &path, float, Scene &, affine &,
-                    std::string &err) {
-  err = "XML scene loading is not built yet: " + path;
-  return false;
-}
-
 } // namespace pg

@@ -1,0 +1,90 @@
+"""Scene-file loader (CS123 XML + OBJ/MTL), host side."""
+
+import os
+
+import numpy as np
+import pytest
+
+from path_gb300 import api, capi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "scenes", "room.xml")
+REFERENCE_SCENES = "/root/reference/scenes"
+
+
+def test_fixture_scene(lib):
+    sc, f2w = api.Scene.load_xml(FIXTURE, 1.0)
+    z = sc.sizes()
+    assert z == {"triangles": 13, "meshes": 1, "instances": 2, "clusters": 2, "materials": 6}
+    ex = sc.export()
+    types = [ex["materials"][i].type for i in range(6)]
+    B = capi.BSDF
+    assert types == [B["Diffuse"], B["Diffuse"], B["Diffuse"], B["DiffuseGlossy"], B["Mirror"],
+                     B["DielectricRefractive"]]
+    lamp = ex["materials"][2]
+    assert list(lamp.emission) == [10, 8, 6]
+    shiny = ex["materials"][3]
+    wd = 0.9 / (0.9 + 1.2)
+    assert abs(shiny.diffuse_weight - wd) < 1e-6 and abs(shiny.shininess - 30) < 1e-6
+    assert abs(ex["materials"][5].ior - 1.45) < 1e-6
+    # emissive clusters: the lamp quad (triangles 4, 5) and the lamp triangle (10)
+    assert ex["clusters"].tolist() == [[2, 4, 6], [2, 10, 11]]
+    # the concave hexagon is cut into 4 triangles covering its 0.2 area
+    t = ex["triangles"].reshape(-1, 3, 3)
+    hexa = t[6:10]
+    areas = 0.5 * np.linalg.norm(np.cross(hexa[:, 1] - hexa[:, 0], hexa[:, 2] - hexa[:, 0]), axis=1)
+    assert abs(areas.sum() - 0.2) < 1e-6
+    # normals from vn for the lamp quad, face normals elsewhere
+    n = ex["normals"].reshape(-1, 3, 3)
+    np.testing.assert_allclose(n[4:6].reshape(-1, 3), np.tile([0, -1, 0], (6, 1)))
+    # second instance: translate (3, 0, 0) then rotate 90 degrees about y
+    x = ex["instance_xforms"][1].reshape(3, 4)
+    np.testing.assert_allclose(x[:, :3], [[0, 0, 1], [0, 1, 0], [-1, 0, 0]], atol=1e-6)
+    np.testing.assert_allclose(x[:, 3], [3, 0, 0], atol=1e-6)
+    # camera from the focus point
+    np.testing.assert_allclose(f2w.reshape(3, 4)[:, 3], [0, 1, 4], atol=1e-6)
+
+
+def test_loader_errors(lib, tmp_path):
+    with pytest.raises(capi.PathError) as e:
+        api.Scene.load_xml(str(tmp_path / "missing.xml"), 1.0)
+    assert e.value.status == 7
+    bad = tmp_path / "bad.xml"
+    bad.write_text("<scenefile><object type='tree' name='root'><transblock>"
+                   "<object type='primitive' name='sphere'/></transblock></object></scenefile>")
+    with pytest.raises(capi.PathError) as e:
+        api.Scene.load_xml(str(bad), 1.0)
+    assert e.value.status == 2
+    light = tmp_path / "light.xml"
+    light.write_text("<scenefile><lightdata/></scenefile>")
+    with pytest.raises(capi.PathError) as e:
+        api.Scene.load_xml(str(light), 1.0)
+    assert e.value.status == 2
+    mtl = tmp_path / "m.mtl"
+    mtl.write_text("newmtl x\nillum 4\nKd 1 1 1\n")
+    (tmp_path / "m.obj").write_text("mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nusemtl x\nf 1 2 3\n")
+    xml = tmp_path / "m.xml"
+    xml.write_text("<scenefile><object type='tree' name='root'><transblock>"
+                   "<object type='primitive' name='mesh' filename='m.obj'/></transblock>"
+                   "</object></scenefile>")
+    with pytest.raises(capi.PathError) as e:
+        api.Scene.load_xml(str(xml), 1.0)
+    assert "illum" in str(e.value)
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_SCENES), reason="reference scenes not mounted")
+def test_reference_scenes_load(lib):
+    loaded = 0
+    for name in sorted(os.listdir(REFERENCE_SCENES)):
+        if not name.endswith(".xml"):
+            continue
+        try:
+            sc, f2w = api.Scene.load_xml(os.path.join(REFERENCE_SCENES, name), 1.0)
+        except capi.PathError as e:
+            # only failures the reference itself reports are acceptable
+            assert any(k in str(e) for k in ("illum", "light", "primitive", "cannot open")), (name, e)
+            continue
+        z = sc.sizes()
+        assert z["triangles"] > 0, name
+        loaded += 1
+    assert loaded >= 5
