@@ -281,6 +281,31 @@ path_status path_work_division(const path_work_division_settings *settings,
 /* number of GPUs visible and the library's build string */
 const char *path_version(void);
 
+/* ---- render without device allocation (no counterpart in the reference) ----
+ * Some callers cannot call cudaMalloc: a host framework that owns all device
+ * memory through its own allocator and forbids raw allocations, or a real-time
+ * loop that must not allocate after start-up because cudaMalloc / cudaFree can
+ * synchronise the whole device.  path_render_noalloc renders like path_render
+ * but allocates nothing: its scratch (the status word, work counters and the
+ * per-sample-block partial sums with their reduction buffer) lives in one
+ * file-scope device array of PATH_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * the library holds until the process exits.  Requirements:
+ *   - the scene is already resident on this renderer: an earlier path_render
+ *     with the same scene, SBVH settings, max_sample_size and samples_per;
+ *   - output->on_device is set (the image is written to caller device memory);
+ *   - partial sums that do not fit the array are rejected with
+ *     PATH_ERR_ARGUMENT (the message gives the bytes needed).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture
+ * begins.  All calls share the one array: calls whose GPU work overlaps in
+ * time race on it, so issue them one after another. */
+#define PATH_NOALLOC_SCRATCH_BYTES (32u << 20)
+path_status path_render_noalloc(path_renderer *renderer,
+                                const path_sample_spec *sample_spec,
+                                const path_output *output,
+                                const path_scene *scene, uint32_t samples_per,
+                                const path_settings *settings, double *seconds);
+
 #ifdef __cplusplus
 }
 #endif

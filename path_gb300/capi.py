@@ -111,6 +111,9 @@ SIGNATURES = {
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),
+    "path_render_noalloc": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), ctypes.POINTER(Output),
+                                           _P, c_u32, ctypes.POINTER(PathSettings),
+                                           ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None

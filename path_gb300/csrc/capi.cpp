@@ -58,6 +58,14 @@ pg::f3 load3(const float *p) { return pg::mk(p[0], p[1], p[2]); }
 
 } // namespace
 
+namespace pg {
+// records the message path_last_error() returns (for entry points defined in
+// other translation units)
+path_status record_status(const Status &s) { return from(s); }
+pg::Renderer &renderer_of(path_renderer *r) { return r->r; }
+const pg::Scene &scene_of(const path_scene *s) { return s->s; }
+} // namespace pg
+
 extern "C" {
 
 const char *path_last_error(void) { return g_last_error.c_str(); }

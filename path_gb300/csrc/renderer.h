@@ -87,6 +87,11 @@ public:
                    uint32_t n_rays, const path_settings &settings, int32_t *idx,
                    float *t);
   const path_render_stats &stats() const { return stats_; }
+  // render that allocates nothing; scratch is device memory the caller owns
+  // (defined in noalloc.cu)
+  Status render_noalloc(const path_sample_spec &spec, const path_output &output,
+                        const Scene &scene, uint32_t spp, const path_settings &settings,
+                        void *scratch, size_t scratch_bytes, double *seconds);
 
 private:
   Status init();
