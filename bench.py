@@ -110,19 +110,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(name):
+def make_workload(name, size=None, spp_override=None):
     from path_gb300 import scenes
     if name == "large_mesh":
         scene = scenes.large_mesh_room(subdivisions=8)
-        w = h = 1024
-        spp, depth = 64, 8
+        w = h = size or 1024
+        spp, depth = spp_override or 64, 8
         desc = ("large-mesh room: 1,310,720-tri displaced icosphere (GGX a=0.2 F0=0.04) + "
-                "19,800-tri glass sphere (IOR 1.5), 1024x1024, 64 spp, depth 8")
+                f"19,800-tri glass sphere (IOR 1.5), {w}x{h}, {spp} spp, depth 8")
     else:
         scene = scenes.cornell_box()
-        w = h = 256
-        spp, depth = 16, 5
-        desc = "Cornell box: 36 triangles, 256x256, 16 spp, depth 5"
+        w = h = size or 256
+        spp, depth = spp_override or 16, 5
+        desc = f"Cornell box: 36 triangles, {w}x{h}, {spp} spp, depth 5"
     return scene, w, h, spp, depth, desc
 
 
@@ -140,7 +140,7 @@ def run_reference(args, rank):
     if rank != 0:
         return
     from path_gb300 import scenes
-    scene, w, h, spp, depth, desc = make_workload(args.workload)
+    scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, "binary")
     f2w = scenes.cornell_camera(w, h)
     threads = os.cpu_count() or 1
@@ -177,8 +177,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mesh", choices=["large_mesh", "cornell"])
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
+    ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
+                    help="wavefront (streaming) or megakernel integration")
     ap.add_argument("--cpu-rows", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=None,
+                    help="image width = height (profiling cases; default: the workload's)")
+    ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -197,8 +202,9 @@ def main():
 
     from path_gb300 import api, build, scenes
     build.build()
-    scene, w, h, spp, depth, desc = make_workload(args.workload)
+    scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, args.traversal)
+    settings.kernel_approach = 1 if args.approach == "streaming" else 0
     f2w = scenes.cornell_camera(w, h)
     spec = api.SquareImage(w, h, f2w)
     r = api.Renderer()
@@ -270,7 +276,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": desc, "triangles": int(scene.sizes()["triangles"]),
             "width": w, "height": h, "spp": spp,
-            "max_depth": depth, "traversal": args.traversal,
+            "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
             "l2": "flushed (512 MB write) before every timed step",
             "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),

@@ -19,6 +19,9 @@
 
 namespace pg {
 namespace dev {
+// internal linkage: every translation unit that includes this header gets
+// its own copy of these device functions
+namespace {
 
 constexpr uint32_t kTag = 1u << 31;
 #define PG_INF __int_as_float(0x7f800000)
@@ -141,10 +144,16 @@ __device__ Hit trace_binary(const RenderParams &P, const ray &r, Counts &cnt) {
 }
 
 // ---------------------------------------------------------------------------
-// compressed 8-wide BVH: node loaded with five 128-bit loads, the eight
-// child boxes decoded to exact planes and tested, leaves tested in slot
-// order, internal hits visited nearest first with the rest on a stack of
-// (node, entry distance) pairs that is culled against the current best
+// compressed 8-wide BVH.  A node is five 128-bit loads.  Its eight child
+// boxes are tested with one fused multiply-add per plane,
+//   t = q * (2^e / d) + (p - o) / d,
+// widened by a rounding margin of 2^-20 (|(p - o) / d| + 255 |2^e / d|),
+// which covers the error of the fused form against the exact plane
+// p + q 2^e (an exactly representable float, see wide.cpp) several times
+// over.  Decoded boxes contain the binary SBVH's boxes, so every box the
+// reference's slab test accepts is accepted here too.  Leaves are tested in
+// slot order; internal hits are visited nearest first, the rest kept on a
+// stack of (node, entry distance) that is culled against the current best.
 __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i) {
   uint32_t w = i < 4 ? lo : hi;
   return (w >> (8 * (i & 3))) & 0xffu;
@@ -154,144 +163,194 @@ __device__ __forceinline__ float exp2_byte(uint32_t e) {
   return __uint_as_float(e << 23);
 }
 
-constexpr int kWideStack = 128;
-
-template <bool kCount>
-__device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt) {
-  Hit best = no_hit();
-  if (P.n_wide_nodes == 0) {
-    return best;
-  }
-  f3 inv = inv_dir(r.d);
-  uint32_t st_node[kWideStack];
-  float st_t[kWideStack];
-  int sp = 0;
-  uint32_t node = 0;
-  while (true) {
-    const uint4 *np = P.wide_nodes + 5 * (size_t)node;
-    uint4 n0 = __ldg(np);
-    uint4 n1 = __ldg(np + 1);
-    uint4 n2 = __ldg(np + 2);
-    uint4 n3 = __ldg(np + 3);
-    uint4 n4 = __ldg(np + 4);
-    if (kCount) {
-      ++cnt.nodes;
-    }
-    const float px = __uint_as_float(n0.x);
-    const float py = __uint_as_float(n0.y);
-    const float pz = __uint_as_float(n0.z);
-    const float sx = exp2_byte(n0.w & 0xffu);
-    const float sy = exp2_byte((n0.w >> 8) & 0xffu);
-    const float sz = exp2_byte((n0.w >> 16) & 0xffu);
-    const uint32_t imask = n0.w >> 24;
-    const uint32_t child_base = n1.x;
-    const uint32_t tri_base = n1.y;
-    // near / far plane bytes per axis according to the ray direction sign
-    const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
-    const uint32_t nxl = nx ? n3.z : n2.x, nxh = nx ? n3.w : n2.y;
-    const uint32_t fxl = nx ? n2.x : n3.z, fxh = nx ? n2.y : n3.w;
-    const uint32_t nyl = ny ? n4.x : n2.z, nyh = ny ? n4.y : n2.w;
-    const uint32_t fyl = ny ? n2.z : n4.x, fyh = ny ? n2.w : n4.y;
-    const uint32_t nzl = nz ? n4.z : n3.x, nzh = nz ? n4.w : n3.y;
-    const uint32_t fzl = nz ? n3.x : n4.z, fzh = nz ? n3.y : n4.w;
-    float ct[8];
-    uint32_t cn[8];
-    int n_int = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const uint32_t meta = byte_of(n1.z, n1.w, i);
-      const bool internal = (imask >> i) & 1u;
-      if (!internal && meta == 0) {
-        continue;
-      }
-      // decoded planes p + q 2^e are exact floats
-      float tnx = ((px + (float)byte_of(nxl, nxh, i) * sx) - r.o.x) * inv.x;
-      float tfx = ((px + (float)byte_of(fxl, fxh, i) * sx) - r.o.x) * inv.x;
-      float tny = ((py + (float)byte_of(nyl, nyh, i) * sy) - r.o.y) * inv.y;
-      float tfy = ((py + (float)byte_of(fyl, fyh, i) * sy) - r.o.y) * inv.y;
-      float tnz = ((pz + (float)byte_of(nzl, nzh, i) * sz) - r.o.z) * inv.z;
-      float tfz = ((pz + (float)byte_of(fzl, fzh, i) * sz) - r.o.z) * inv.z;
-      float tmin = fmax2(fmax2(tnx, tny), tnz);
-      float tmax = fmin2(fmin2(tfx, tfy), tfz);
-      if (!(tmin <= tmax) || tmax < 0.f || !(tmin < best.t)) {
-        continue;
-      }
-      if (internal) {
-        ct[n_int] = tmin;
-        cn[n_int] = child_base + meta;
-        ++n_int;
-      } else {
-        uint32_t count = meta >> 5;
-        uint32_t first = tri_base + (meta & 31u);
-        for (uint32_t k = 0; k < count; ++k) {
-          const float4 *tp = P.wide_tris + 3 * (size_t)(first + k);
-          float4 a = __ldg(tp);
-          float4 b = __ldg(tp + 1);
-          float4 c = __ldg(tp + 2);
-          if (kCount) {
-            ++cnt.tris;
-          }
-          float t;
-          bool back;
-          if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), r,
-                      &t, &back)) {
-            fold(best, t, back, __float_as_uint(c.y));
-          }
-        }
-      }
-    }
-    if (n_int > 0) {
-      // order internal hits by entry distance (insertion sort, <= 8)
-      for (int i = 1; i < n_int; ++i) {
-        float kt = ct[i];
-        uint32_t kn = cn[i];
-        int j = i - 1;
-        while (j >= 0 && ct[j] > kt) {
-          ct[j + 1] = ct[j];
-          cn[j + 1] = cn[j];
-          --j;
-        }
-        ct[j + 1] = kt;
-        cn[j + 1] = kn;
-      }
-      if (sp + n_int - 1 > kWideStack) {
-        set_status(P.status, kStatusStackOverflow);
-        return no_hit();
-      }
-      for (int i = n_int - 1; i >= 1; --i) {
-        st_node[sp] = cn[i];
-        st_t[sp] = ct[i];
-        ++sp;
-      }
-      node = cn[0];
-      continue;
-    }
-    bool found = false;
-    while (sp > 0) {
-      --sp;
-      if (st_t[sp] < best.t) {
-        node = st_node[sp];
-        found = true;
-        break;
-      }
-    }
-    if (!found) {
-      break;
-    }
-  }
-  return best;
+// byte i (0..3) of w as a float: (2^23 + byte) - 2^23, exact
+__device__ __forceinline__ float byte_float(uint32_t w, int i) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)i)) - 8388608.0f;
 }
 
+__device__ __forceinline__ float byte8_float(uint32_t lo, uint32_t hi, int i) {
+  return byte_float(i < 4 ? lo : hi, i & 3);
+}
+
+constexpr int kWideStack = 128;
+
+// traversal state of one ray through the wide BVH
+struct WideWalk {
+  ray r;
+  f3 inv;
+  Hit best;   // best.t is the pruning distance: tlimit until the first hit
+  uint32_t node;
+  int sp;
+  bool done;
+};
+
+// tlimit: hits beyond it are not wanted (shadow rays only need hits up to
+// just past the light); INF for extension rays.  Within the limit the
+// closest hit and the equal-distance rule are the same as without it.
+__device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, const ray &r,
+                                           float tlimit) {
+  w.r = r;
+  w.inv = inv_dir(r.d);
+  w.best = no_hit();
+  w.best.t = tlimit;
+  w.node = 0;
+  w.sp = 0;
+  w.done = P.n_wide_nodes == 0;
+}
+
+// visit w.node, then move to the next node or finish
+template <bool kCount>
+__device__ __forceinline__ void wide_visit(const RenderParams &P, WideWalk &w,
+                                           uint32_t *st_node, float *st_t, Counts &cnt) {
+  const uint4 *np = P.wide_nodes + 5 * (size_t)w.node;
+  const uint4 n0 = __ldg(np);
+  const uint4 n1 = __ldg(np + 1);
+  const uint4 n2 = __ldg(np + 2);
+  const uint4 n3 = __ldg(np + 3);
+  const uint4 n4 = __ldg(np + 4);
+  if (kCount) {
+    ++cnt.nodes;
+  }
+  const f3 inv = w.inv;
+  // per axis: t per quantum, offset of the node origin, rounding margin
+  const float ax = exp2_byte(n0.w & 0xffu) * inv.x;
+  const float ay = exp2_byte((n0.w >> 8) & 0xffu) * inv.y;
+  const float az = exp2_byte((n0.w >> 16) & 0xffu) * inv.z;
+  const float bx = (__uint_as_float(n0.x) - w.r.o.x) * inv.x;
+  const float by = (__uint_as_float(n0.y) - w.r.o.y) * inv.y;
+  const float bz = (__uint_as_float(n0.z) - w.r.o.z) * inv.z;
+  const float ex = __fmul_rn(__fmaf_rn(255.f, fabsf(ax), fabsf(bx)), 0x1p-20f);
+  const float ey = __fmul_rn(__fmaf_rn(255.f, fabsf(ay), fabsf(by)), 0x1p-20f);
+  const float ez = __fmul_rn(__fmaf_rn(255.f, fabsf(az), fabsf(bz)), 0x1p-20f);
+  const float bnx = bx - ex, bfx = bx + ex;
+  const float bny = by - ey, bfy = by + ey;
+  const float bnz = bz - ez, bfz = bz + ez;
+  const uint32_t imask = n0.w >> 24;
+  const uint32_t child_base = n1.x;
+  const uint32_t tri_base = n1.y;
+  // near / far plane bytes per axis according to the direction's sign
+  const bool sx = inv.x < 0.f, sy = inv.y < 0.f, sz = inv.z < 0.f;
+  const uint32_t nxl = sx ? n3.z : n2.x, nxh = sx ? n3.w : n2.y;
+  const uint32_t fxl = sx ? n2.x : n3.z, fxh = sx ? n2.y : n3.w;
+  const uint32_t nyl = sy ? n4.x : n2.z, nyh = sy ? n4.y : n2.w;
+  const uint32_t fyl = sy ? n2.z : n4.x, fyh = sy ? n2.w : n4.y;
+  const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
+  const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
+  float ct[8];
+  uint32_t cn[8];
+  int n_int = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint32_t meta = byte_of(n1.z, n1.w, i);
+    const bool internal = (imask >> i) & 1u;
+    if (!internal && meta == 0) {
+      continue;
+    }
+    const float tnx = __fmaf_rn(byte8_float(nxl, nxh, i), ax, bnx);
+    const float tfx = __fmaf_rn(byte8_float(fxl, fxh, i), ax, bfx);
+    const float tny = __fmaf_rn(byte8_float(nyl, nyh, i), ay, bny);
+    const float tfy = __fmaf_rn(byte8_float(fyl, fyh, i), ay, bfy);
+    const float tnz = __fmaf_rn(byte8_float(nzl, nzh, i), az, bnz);
+    const float tfz = __fmaf_rn(byte8_float(fzl, fzh, i), az, bfz);
+    const float tmin = fmaxf(fmaxf(tnx, tny), tnz);
+    const float tmax = fminf(fminf(tfx, tfy), tfz);
+    if (!(tmin <= tmax) || tmax < 0.f || !(tmin < w.best.t)) {
+      continue;
+    }
+    if (internal) {
+      ct[n_int] = tmin;
+      cn[n_int] = child_base + meta;
+      ++n_int;
+    } else {
+      const uint32_t count = meta >> 5;
+      const uint32_t first = tri_base + (meta & 31u);
+      for (uint32_t k = 0; k < count; ++k) {
+        const float4 *tp = P.wide_tris + 3 * (size_t)(first + k);
+        const float4 a = __ldg(tp);
+        const float4 b = __ldg(tp + 1);
+        const float4 c = __ldg(tp + 2);
+        if (kCount) {
+          ++cnt.tris;
+        }
+        float t;
+        bool back;
+        if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), w.r, &t,
+                    &back) &&
+            (w.best.ok || t <= w.best.t)) {
+          fold(w.best, t, back, __float_as_uint(c.y));
+        }
+      }
+    }
+  }
+  if (n_int > 0) {
+    // nearest internal hit next, the others on the stack far to near
+    for (int i = 1; i < n_int; ++i) {
+      const float kt = ct[i];
+      const uint32_t kn = cn[i];
+      int j = i - 1;
+      while (j >= 0 && ct[j] > kt) {
+        ct[j + 1] = ct[j];
+        cn[j + 1] = cn[j];
+        --j;
+      }
+      ct[j + 1] = kt;
+      cn[j + 1] = kn;
+    }
+    if (w.sp + n_int - 1 > kWideStack) {
+      set_status(P.status, kStatusStackOverflow);
+      w.best = no_hit();
+      w.done = true;
+      return;
+    }
+    for (int i = n_int - 1; i >= 1; --i) {
+      st_node[w.sp] = cn[i];
+      st_t[w.sp] = ct[i];
+      ++w.sp;
+    }
+    w.node = cn[0];
+    return;
+  }
+  while (w.sp > 0) {
+    --w.sp;
+    if (st_t[w.sp] < w.best.t) {
+      w.node = st_node[w.sp];
+      return;
+    }
+  }
+  w.done = true;
+}
+
+template <bool kCount>
+__device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, float tlimit) {
+  WideWalk w;
+  wide_begin(P, w, r, tlimit);
+  uint32_t st_node[kWideStack];
+  float st_t[kWideStack];
+  while (!w.done) {
+    wide_visit<kCount>(P, w, st_node, st_t, cnt);
+  }
+  return w.best;
+}
+
+// closest hit; the binary traversal keeps the reference's order and
+// pruning exactly and ignores tlimit
 template <uint32_t kTrav, bool kCount>
-__device__ __forceinline__ Hit trace(const RenderParams &P, const ray &r,
-                                     Counts &cnt) {
+__device__ __forceinline__ Hit trace(const RenderParams &P, const ray &r, Counts &cnt,
+                                     float tlimit) {
   if (kCount) {
     ++cnt.rays;
   }
   if (kTrav == kTravWide) {
-    return trace_wide<kCount>(P, r, cnt);
+    return trace_wide<kCount>(P, r, cnt, tlimit);
   }
   return trace_binary<kCount>(P, r, cnt);
+}
+
+// A light sample is visible when the closest hit lies within 1e-6 of the
+// light point's distance (rendering_equation_iteration.h:22-27); no hit
+// beyond target + 1e-6 can pass, so shadow rays only need hits up to here.
+__device__ __forceinline__ float light_bound(float target) {
+  return target * 1.0000005f + 2e-6f;
 }
 
 // ---------------------------------------------------------------------------
@@ -731,112 +790,149 @@ __device__ __forceinline__ f3 shading_normal(const RenderParams &P, uint32_t idx
   return normalize((n0 * w[0] + n1 * w[1]) + n2 * w[2]);
 }
 
-// one camera sample of rendering_equation, with at most one light sample
-// per vertex
+// State of one camera sample between traces: the loop variables of
+// rendering_equation (include/integrate/rendering_equation.h:41-124) and the
+// RenderingEquationState (rendering_equation_state.h:14-52) with at most
+// one light sample per vertex.  o is the current vertex, the origin of both
+// the next extension ray (direction d) and the light ray (direction ld).
+struct PathState {
+  f3 o, d, ld;
+  float light_target;
+  rgb multiplier, light_mult, total;
+  uint32_t iters;
+  bool count_emission, has_next, has_light;
+  Rng rng;
+};
+
+// camera ray of a sample (initial_ray_sample.h:36-56, 2 RNG draws)
+__device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sample_idx,
+                                           uint32_t x, uint32_t y, PathState &s) {
+  const uint32_t location = x + y * P.x_dim;
+  s.rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
+  s.rng.bound = P.dim_bound;
+  s.rng.dim = fnv_hash(location) % P.init_dim_bound;
+  float xo = s.rng.next();
+  float yo = s.rng.next();
+  ray r = camera_ray(P, (float)x + xo, (float)y + yo);
+  s.o = r.o;
+  s.d = r.d;
+  s.ld = mk(0.f, 0.f, 0.f);
+  s.light_target = 0.f;
+  s.multiplier = mkrgb(1.f, 1.f, 1.f);
+  s.light_mult = zero_rgb();
+  s.total = zero_rgb();
+  s.iters = 0;
+  s.count_emission = true;
+  s.has_next = true;
+  s.has_light = false;
+}
+
+// One rendering_equation_iteration (rendering_equation_iteration.h:9-153)
+// given the closest hits of the pending light ray (lh) and extension ray
+// (nh).  Returns true while the path has rays left to trace; s.total is the
+// sample's radiance once it returns false.
+__device__ __noinline__ bool path_step(const RenderParams &P, PathState &s, const Hit &lh,
+                                       const Hit &nh) {
+  const bool performs_samples = P.light_sampler == 0;
+  const bool cull = P.back_cull != 0;
+  if (s.has_light && lh.ok && pm::fabs(s.light_target - lh.t) <= 1e-6f &&
+      (!cull || !lh.back)) {
+    float4 c = __ldg(P.tri_data + 3 * lh.idx + 2);
+    s.total = s.total + emission_of(P.materials + __float_as_uint(c.w)) * s.light_mult;
+  }
+  if (!s.has_next || !nh.ok) {
+    return false;
+  }
+  f3 point = s.o + s.d * nh.t;
+  uint32_t mi;
+  f3 normal = shading_normal(P, nh.idx, point, mi);
+  const Mat mat = load_mat(P.materials + mi);
+  if ((!performs_samples || s.count_emission) && (!cull || !nh.back)) {
+    s.total = s.total + s.multiplier * mat.emission;
+  }
+  bool new_has_light = false;
+  rgb new_light_mult = zero_rgb();
+  float new_light_target = 0.f;
+  f3 new_ld = s.ld;
+  float pc = prob_continuous(mat);
+  if (pc > 0.f && performs_samples) {
+    LightSample ls;
+    if (sample_light(P, point, mat, normal, s.rng, ls)) {
+      rgb f = continuous_eval(mat, s.d, ls.dir, normal);
+      new_light_mult = ((s.multiplier * f) * pc) / ls.mult;
+      new_light_target = ls.target;
+      new_ld = ls.dir;
+      new_has_light = true;
+    }
+  }
+  bool take_discrete;
+  if (pc == 0.f) {
+    take_discrete = true;
+  } else if (pc == 1.f) {
+    take_discrete = false;
+  } else {
+    take_discrete = pc < s.rng.next();
+  }
+  Sample smp;
+  if (take_discrete) {
+    smp = discrete_sample(mat, s.d, normal, s.rng);
+  } else if (P.dir_sampler == 0) {
+    smp = continuous_sample(mat, s.d, normal, s.rng);
+  } else {
+    smp = uniform_dir_sample(mat, s.d, normal, s.rng);
+  }
+  rgb new_multiplier = s.multiplier * smp.mult;
+  float p = term_prob(P, s.iters, new_multiplier);
+  bool next = s.rng.next() > p;
+  s.iters += 1;
+  s.count_emission = take_discrete;
+  s.has_light = new_has_light;
+  s.light_mult = new_light_mult;
+  s.light_target = new_light_target;
+  s.ld = new_ld;
+  s.o = point;
+  if (next) {
+    s.multiplier = new_multiplier / (1.0f - p);
+    s.d = smp.dir;
+    s.has_next = true;
+  } else {
+    s.has_next = false;
+  }
+  return s.has_next || s.has_light;
+}
+
+// the safety bound on path vertices (no counterpart in the reference)
+__device__ __forceinline__ bool path_continues(const RenderParams &P, PathState &s,
+                                               bool cont) {
+  if (cont && s.iters >= kMaxPathVertices) {
+    set_status(P.status, kStatusPathTooLong);
+    return false;
+  }
+  return cont;
+}
+
+// one camera sample of rendering_equation, traced in a loop
 template <uint32_t kTrav, bool kCount>
 __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
                                 uint32_t x, uint32_t y, Counts &cnt) {
-  const uint32_t location = x + y * P.x_dim;
-  Rng rng;
-  rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
-  rng.bound = P.dim_bound;
-  rng.dim = fnv_hash(location) % P.init_dim_bound;
-  float xo = rng.next();
-  float yo = rng.next();
-  ray r = camera_ray(P, (float)x + xo, (float)y + yo);
-
-  uint32_t iters = 0;
-  bool count_emission = true;
-  bool has_next = true;
-  rgb multiplier = mkrgb(1.f, 1.f, 1.f);
-  bool has_light = false;
-  ray light_ray;
-  light_ray.o = mk(0.f, 0.f, 0.f);
-  light_ray.d = mk(0.f, 0.f, 0.f);
-  rgb light_mult = zero_rgb();
-  float light_target = 0.f;
-  rgb total = zero_rgb();
-  const bool performs_samples = P.light_sampler == 0;
-  const bool cull = P.back_cull != 0;
-
+  PathState s;
+  path_begin(P, sample_idx, x, y, s);
   while (true) {
-    if (iters >= kMaxPathVertices) {
-      set_status(P.status, kStatusPathTooLong);
-      return total;
-    }
     Hit lh = no_hit(), nh = no_hit();
-    if (has_light) {
-      lh = trace<kTrav, kCount>(P, light_ray, cnt);
+    if (s.has_light) {
+      ray lr;
+      lr.o = s.o;
+      lr.d = s.ld;
+      lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target));
     }
-    if (has_next) {
-      nh = trace<kTrav, kCount>(P, r, cnt);
+    if (s.has_next) {
+      ray r;
+      r.o = s.o;
+      r.d = s.d;
+      nh = trace<kTrav, kCount>(P, r, cnt, PG_INF);
     }
-    if (has_light && lh.ok && pm::fabs(light_target - lh.t) <= 1e-6f &&
-        (!cull || !lh.back)) {
-      float4 c = __ldg(P.tri_data + 3 * lh.idx + 2);
-      total = total + emission_of(P.materials + __float_as_uint(c.w)) * light_mult;
-    }
-    if (!has_next || !nh.ok) {
-      return total;
-    }
-    f3 point = r.o + r.d * nh.t;
-    uint32_t mi;
-    f3 normal = shading_normal(P, nh.idx, point, mi);
-    const Mat mat = load_mat(P.materials + mi);
-    if ((!performs_samples || count_emission) && (!cull || !nh.back)) {
-      total = total + multiplier * mat.emission;
-    }
-    bool new_has_light = false;
-    rgb new_light_mult = zero_rgb();
-    float new_light_target = 0.f;
-    ray new_light_ray = light_ray;
-    float pc = prob_continuous(mat);
-    if (pc > 0.f && performs_samples) {
-      LightSample ls;
-      if (sample_light(P, point, mat, normal, rng, ls)) {
-        rgb f = continuous_eval(mat, r.d, ls.dir, normal);
-        new_light_mult = ((multiplier * f) * pc) / ls.mult;
-        new_light_target = ls.target;
-        new_light_ray.o = point;
-        new_light_ray.d = ls.dir;
-        new_has_light = true;
-      }
-    }
-    bool take_discrete;
-    if (pc == 0.f) {
-      take_discrete = true;
-    } else if (pc == 1.f) {
-      take_discrete = false;
-    } else {
-      take_discrete = pc < rng.next();
-    }
-    Sample smp;
-    if (take_discrete) {
-      smp = discrete_sample(mat, r.d, normal, rng);
-    } else if (P.dir_sampler == 0) {
-      smp = continuous_sample(mat, r.d, normal, rng);
-    } else {
-      smp = uniform_dir_sample(mat, r.d, normal, rng);
-    }
-    rgb new_multiplier = multiplier * smp.mult;
-    float p = term_prob(P, iters, new_multiplier);
-    bool next = rng.next() > p;
-    iters += 1;
-    count_emission = take_discrete;
-    has_light = new_has_light;
-    light_mult = new_light_mult;
-    light_target = new_light_target;
-    light_ray = new_light_ray;
-    if (next) {
-      multiplier = new_multiplier / (1.0f - p);
-      r.o = point;
-      r.d = smp.dir;
-      has_next = true;
-    } else {
-      has_next = false;
-      if (!has_light) {
-        return total;
-      }
+    if (!path_continues(P, s, path_step(P, s, lh, nh))) {
+      return s.total;
     }
   }
 }
@@ -893,5 +989,6 @@ __device__ __forceinline__ void write_pixel(float *out_rgb, uint8_t *out_bgra,
   }
 }
 
+} // namespace
 } // namespace dev
 } // namespace pg

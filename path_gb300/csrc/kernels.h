@@ -44,6 +44,43 @@ struct RenderParams {
 
 enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
 
+// queue heads of the wavefront render
+struct WaveQueues {
+  uint32_t active[2];   // live-slot counts of the two live lists
+  uint32_t rays;        // entries in the ray queue
+  uint32_t ray_cursor;  // next ray entry to trace
+  uint32_t shade_cursor;
+  uint32_t pad[3];
+};
+
+// wavefront render state (device pointers); slot arrays hold PathState
+struct WaveParams {
+  RenderParams P;
+  float4 *o;      // vertex xyz, light target distance in w
+  float4 *d;      // next extension direction
+  float4 *ld;     // light ray direction
+  float4 *mult;   // path multiplier
+  float4 *lmult;  // light sample multiplier
+  float4 *total;  // radiance gathered so far
+  uint4 *state;   // sample id (2 words), RNG dimension, iters | flags << 24
+  uint2 *hit_ext, *hit_light;
+  uint32_t *active[2]; // live slot lists
+  uint32_t *rays;      // ray queue: slot << 1 | (1 for the light ray)
+  WaveQueues *q;
+  unsigned long long *next_sample;
+  unsigned long long total_samples;
+  float *sample_rgb;   // [total_samples][3]
+  uint32_t n_slots;
+};
+
+cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
+// one trace + shade iteration (three launches)
+cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity, uint32_t grid,
+                                       bool counting, cudaStream_t s);
+// per-pixel sums of the sample buffer into p.out_rgb / p.out_bgra
+cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
+                                 cudaStream_t s);
+
 // integration megakernel over blocks [start_block, start_block + n_blocks)
 cudaError_t launch_render(const RenderParams &p, uint32_t traversal,
                           uint32_t n_blocks, bool counting, cudaStream_t s);

@@ -376,6 +376,9 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     }
     prep_.valid = true;
   }
+  if (st.kernel_approach == PATH_KERNEL_STREAMING && st.traversal != PATH_TRAVERSAL_WIDE8) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the streaming approach traces the 8-wide BVH only");
+  }
   if (st.traversal == PATH_TRAVERSAL_BINARY) {
     if (prep_.bvh.depth + 2 > 64) {
       return Status::err(PATH_ERR_UNSUPPORTED, "SBVH deeper than the 64-entry traversal stack");
@@ -454,9 +457,16 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   auto t0 = std::chrono::steady_clock::now();
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
-  PG_TRY_CUDA(launch_render(p, st.traversal, wd.total_blocks(), st.count_work != 0, stream_),
-              "render kernel");
-  ++launches;
+  if (st.kernel_approach == PATH_KERNEL_STREAMING) {
+    Status sw = run_wavefront(p, st.count_work != 0, &launches);
+    if (!sw.good()) {
+      return sw;
+    }
+  } else {
+    PG_TRY_CUDA(launch_render(p, st.traversal, wd.total_blocks(), st.count_work != 0, stream_),
+                "render kernel");
+    ++launches;
+  }
   // ReduceFloatRGB passes
   uint32_t factor = nsb;
   float *in = p.out_rgb;
@@ -532,6 +542,81 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
                        "kernel reported device status " + std::to_string(status) +
                            " (1 stack overflow, 2 candidate overflow, 3 bad node, 4 path too long)");
   }
+  return Status::ok();
+}
+
+// wavefront render of the whole image into p.out_rgb / p.out_bgra (see
+// wavefront.cu); the host checks the live-slot count every few iterations
+Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t *launches) {
+  if (num_sms_ == 0) {
+    int dev = 0;
+    PG_TRY_CUDA(cudaGetDevice(&dev), "device");
+    PG_TRY_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev), "sm count");
+  }
+  const unsigned long long total = (unsigned long long)p.x_dim * p.y_dim * p.spp;
+  const uint32_t n_slots = (uint32_t)std::min<unsigned long long>(total, 1ull << 21);
+  auto a256 = [](size_t n) { return (n + 255) & ~size_t(255); };
+  const size_t f4 = a256((size_t)n_slots * 16), u2 = a256((size_t)n_slots * 8),
+               u1 = a256((size_t)n_slots * 4);
+  PG_TRY_CUDA(wf_slots_.ensure(7 * f4 + 2 * u2 + 2 * u1 + 2 * u1), "wavefront slots");
+  PG_TRY_CUDA(wf_queues_.ensure(64), "wavefront queues");
+  PG_TRY_CUDA(wf_samples_.ensure((size_t)total * 12), "sample buffer");
+  PG_TRY_CUDA(wf_host_.ensure(64), "staging");
+  unsigned char *b = wf_slots_.as<unsigned char>();
+  WaveParams w;
+  std::memset(&w, 0, sizeof(w));
+  w.P = p;
+  w.o = reinterpret_cast<float4 *>(b);
+  w.d = reinterpret_cast<float4 *>(b + f4);
+  w.ld = reinterpret_cast<float4 *>(b + 2 * f4);
+  w.mult = reinterpret_cast<float4 *>(b + 3 * f4);
+  w.lmult = reinterpret_cast<float4 *>(b + 4 * f4);
+  w.total = reinterpret_cast<float4 *>(b + 5 * f4);
+  w.state = reinterpret_cast<uint4 *>(b + 6 * f4);
+  w.hit_ext = reinterpret_cast<uint2 *>(b + 7 * f4);
+  w.hit_light = reinterpret_cast<uint2 *>(b + 7 * f4 + u2);
+  w.active[0] = reinterpret_cast<uint32_t *>(b + 7 * f4 + 2 * u2);
+  w.active[1] = reinterpret_cast<uint32_t *>(b + 7 * f4 + 2 * u2 + u1);
+  w.rays = reinterpret_cast<uint32_t *>(b + 7 * f4 + 2 * u2 + 2 * u1);
+  w.q = wf_queues_.as<WaveQueues>();
+  w.next_sample = reinterpret_cast<unsigned long long *>(wf_queues_.as<unsigned char>() + 32);
+  w.total_samples = total;
+  w.sample_rgb = wf_samples_.as<float>();
+  w.n_slots = n_slots;
+  // queue heads: n_slots live slots, one extension ray each
+  uint32_t *h = wf_host_.as<uint32_t>();
+  std::memset(h, 0, 64);
+  h[0] = n_slots;
+  h[2] = n_slots;
+  unsigned long long next = n_slots;
+  std::memcpy(h + 8, &next, sizeof(next));
+  PG_TRY_CUDA(cudaMemcpyAsync(wf_queues_.get(), h, 48, cudaMemcpyHostToDevice, stream_),
+              "queue init");
+  PG_TRY_CUDA(launch_wavefront_init(w, n_slots, stream_), "wavefront init");
+  *launches += 1;
+  const uint32_t grid = (uint32_t)num_sms_ * 8;
+  uint32_t parity = 0;
+  volatile uint32_t *live = h + 12;
+  for (uint32_t round = 0;; ++round) {
+    for (int k = 0; k < 4; ++k) {
+      PG_TRY_CUDA(launch_wavefront_iteration(w, parity, grid, counting, stream_),
+                  "wavefront iteration");
+      *launches += 3;
+      parity ^= 1u;
+    }
+    PG_TRY_CUDA(cudaMemcpyAsync(h + 12, &w.q->active[parity], 4, cudaMemcpyDeviceToHost,
+                                stream_),
+                "live count");
+    PG_TRY_CUDA(cudaStreamSynchronize(stream_), "wavefront sync");
+    if (*live == 0) {
+      break;
+    }
+    if (round > 4 * kMaxPathVertices) {
+      return Status::err(PATH_ERR_DEVICE_TIMEOUT, "wavefront did not drain");
+    }
+  }
+  PG_TRY_CUDA(launch_wavefront_sum(p, w.sample_rgb, stream_), "sample sum");
+  *launches += 1;
   return Status::ok();
 }
 

@@ -114,6 +114,11 @@ private:
   DeviceBuffer sobol_dirs_, sobol_scramble_, sobol_table_;
   uint32_t sobol_bound_ = 0, sobol_count_ = 0;
   DeviceBuffer out_a_, out_b_, bgra_, status_, counters_;
+  // wavefront state
+  Status run_wavefront(const RenderParams &p, bool counting, uint32_t *launches);
+  DeviceBuffer wf_slots_, wf_queues_, wf_samples_;
+  PinnedBuffer wf_host_;
+  int num_sms_ = 0;
   path_render_stats stats_{};
 };
 

@@ -1,0 +1,327 @@
+// Wavefront ("streaming") render: persistent trace and shade kernels over
+// queues, the GB300 form of the reference's streaming::Run
+// (include/render/detail/integrate_image/streaming/run_impl.h:159-460).
+//
+// Path slots hold the state of up to n_slots camera samples between traces
+// (PathState in structure-of-arrays form).  One iteration is
+//   k_wf_trace : every queued ray (extension or light) of every live slot is
+//                traced by a persistent grid, one wide-BVH node per lane and
+//                step; idle lanes of a warp take new queue entries together;
+//   k_wf_prep  : resets the queue heads for the shade pass;
+//   k_wf_shade : every live slot runs one rendering_equation_iteration
+//                (path_step, the same code the megakernel runs); slots whose
+//                path continues are appended to the next live list and their
+//                rays to the ray queue -- compacted per warp with ballots and
+//                one atomic per warp and queue -- and finished slots write
+//                their sample's radiance and take the next sample index.
+// Sample radiance lands in a [samples][3] buffer; k_wf_sum then sums each
+// pixel's samples in the reference's order (per WorkDivision thread, then
+// the shuffle tree), so the image is bit-identical to the megakernel's.
+#include "integrator.cuh"
+
+namespace pg {
+namespace dev {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kMissIdx = 0xffffffffu;
+constexpr uint32_t kFlagNext = 1u, kFlagLight = 2u, kFlagEmission = 4u;
+
+__device__ __forceinline__ uint2 pack_hit(const Hit &h) {
+  uint2 v;
+  v.x = __float_as_uint(h.t);
+  v.y = h.ok ? (h.idx | (h.back ? 0x80000000u : 0u)) : kMissIdx;
+  return v;
+}
+
+__device__ __forceinline__ Hit unpack_hit(uint2 v) {
+  Hit h;
+  h.ok = v.y != kMissIdx;
+  h.t = __uint_as_float(v.x);
+  h.idx = v.y & 0x7fffffffu;
+  h.back = (v.y & 0x80000000u) != 0;
+  return h;
+}
+
+// the pixel and sample index of a linear sample id (pixel-major order)
+__device__ __forceinline__ void sample_coords(const RenderParams &P, unsigned long long id,
+                                              uint32_t &x, uint32_t &y, uint32_t &s) {
+  unsigned long long pixel = id / P.spp;
+  s = (uint32_t)(id - pixel * P.spp);
+  x = (uint32_t)(pixel % P.x_dim);
+  y = (uint32_t)(pixel / P.x_dim);
+}
+
+__device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
+                                           const PathState &s, unsigned long long id) {
+  W.o[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.light_target);
+  W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, 0.f);
+  W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, 0.f);
+  W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
+  W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
+  W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
+  uint32_t flags = (s.has_next ? kFlagNext : 0u) | (s.has_light ? kFlagLight : 0u) |
+                   (s.count_emission ? kFlagEmission : 0u);
+  W.state[slot] = make_uint4((uint32_t)id, (uint32_t)(id >> 32), s.rng.dim,
+                             s.iters | (flags << 24));
+}
+
+__device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
+                                                        PathState &s) {
+  const RenderParams &P = W.P;
+  float4 o = W.o[slot], d = W.d[slot], ld = W.ld[slot];
+  float4 m = W.mult[slot], lm = W.lmult[slot], t = W.total[slot];
+  uint4 st = W.state[slot];
+  unsigned long long id = (unsigned long long)st.x | ((unsigned long long)st.y << 32);
+  s.o = mk(o.x, o.y, o.z);
+  s.light_target = o.w;
+  s.d = mk(d.x, d.y, d.z);
+  s.ld = mk(ld.x, ld.y, ld.z);
+  s.multiplier = mkrgb(m.x, m.y, m.z);
+  s.light_mult = mkrgb(lm.x, lm.y, lm.z);
+  s.total = mkrgb(t.x, t.y, t.z);
+  uint32_t flags = st.w >> 24;
+  s.iters = st.w & 0xffffffu;
+  s.has_next = (flags & kFlagNext) != 0;
+  s.has_light = (flags & kFlagLight) != 0;
+  s.count_emission = (flags & kFlagEmission) != 0;
+  uint32_t x, y, smp;
+  sample_coords(P, id, x, y, smp);
+  s.rng.row = P.sobol + (size_t)smp * P.dim_bound;
+  s.rng.bound = P.dim_bound;
+  s.rng.dim = st.z;
+  return id;
+}
+
+__device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
+                                             unsigned long long id) {
+  uint32_t x, y, smp;
+  sample_coords(W.P, id, x, y, smp);
+  PathState s;
+  path_begin(W.P, smp, x, y, s);
+  store_path(W, slot, s, id);
+}
+
+// slot i takes sample i; the first ray of each is queued
+__global__ void k_wf_init(const WaveParams W, uint32_t n0) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n0) {
+    return;
+  }
+  begin_sample(W, i, i);
+  W.active[0][i] = i;
+  W.rays[i] = i << 1;
+}
+
+// Persistent trace: each lane walks one ray through the wide BVH one node
+// per step; when a quarter of a warp's lanes are idle they take new queue
+// entries together (one atomic per warp), so lanes rarely wait on the
+// longest ray of a batch.
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_wf_trace(const WaveParams W) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t count = W.q->rays;
+  Counts cnt = {0, 0, 0};
+  WideWalk w;
+  w.done = true;
+  bool have = false;
+  bool drained = false;
+  uint32_t entry = 0;
+  uint32_t st_node[kWideStack];
+  float st_t[kWideStack];
+  while (true) {
+    const uint32_t idle = __ballot_sync(kFull, !have);
+    if (!drained && __popc(idle) >= 8) {
+      uint32_t base = 0;
+      if (lane == 0) {
+        base = atomicAdd(&W.q->ray_cursor, (uint32_t)__popc(idle));
+      }
+      base = __shfl_sync(kFull, base, 0);
+      drained = base + (uint32_t)__popc(idle) >= count;
+      if (!have) {
+        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (i < count) {
+          entry = W.rays[i];
+          const uint32_t slot = entry >> 1;
+          const bool light = (entry & 1u) != 0;
+          const float4 o = W.o[slot];
+          const float4 d = light ? W.ld[slot] : W.d[slot];
+          ray r;
+          r.o = mk(o.x, o.y, o.z);
+          r.d = mk(d.x, d.y, d.z);
+          wide_begin(W.P, w, r, light ? light_bound(o.w) : PG_INF);
+          have = true;
+          if (kCount) {
+            ++cnt.rays;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(kFull, have) == 0) {
+      if (drained) {
+        break;
+      }
+      continue;
+    }
+    if (have) {
+      if (!w.done) {
+        wide_visit<kCount>(W.P, w, st_node, st_t, cnt);
+      }
+      if (w.done) {
+        const uint32_t slot = entry >> 1;
+        ((entry & 1u) ? W.hit_light : W.hit_ext)[slot] = pack_hit(w.best);
+        have = false;
+      }
+    }
+  }
+  if (kCount) {
+    atomicAdd(W.P.counters + 0, (unsigned long long)cnt.rays);
+    atomicAdd(W.P.counters + 1, (unsigned long long)cnt.nodes);
+    atomicAdd(W.P.counters + 2, (unsigned long long)cnt.tris);
+  }
+}
+
+__global__ void k_wf_prep(const WaveParams W, uint32_t parity) {
+  W.q->active[parity ^ 1u] = 0;
+  W.q->rays = 0;
+  W.q->shade_cursor = 0;
+  W.q->ray_cursor = 0;
+}
+
+// warp-aggregated append: lanes with pred get consecutive positions
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool pred, uint32_t lane) {
+  const uint32_t mask = __ballot_sync(kFull, pred);
+  uint32_t base = 0;
+  if (lane == 0 && mask != 0) {
+    base = atomicAdd(counter, (uint32_t)__popc(mask));
+  }
+  base = __shfl_sync(kFull, base, 0);
+  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t parity) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t count = W.q->active[parity];
+  const uint32_t *in = W.active[parity];
+  uint32_t *out = W.active[parity ^ 1u];
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) {
+      base = atomicAdd(&W.q->shade_cursor, 32u);
+    }
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= count) {
+      break;
+    }
+    const uint32_t i = base + lane;
+    const bool valid = i < count;
+    uint32_t slot = 0;
+    bool live = false, finished = false, want_next = false, want_light = false;
+    if (valid) {
+      slot = in[i];
+      PathState s;
+      unsigned long long id = load_path(W, slot, s);
+      Hit lh = s.has_light ? unpack_hit(W.hit_light[slot]) : no_hit();
+      Hit nh = s.has_next ? unpack_hit(W.hit_ext[slot]) : no_hit();
+      bool cont = path_continues(W.P, s, path_step(W.P, s, lh, nh));
+      if (cont) {
+        store_path(W, slot, s, id);
+        live = true;
+        want_next = s.has_next;
+        want_light = s.has_light;
+      } else {
+        float *dst = W.sample_rgb + 3 * id;
+        dst[0] = s.total.r;
+        dst[1] = s.total.g;
+        dst[2] = s.total.b;
+        finished = true;
+      }
+    }
+    __syncwarp();
+    // finished slots take the next sample index (one atomic per warp)
+    {
+      const uint32_t mask = __ballot_sync(kFull, finished);
+      unsigned long long first = 0;
+      if (lane == 0 && mask != 0) {
+        first = atomicAdd(W.next_sample, (unsigned long long)__popc(mask));
+      }
+      first = __shfl_sync(kFull, first, 0);
+      if (finished) {
+        unsigned long long id = first + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
+        if (id < W.total_samples) {
+          begin_sample(W, slot, id);
+          live = true;
+          want_next = true;
+          want_light = false;
+        }
+      }
+    }
+    const uint32_t pos = warp_append(&W.q->active[parity ^ 1u], live, lane);
+    if (live) {
+      out[pos] = slot;
+    }
+    const uint32_t pn = warp_append(&W.q->rays, want_next, lane);
+    if (want_next) {
+      W.rays[pn] = slot << 1;
+    }
+    const uint32_t pl = warp_append(&W.q->rays, want_light, lane);
+    if (want_light) {
+      W.rays[pl] = (slot << 1) | 1u;
+    }
+  }
+}
+
+// each WorkDivision thread sums its samples in order, then the shuffle tree
+// (the same summation as k_render, from the per-sample buffer)
+__global__ void __launch_bounds__(256) k_wf_sum(const RenderParams P, const float *sample_rgb) {
+  const uint32_t block = blockIdx.x;
+  const uint32_t tid = threadIdx.x;
+  const ThreadWork tw = thread_work(P.wd, block, tid);
+  rgb total = zero_rgb();
+  if (!tw.exit) {
+    const size_t pixel = tw.x + (size_t)tw.y * P.x_dim;
+    for (uint32_t s = tw.start; s < tw.end; ++s) {
+      const float *v = sample_rgb + 3 * (pixel * P.spp + s);
+      total = total + mkrgb(v[0], v[1], v[2]);
+    }
+  }
+  const uint32_t sbs = P.wd.sample_block_size;
+  total = sub_block_reduce(total, tid, sbs);
+  if (!tw.exit && tid % sbs == 0) {
+    const uint32_t nsb = P.wd.num_sample_blocks;
+    const size_t idx = (block % nsb) + (size_t)nsb * (tw.x + (size_t)tw.y * P.x_dim);
+    if (nsb == 1) {
+      total = total / (float)P.spp;
+    }
+    write_pixel(P.out_rgb, P.out_bgra, P.output_bgra && nsb == 1, idx, total);
+  }
+}
+
+} // namespace dev
+
+cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s) {
+  if (n0 == 0) {
+    return cudaSuccess;
+  }
+  dev::k_wf_init<<<(n0 + 255) / 256, 256, 0, s>>>(w, n0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity, uint32_t grid,
+                                       bool counting, cudaStream_t s) {
+  if (counting) {
+    dev::k_wf_trace<true><<<grid, 256, 0, s>>>(w);
+  } else {
+    dev::k_wf_trace<false><<<grid, 256, 0, s>>>(w);
+  }
+  dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
+  dev::k_wf_shade<<<grid, 256, 0, s>>>(w, parity);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
+                                 cudaStream_t s) {
+  dev::k_wf_sum<<<p.wd.total_blocks(), p.wd.block_size, 0, s>>>(p, sample_rgb);
+  return cudaGetLastError();
+}
+
+} // namespace pg

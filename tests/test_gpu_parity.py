@@ -234,3 +234,42 @@ def test_device_output_equals_host_output(lib):
     r.render(api.ExecutionModel.GPU, api.SquareImage(64, 64, f2w), dev, sc, 16, s)
     torch.cuda.synchronize()
     assert np.array_equal(bits(dev.cpu().numpy()), bits(host))
+
+
+@pytest.mark.parametrize("case", ["cornell", "zoo", "large_mesh", "sample_blocks"])
+def test_streaming_matches_oracle(lib, oracle, case):
+    """The wavefront (streaming) render: per-sample radiance from queued
+    trace / shade passes, summed per pixel in the reference's order."""
+    spp = 16
+    if case == "cornell":
+        sc, w, h, depth = scenes.cornell_box(), 64, 64, 5
+    elif case == "zoo":
+        sc, w, h, depth = _material_zoo_scene(), 48, 48, 6
+    elif case == "large_mesh":
+        sc, w, h, depth = scenes.large_mesh_room(5, 40, 40), 64, 64, 8
+        spp = 8
+    else:
+        sc, w, h, depth = scenes.cornell_box(), 32, 32, 5
+        spp = 128
+    s = scenes.path_settings(depth, "wide")
+    s.kernel_approach = 1
+    if case == "sample_blocks":
+        s.render_work_division.block_size = 32
+        s.render_work_division.force_target_samples = 1
+        s.render_work_division.forced_target_samples_per_thread = 1
+    f2w = scenes.cornell_camera(w, h)
+    gpu = _render_gpu(sc, s, spp, w, h, f2w)
+    ref = _render_oracle(sc, s, spp, w, h, f2w)
+    err = rel_rmse(gpu, ref)
+    print(f"streaming {case} rel RMSE {err:.3e}")
+    assert err <= RMSE_TOL
+
+
+def test_streaming_equals_megakernel_full_cornell(lib):
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "wide")
+    f2w = scenes.cornell_camera(256, 256)
+    mega = _render_gpu(sc, s, 16, 256, 256, f2w)
+    s.kernel_approach = 1
+    wave = _render_gpu(sc, s, 16, 256, 256, f2w)
+    assert np.array_equal(bits(mega), bits(wave))
