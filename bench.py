@@ -184,6 +184,8 @@ def main():
     ap.add_argument("--size", type=int, default=None,
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
+    ap.add_argument("--trace-min-blocks", type=int, default=0,
+                    help="streaming trace kernel variant (resident blocks per SM, 3..6)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -205,6 +207,7 @@ def main():
     scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, args.traversal)
     settings.kernel_approach = 1 if args.approach == "streaming" else 0
+    settings.trace_min_blocks = args.trace_min_blocks
     f2w = scenes.cornell_camera(w, h)
     spec = api.SquareImage(w, h, f2w)
     r = api.Renderer()
@@ -277,6 +280,7 @@ def main():
         "config": {"workload": desc, "triangles": int(scene.sizes()["triangles"]),
             "width": w, "height": h, "spp": spp,
             "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
+            "trace_min_blocks": args.trace_min_blocks or 4,
             "l2": "flushed (512 MB write) before every timed step",
             "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),

@@ -126,35 +126,54 @@ typedef struct {
   uint32_t count_work;       /* 1: count rays / nodes / triangles (slower) */
   uint32_t upload_scene_every_render; /* 1: re-copy the cached scene arrays
                                          host -> device on every render */
-  uint32_t reserved[4];
+  uint32_t trace_min_blocks; /* streaming trace kernel: resident 256-thread
+                                blocks per SM it is compiled for (3..6, 0 =
+                                default 4); fewer registers per thread above 3 */
+  uint32_t reserved[3];
 } path_settings;
 
 typedef enum {
   PATH_SAMPLE_SQUARE_IMAGE = 0,
-  PATH_SAMPLE_INITIAL_RAYS = 1
+  PATH_SAMPLE_INITIAL_RAYS = 1,
+  PATH_SAMPLE_INITIAL_IDX_AND_DIR = 2
 } path_sample_spec_type;
 
-/* render::SampleSpec (include/render/renderer.h:19-41) */
+/* render::SampleSpec (include/render/renderer.h:19-41).  INITIAL_RAYS and
+ * INITIAL_IDX_AND_DIR render one location per entry (x = entry index, one
+ * row).  INITIAL_IDX_AND_DIR (render::InitialIdxAndDirSpec, renderer.h:31-35)
+ * starts each path at a known hit: triangle idxs[i] (index in scene order:
+ * instances in order, each mesh's triangles in order) at distance 1 along
+ * rays[i], front side; MegaKernel approach only, as in the reference. */
 typedef struct {
   uint32_t type;          /* path_sample_spec_type */
   uint32_t x_dim, y_dim;  /* SQUARE_IMAGE */
   float film_to_world[12]; /* 3x4 row-major affine, SQUARE_IMAGE */
-  const float *rays;      /* INITIAL_RAYS: [n_rays][6] origin, direction */
+  const float *rays;      /* INITIAL_*: [n_rays][6] origin, unit direction */
   uint32_t n_rays;
+  const uint32_t *idxs;   /* INITIAL_IDX_AND_DIR: [n_rays] triangle index */
 } path_sample_spec;
 
 typedef enum {
   PATH_OUTPUT_BGRA = 0,
-  PATH_OUTPUT_FLOAT_RGB = 1
+  PATH_OUTPUT_FLOAT_RGB = 1,
+  PATH_OUTPUT_PER_STEP = 2
 } path_output_type;
+
+/* Most path steps one PER_STEP render may ask for. */
+#define PATH_MAX_OUTPUT_STEPS 64u
 
 /* render::Output (include/render/renderer.h:13-17,37-38).  data is host
  * memory unless on_device is set, in which case it is a device pointer and
- * the final copy to the host is skipped. */
+ * the final copy to the host is skipped.  PER_STEP (OutputType::OutputPerStep)
+ * writes, for each path step k < n_steps, the mean radiance gathered at that
+ * step, and cuts every path after n_steps steps; MegaKernel approach only, as
+ * in the reference. */
 typedef struct {
   uint32_t type;      /* path_output_type */
-  void *data;         /* BGRA: 4 bytes/pixel (B,G,R,0); FLOAT_RGB: 3 floats */
+  void *data;         /* BGRA: 4 bytes/location (B,G,R,0); FLOAT_RGB: 3
+                         floats/location; PER_STEP: [n_steps][locations][3] */
   uint32_t on_device;
+  uint32_t n_steps;   /* PER_STEP: 1..PATH_MAX_OUTPUT_STEPS */
 } path_output;
 
 typedef struct path_scene path_scene;
@@ -246,6 +265,16 @@ path_status path_sbvh_build(const float *triangles, uint32_t n,
                             const path_settings *settings, uint32_t *sizes,
                             uint32_t *node_words, float *node_aabbs,
                             uint32_t *extra_idxs, uint32_t *permutation);
+/* The compressed 8-wide BVH the GPU traverses, collapsed from the SBVH the
+ * same settings build (GB300 addition, no counterpart in the reference;
+ * for inspection and tests).  sizes receives [n_nodes, n_leaf_refs, depth];
+ * nodes = n_nodes records of 80 bytes (quantised child boxes, see
+ * path_gb300/csrc/devtypes.h WideNode); leaf_refs = BVH-order triangle index
+ * of every wide-leaf entry; permutation = BVH order -> input order.  The
+ * arrays may be NULL to query sizes. */
+path_status path_wide_build(const float *triangles, uint32_t n,
+                            const path_settings *settings, uint32_t *sizes,
+                            void *nodes, uint32_t *leaf_refs, uint32_t *permutation);
 /* closest hit of each ray against the triangle soup on the GPU
  * (AccelRef::intersect_objects with Triangle::intersect): idx = original
  * triangle index or -1, t = distance (NaN when none).  rays/idx/t are host

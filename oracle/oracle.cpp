@@ -1358,6 +1358,8 @@ Ray initial_ray(float x, float y, unsigned x_dim, unsigned y_dim,
   return r;
 }
 
+Ray read_ray(const float *p);
+
 struct RenderCtx {
   const FlatScene *scene;
   const BVH *bvh;
@@ -1365,19 +1367,31 @@ struct RenderCtx {
   const SobolTable *sobol;
   Affine f2w;
   unsigned x_dim, y_dim;
+  const float *rays = nullptr; // InitialRays / InitialIdxAndDir: one ray per location
+  const unsigned *idxs = nullptr; // InitialIdxAndDir: BVH-order hit triangle per location
+  unsigned n_steps = 0;           // OutputPerStep: steps per path, 0 = off
 };
 
 // rendering_equation.h:27-129 + rendering_equation_iteration.h:9-153 for one
 // camera sample, with one light sample per vertex (RandomTriangle) or none.
+// With OutputPerStep (steps != nullptr) the radiance gathered in pass k is
+// added to steps[k] and the path stops after c.n_steps passes
+// (rendering_equation.h:61-124).
 RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
-                     unsigned y) {
+                     unsigned y, RGB *steps = nullptr) {
   const FlatScene &sc = *c.scene;
   const oracle_settings &st = *c.st;
   unsigned location = x + y * c.x_dim;
   RngState rng = get_generator(*c.sobol, sample_idx, location);
-  float xo = rng.next();
-  float yo = rng.next();
-  Ray ray = initial_ray((float)x + xo, (float)y + yo, c.x_dim, c.y_dim, c.f2w);
+  Ray ray;
+  if (c.rays != nullptr) {
+    // initial_ray_sample.h:47-48: the caller's ray, no RNG draw
+    ray = read_ray(c.rays + 6 * (size_t)x);
+  } else {
+    float xo = rng.next();
+    float yo = rng.next();
+    ray = initial_ray((float)x + xo, (float)y + yo, c.x_dim, c.y_dim, c.f2w);
+  }
 
   unsigned iters = 0;
   bool count_emission = true;
@@ -1393,8 +1407,19 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
   auto include_lighting = [&](const Hit &h) {
     return !st.back_cull_emission || !h.back;
   };
+  unsigned step = 0;
+  auto end_pass = [&]() {
+    if (steps != nullptr) {
+      steps[step] = steps[step] + total;
+      total = rgb_zero();
+    }
+    ++step;
+  };
 
   while (true) {
+    if (steps != nullptr && step >= c.n_steps) {
+      return total;
+    }
     // safety bound shared with the kernels (no counterpart in the reference;
     // no path of the tested settings reaches it)
     if (iters >= 4096) {
@@ -1406,7 +1431,15 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
       light_hit = bvh_intersect(*c.bvh, light_ray);
     }
     if (has_next) {
-      next_hit = bvh_intersect(*c.bvh, ray);
+      if (step == 0 && c.idxs != nullptr) {
+        // initial_ray_sample.h:58-74: the caller's hit, distance 1, front
+        next_hit.ok = true;
+        next_hit.t = 1.f;
+        next_hit.back = false;
+        next_hit.idx = c.idxs[x];
+      } else {
+        next_hit = bvh_intersect(*c.bvh, ray);
+      }
     }
     if (has_light) {
       if (light_hit.ok &&
@@ -1416,10 +1449,8 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
         total = total + sc.materials[d.material].emission * light_mult;
       }
     }
-    if (!has_next) {
-      return total;
-    }
-    if (!next_hit.ok) {
+    if (!has_next || !next_hit.ok) {
+      end_pass();
       return total;
     }
     V3 point = ray.o + ray.d * next_hit.t;
@@ -1482,9 +1513,11 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
     } else {
       has_next = false;
       if (!has_light) {
+        end_pass();
         return total;
       }
     }
+    end_pass();
   }
 }
 
@@ -1630,41 +1663,62 @@ struct Reducer {
 
 // one "kernel launch" of the CPU execution model
 // (include/kernel/kernel_launch_impl_cpu.h:10-26): blocks in parallel,
-// threads of a block in order; per-thread values reduced over
-// reduction_factor lanes (runtime_constants_reducer.h:46-62 for CPU order)
+// threads of a block in order; each thread yields n_vals values, each
+// reduced over reduction_factor lanes (runtime_constants_reducer.h:46-62
+// for CPU order) and handed to out_fn(block, info, value index, total)
 template <typename ThreadFn, typename OutFn>
-void run_blocks(const oracle_work_division &w, unsigned n_threads_omp,
-                unsigned order, ThreadFn thread_fn, OutFn out_fn) {
+void run_blocks_n(const oracle_work_division &w, unsigned n_threads_omp,
+                  unsigned order, unsigned n_vals, ThreadFn thread_fn, OutFn out_fn) {
   unsigned nb = total_blocks(w);
   int nt = n_threads_omp ? (int)n_threads_omp : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
   for (unsigned block = 0; block < nb; ++block) {
-    std::vector<RGB> vals(w.block_size, rgb_zero());
+    // vals[k * block_size + t]: value k of thread t
+    std::vector<RGB> vals((size_t)n_vals * w.block_size, rgb_zero());
+    std::vector<RGB> mine(n_vals);
     std::vector<ThreadInfo> infos(w.block_size);
     for (unsigned t = 0; t < w.block_size; ++t) {
       infos[t] = thread_info(w, block, t);
       if (!infos[t].exit) {
-        vals[t] = thread_fn(block, infos[t]);
+        std::fill(mine.begin(), mine.end(), rgb_zero());
+        thread_fn(block, infos[t], mine.data());
+        for (unsigned k = 0; k < n_vals; ++k) {
+          vals[(size_t)k * w.block_size + t] = mine[k];
+        }
       }
     }
     unsigned rf = w.sample_block_size;
     auto add = [](RGB a, RGB b) { return a + b; };
-    for (unsigned t = 0; t < w.block_size; t += rf) {
-      if (infos[t].exit) {
-        continue;
-      }
-      RGB total;
-      if (order == 0) {
-        total = vals[t];
-        for (unsigned k = 1; k < rf; ++k) {
-          total = add(total, vals[t + k]);
+    for (unsigned k = 0; k < n_vals; ++k) {
+      const RGB *v = vals.data() + (size_t)k * w.block_size;
+      for (unsigned t = 0; t < w.block_size; t += rf) {
+        if (infos[t].exit) {
+          continue;
         }
-      } else {
-        total = tree_reduce(vals.data(), w.block_size, rf, t, add);
+        RGB total;
+        if (order == 0) {
+          total = v[t];
+          for (unsigned j = 1; j < rf; ++j) {
+            total = add(total, v[t + j]);
+          }
+        } else {
+          total = tree_reduce(v, w.block_size, rf, t, add);
+        }
+        out_fn(block, infos[t], k, total);
       }
-      out_fn(block, infos[t], total);
     }
   }
+}
+
+template <typename ThreadFn, typename OutFn>
+void run_blocks(const oracle_work_division &w, unsigned n_threads_omp,
+                unsigned order, ThreadFn thread_fn, OutFn out_fn) {
+  run_blocks_n(
+      w, n_threads_omp, order, 1,
+      [&](unsigned block, const ThreadInfo &ti, RGB *out) { out[0] = thread_fn(block, ti); },
+      [&](unsigned block, const ThreadInfo &ti, unsigned, RGB total) {
+        out_fn(block, ti, total);
+      });
 }
 
 struct RenderOut {
@@ -1673,10 +1727,16 @@ struct RenderOut {
 
 // include/render/detail/integrate_image/assign_output.h:11-31 and
 // mega_kernel/reduce_float_rgb_impl.h:17-63
+struct SpecExtras {
+  const float *rays = nullptr;      // InitialRays / InitialIdxAndDir
+  const uint32_t *idxs = nullptr;   // InitialIdxAndDir, scene-order triangles
+  unsigned n_steps = 0;             // OutputPerStep
+};
+
 bool render_image(const oracle_scene &scene, const oracle_settings &st,
                   unsigned spp, unsigned x_dim, unsigned y_dim,
                   const float *f2w, unsigned row_start, unsigned row_end,
-                  RenderOut &out, double *seconds) {
+                  RenderOut &out, double *seconds, const SpecExtras &ex = SpecExtras()) {
   FlatScene sc = flatten(scene);
   if (st.light_sampler != 0) {
     sc.light_tris.clear();
@@ -1692,64 +1752,92 @@ bool render_image(const oracle_scene &scene, const oracle_settings &st,
   if (!make_division(st.render_wd, spp, x_dim, y_dim, w)) {
     return false;
   }
-  RenderCtx ctx{&sc, &bvh, &st, &sobol, read_affine(f2w), x_dim, y_dim};
+  float identity[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  std::vector<unsigned> bvh_idxs;
+  if (ex.idxs != nullptr) {
+    std::vector<unsigned> orig_to_bvh(bvh.permutation.size());
+    for (size_t i = 0; i < bvh.permutation.size(); ++i) {
+      orig_to_bvh[bvh.permutation[i]] = (unsigned)i;
+    }
+    bvh_idxs.resize(x_dim);
+    for (unsigned i = 0; i < x_dim; ++i) {
+      if (ex.idxs[i] >= orig_to_bvh.size()) {
+        return false;
+      }
+      bvh_idxs[i] = orig_to_bvh[ex.idxs[i]];
+    }
+  }
+  RenderCtx ctx{&sc, &bvh, &st, &sobol, read_affine(f2w ? f2w : identity), x_dim, y_dim,
+                ex.rays, ex.idxs ? bvh_idxs.data() : nullptr, ex.n_steps};
+  const unsigned n_out = ex.n_steps ? ex.n_steps : 1;
+  const size_t n_pix = (size_t)x_dim * y_dim;
   auto t0 = std::chrono::steady_clock::now();
   unsigned nsb = w.num_sample_blocks;
-  std::vector<RGB> partial((size_t)nsb * x_dim * y_dim, rgb_zero());
-  out.rgb.assign((size_t)x_dim * y_dim, rgb_zero());
-  run_blocks(
-      w, st.n_threads, st.reduce_order,
-      [&](unsigned, const ThreadInfo &ti) -> RGB {
+  // partial[k][...]: output step k (one image unless OutputPerStep)
+  std::vector<std::vector<RGB>> partial(n_out,
+                                        std::vector<RGB>((size_t)nsb * n_pix, rgb_zero()));
+  run_blocks_n(
+      w, st.n_threads, st.reduce_order, n_out,
+      [&](unsigned, const ThreadInfo &ti, RGB *vals) {
         if (ti.y < row_start || ti.y >= row_end) {
-          return rgb_zero();
+          return;
+        }
+        if (ex.n_steps) {
+          for (unsigned s = ti.start; s < ti.end; ++s) {
+            integrate_sample(ctx, s, ti.x, ti.y, vals);
+          }
+          return;
         }
         RGB total = rgb_zero();
         for (unsigned s = ti.start; s < ti.end; ++s) {
           total = total + integrate_sample(ctx, s, ti.x, ti.y);
         }
-        return total;
+        vals[0] = total;
       },
-      [&](unsigned block, const ThreadInfo &ti, RGB total) {
+      [&](unsigned block, const ThreadInfo &ti, unsigned k, RGB total) {
         unsigned sb = block % nsb;
         size_t idx = sb + (size_t)nsb * (ti.x + ti.y * x_dim);
         if (nsb == 1) {
           total = total / (float)spp;
         }
-        partial[idx] = total;
+        partial[k][idx] = total;
       });
-  // ReduceFloatRGB: repeated WorkDivision over the partial sums
-  unsigned reduction_factor = nsb;
-  std::vector<RGB> in = partial;
-  while (reduction_factor != 1) {
-    unsigned xd = (unsigned)(in.size() / reduction_factor);
-    oracle_work_division rw;
-    if (!make_division(st.reduce_wd, reduction_factor, xd, 1, rw)) {
-      return false;
+  out.rgb.assign(n_out * n_pix, rgb_zero());
+  for (unsigned k = 0; k < n_out; ++k) {
+    // ReduceFloatRGB: repeated WorkDivision over the partial sums
+    unsigned reduction_factor = nsb;
+    std::vector<RGB> in = partial[k];
+    while (reduction_factor != 1) {
+      unsigned xd = (unsigned)(in.size() / reduction_factor);
+      oracle_work_division rw;
+      if (!make_division(st.reduce_wd, reduction_factor, xd, 1, rw)) {
+        return false;
+      }
+      unsigned rnsb = rw.num_sample_blocks;
+      std::vector<RGB> next((size_t)xd * rnsb, rgb_zero());
+      run_blocks(
+          rw, st.n_threads, st.reduce_order,
+          [&](unsigned, const ThreadInfo &ti) -> RGB {
+            RGB total = rgb_zero();
+            for (unsigned i = ti.start; i < ti.end; ++i) {
+              total = total + in[i + (size_t)ti.x * reduction_factor];
+            }
+            return total;
+          },
+          [&](unsigned block, const ThreadInfo &ti, RGB total) {
+            unsigned sb = block % rnsb;
+            size_t idx = sb + (size_t)rnsb * ti.x;
+            if (rnsb == 1) {
+              total = total / (float)spp;
+            }
+            next[idx] = total;
+          });
+      reduction_factor = rnsb;
+      in.swap(next);
     }
-    unsigned rnsb = rw.num_sample_blocks;
-    std::vector<RGB> next((size_t)xd * rnsb, rgb_zero());
-    run_blocks(
-        rw, st.n_threads, st.reduce_order,
-        [&](unsigned, const ThreadInfo &ti) -> RGB {
-          RGB total = rgb_zero();
-          for (unsigned i = ti.start; i < ti.end; ++i) {
-            total = total + in[i + (size_t)ti.x * reduction_factor];
-          }
-          return total;
-        },
-        [&](unsigned block, const ThreadInfo &ti, RGB total) {
-          unsigned sb = block % rnsb;
-          size_t idx = sb + (size_t)rnsb * ti.x;
-          if (rnsb == 1) {
-            total = total / (float)spp;
-          }
-          next[idx] = total;
-        });
-    reduction_factor = rnsb;
-    in.swap(next);
-  }
-  for (size_t i = 0; i < out.rgb.size(); ++i) {
-    out.rgb[i] = in[i];
+    for (size_t i = 0; i < n_pix; ++i) {
+      out.rgb[k * n_pix + i] = in[i];
+    }
   }
   auto t1 = std::chrono::steady_clock::now();
   if (seconds) {
@@ -1973,6 +2061,47 @@ int oracle_render(const oracle_scene *scene, const oracle_settings *settings,
 }
 
 // include/lib/bgra_32.h:12-31 with tone_map v / (v + 1)
+// InitialRays (idxs == NULL) and InitialIdxAndDir sample specs: location x
+// renders entry x (x_dim = n_rays, y_dim = 1, mega_kernel/run_impl.h:56-67).
+// n_steps == 0: out = [n_rays][3]; OutputPerStep: out = [n_steps][n_rays][3]
+int oracle_render_rays(const oracle_scene *scene, const oracle_settings *settings,
+                       uint32_t samples_per, const float *rays, const uint32_t *idxs,
+                       uint32_t n_rays, uint32_t n_steps, float *out) {
+  RenderOut r;
+  SpecExtras ex;
+  ex.rays = rays;
+  ex.idxs = idxs;
+  ex.n_steps = n_steps;
+  if (!render_image(*scene, *settings, samples_per, n_rays, 1, nullptr, 0, 1, r, nullptr, ex)) {
+    return 1;
+  }
+  for (size_t i = 0; i < r.rgb.size(); ++i) {
+    out[3 * i] = r.rgb[i].r;
+    out[3 * i + 1] = r.rgb[i].g;
+    out[3 * i + 2] = r.rgb[i].b;
+  }
+  return 0;
+}
+
+// OutputPerStep of a square image: out = [n_steps][y_dim * x_dim][3]
+int oracle_render_steps(const oracle_scene *scene, const oracle_settings *settings,
+                        uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
+                        const float *film_to_world, uint32_t n_steps, float *out) {
+  RenderOut r;
+  SpecExtras ex;
+  ex.n_steps = n_steps;
+  if (n_steps == 0 || !render_image(*scene, *settings, samples_per, x_dim, y_dim,
+                                    film_to_world, 0, y_dim, r, nullptr, ex)) {
+    return 1;
+  }
+  for (size_t i = 0; i < r.rgb.size(); ++i) {
+    out[3 * i] = r.rgb[i].r;
+    out[3 * i + 1] = r.rgb[i].g;
+    out[3 * i + 2] = r.rgb[i].b;
+  }
+  return 0;
+}
+
 int oracle_render_bgra(const oracle_scene *scene,
                        const oracle_settings *settings, uint32_t samples_per,
                        uint32_t x_dim, uint32_t y_dim,

@@ -169,6 +169,18 @@ int oracle_render(const oracle_scene *scene, const oracle_settings *settings,
                   const float *film_to_world, uint32_t row_start,
                   uint32_t row_end, float *out, double *seconds);
 
+/* InitialRays (idxs NULL) or InitialIdxAndDir (idxs = scene-order triangle
+ * hit at distance 1 along each ray) sample spec.  out = [n_rays][3]
+ * FloatRGB, or [n_steps][n_rays][3] with OutputPerStep (n_steps > 0). */
+int oracle_render_rays(const oracle_scene *scene, const oracle_settings *settings,
+                       uint32_t samples_per, const float *rays, const uint32_t *idxs,
+                       uint32_t n_rays, uint32_t n_steps, float *out);
+
+/* OutputPerStep of a square image: out = [n_steps][y_dim * x_dim][3] */
+int oracle_render_steps(const oracle_scene *scene, const oracle_settings *settings,
+                        uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
+                        const float *film_to_world, uint32_t n_steps, float *out);
+
 /* render with BGRA32 output: out = [y_dim * x_dim][4] bytes */
 int oracle_render_bgra(const oracle_scene *scene,
                        const oracle_settings *settings, uint32_t samples_per,

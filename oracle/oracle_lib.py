@@ -109,6 +109,12 @@ def load():
         lib.oracle_render.argtypes = [ctypes.POINTER(OracleScene),
                                       ctypes.POINTER(OracleSettings), c_u32, c_u32, c_u32, _PF,
                                       c_u32, c_u32, _PF, ctypes.POINTER(ctypes.c_double)]
+        lib.oracle_render_rays.argtypes = [ctypes.POINTER(OracleScene),
+                                           ctypes.POINTER(OracleSettings), c_u32, _PF, _PU,
+                                           c_u32, c_u32, _PF]
+        lib.oracle_render_steps.argtypes = [ctypes.POINTER(OracleScene),
+                                            ctypes.POINTER(OracleSettings), c_u32, c_u32, c_u32,
+                                            _PF, c_u32, _PF]
         lib.oracle_render_bgra.argtypes = [ctypes.POINTER(OracleScene),
                                            ctypes.POINTER(OracleSettings), c_u32, c_u32, c_u32,
                                            _PF, ctypes.POINTER(ctypes.c_uint8)]
@@ -326,6 +332,34 @@ def render_samples(scene_arrays, settings, samples_per, x_dim, y_dim, film_to_wo
     f2w = np.ascontiguousarray(film_to_world, np.float32).reshape(12)
     rc = load().oracle_render_samples(ctypes.byref(scene_arrays.c), ctypes.byref(settings),
                                       samples_per, x_dim, y_dim, _f(f2w), x, y, _f(out))
+    if rc != 0:
+        raise RuntimeError("oracle render failed")
+    return out
+
+
+def render_rays(scene_arrays, settings, samples_per, rays, idxs=None, n_steps=0):
+    """InitialRays (idxs None) / InitialIdxAndDir radiance: [n_rays, 3], or
+    [n_steps, n_rays, 3] with OutputPerStep."""
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    shape = (n_steps, len(rays), 3) if n_steps else (len(rays), 3)
+    out = np.zeros(shape, np.float32)
+    ip = None
+    if idxs is not None:
+        idxs = np.ascontiguousarray(idxs, np.uint32).reshape(-1)
+        ip = _u(idxs)
+    rc = load().oracle_render_rays(ctypes.byref(scene_arrays.c), ctypes.byref(settings),
+                                   samples_per, _f(rays), ip, len(rays), n_steps, _f(out))
+    if rc != 0:
+        raise RuntimeError("oracle render failed")
+    return out
+
+
+def render_steps(scene_arrays, settings, samples_per, x_dim, y_dim, film_to_world, n_steps):
+    """OutputPerStep of a square image: [n_steps, y_dim, x_dim, 3]."""
+    f2w = np.ascontiguousarray(film_to_world, np.float32).reshape(12)
+    out = np.zeros((n_steps, y_dim, x_dim, 3), np.float32)
+    rc = load().oracle_render_steps(ctypes.byref(scene_arrays.c), ctypes.byref(settings),
+                                    samples_per, x_dim, y_dim, _f(f2w), n_steps, _f(out))
     if rc != 0:
         raise RuntimeError("oracle render failed")
     return out

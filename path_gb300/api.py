@@ -178,6 +178,50 @@ class SquareImage:
         return s
 
 
+class InitialRays:
+    """render::SampleSpec InitialRays: one output value per caller ray
+    (origin xyz, unit direction xyz); the camera draws no random numbers."""
+
+    def __init__(self, rays):
+        self.rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+
+    def to_c(self):
+        s = capi.SampleSpec()
+        s.type = capi.SAMPLE_INITIAL_RAYS
+        s.rays = self.rays.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        s.n_rays = self.rays.shape[0]
+        return s
+
+
+class InitialIdxAndDir:
+    """render::InitialIdxAndDirSpec list (include/render/renderer.h:31-35):
+    each path starts at triangle idxs[i] (scene order) hit at distance 1
+    along rays[i] (origin xyz, unit direction xyz), front side."""
+
+    def __init__(self, idxs, rays):
+        self.idxs = np.ascontiguousarray(idxs, np.uint32).reshape(-1)
+        self.rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        if self.idxs.shape[0] != self.rays.shape[0]:
+            raise ValueError("one triangle index per ray")
+
+    def to_c(self):
+        s = capi.SampleSpec()
+        s.type = capi.SAMPLE_INITIAL_IDX_AND_DIR
+        s.rays = self.rays.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        s.idxs = _uptr(self.idxs)
+        s.n_rays = self.rays.shape[0]
+        return s
+
+
+class OutputPerStep:
+    """OutputType::OutputPerStep: float32 array [n_steps, ..., 3] (numpy, or a
+    torch tensor on the host or the GPU) receiving each path step's radiance."""
+
+    def __init__(self, array):
+        self.array = array
+        self.n_steps = int(array.shape[0])
+
+
 class Renderer:
     """render::Renderer: caches the scene's accel and device buffers."""
 
@@ -197,9 +241,16 @@ class Renderer:
         """Render into ``output``; returns the reference's timed seconds.
 
         output: numpy float32 [H, W, 3] (FloatRGB) or uint8 [H, W, 4] (BGRA) in
-        host memory, or a torch CUDA tensor of the same shape (device output).
+        host memory, or a torch CUDA tensor of the same shape (device output);
+        or an ``OutputPerStep`` wrapping [n_steps, H, W, 3] float32.
         """
         o = capi.Output()
+        if isinstance(output, OutputPerStep):
+            o.n_steps = output.n_steps
+            output = output.array
+            per_step = True
+        else:
+            per_step = False
         dtype = getattr(output, "dtype", None)
         is_torch = hasattr(output, "data_ptr")
         if is_torch:
@@ -215,6 +266,8 @@ class Renderer:
             o.type = capi.OUTPUT_BGRA if dtype == np.uint8 else capi.OUTPUT_FLOAT_RGB
             o.data = output.ctypes.data
             o.on_device = 0
+        if per_step:
+            o.type = capi.OUTPUT_PER_STEP
         spec = sample_spec.to_c()
         secs = ctypes.c_double()
         capi.check(capi.load().path_render(self._h, int(execution_model), ctypes.byref(spec),
@@ -276,6 +329,30 @@ def sbvh_build(triangles, settings):
                                    _uptr(words), _fptr(boxes), _uptr(extra), _uptr(perm)))
     return {"node_words": words, "node_aabbs": boxes, "extra_idxs": extra[:sizes[1]],
             "permutation": perm[:n]}
+
+
+WIDE_NODE_DTYPE = np.dtype([("p", "<f4", 3), ("e", "u1", 3), ("imask", "u1"),
+                            ("child_base", "<u4"), ("tri_base", "<u4"), ("meta", "u1", 8),
+                            ("qlo", "u1", (3, 8)), ("qhi", "u1", (3, 8))])
+
+
+def wide_build(triangles, settings):
+    """The 8-wide BVH the GPU traverses: dict of nodes (WIDE_NODE_DTYPE
+    records), leaf_refs (BVH-order triangle per wide-leaf entry), permutation
+    (BVH order -> input order) and depth."""
+    tris = np.ascontiguousarray(triangles, np.float32).reshape(-1, 9)
+    n = tris.shape[0]
+    sizes = (ctypes.c_uint32 * 3)()
+    lib = capi.load()
+    capi.check(lib.path_wide_build(_fptr(tris), n, ctypes.byref(settings.raw), sizes, None, None,
+                                   None))
+    nodes = np.zeros(sizes[0], WIDE_NODE_DTYPE)
+    refs = np.zeros(max(sizes[1], 1), np.uint32)
+    perm = np.zeros(max(n, 1), np.uint32)
+    capi.check(lib.path_wide_build(_fptr(tris), n, ctypes.byref(settings.raw), sizes,
+                                   nodes.ctypes.data, _uptr(refs), _uptr(perm)))
+    return {"nodes": nodes, "leaf_refs": refs[:sizes[1]], "permutation": perm[:n],
+            "depth": sizes[2]}
 
 
 def sobol_table(dimension_bound, count, use_curand=False):

@@ -42,17 +42,19 @@ class PathSettings(ctypes.Structure):
                 ("term_prob_min_prob", c_f32), ("rng", c_u32), ("max_sample_size", c_u32),
                 ("back_cull_emission", c_u32), ("traversal", c_u32),
                 ("persistent_ctas_per_sm", c_u32), ("count_work", c_u32),
-                ("upload_scene_every_render", c_u32), ("reserved", c_u32 * 4)]
+                ("upload_scene_every_render", c_u32), ("trace_min_blocks", c_u32),
+                ("reserved", c_u32 * 3)]
 
 
 class SampleSpec(ctypes.Structure):
     _fields_ = [("type", c_u32), ("x_dim", c_u32), ("y_dim", c_u32),
                 ("film_to_world", c_f32 * 12), ("rays", ctypes.POINTER(c_f32)),
-                ("n_rays", c_u32)]
+                ("n_rays", c_u32), ("idxs", ctypes.POINTER(c_u32))]
 
 
 class Output(ctypes.Structure):
-    _fields_ = [("type", c_u32), ("data", ctypes.c_void_p), ("on_device", c_u32)]
+    _fields_ = [("type", c_u32), ("data", ctypes.c_void_p), ("on_device", c_u32),
+                ("n_steps", c_u32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -72,8 +74,9 @@ STATUS_NAMES = {0: "PATH_OK", 1: "PATH_ERR_ARGUMENT", 2: "PATH_ERR_SCENE_PARSE",
 EXEC_CPU, EXEC_GPU = 0, 1
 BSDF = {"Diffuse": 0, "Glossy": 1, "DiffuseGlossy": 2, "DiffuseMirror": 3, "Mirror": 4,
         "DielectricRefractive": 5, "GGX": 6}
-SAMPLE_SQUARE_IMAGE, SAMPLE_INITIAL_RAYS = 0, 1
-OUTPUT_BGRA, OUTPUT_FLOAT_RGB = 0, 1
+SAMPLE_SQUARE_IMAGE, SAMPLE_INITIAL_RAYS, SAMPLE_INITIAL_IDX_AND_DIR = 0, 1, 2
+OUTPUT_BGRA, OUTPUT_FLOAT_RGB, OUTPUT_PER_STEP = 0, 1, 2
+MAX_OUTPUT_STEPS = 64
 TRAVERSAL_BINARY, TRAVERSAL_WIDE8 = 0, 1
 TERM = {"Constant": 0, "NIters": 1, "MultiplierFunc": 2, "Normalize": 3}
 
@@ -104,6 +107,8 @@ SIGNATURES = {
     "path_renderer_stats": (ctypes.c_int, [_P, ctypes.POINTER(RenderStats)]),
     "path_sbvh_build": (ctypes.c_int, [_PF, c_u32, ctypes.POINTER(PathSettings), _PU, _PU, _PF,
                                        _PU, _PU]),
+    "path_wide_build": (ctypes.c_int, [_PF, c_u32, ctypes.POINTER(PathSettings), _PU, _P, _PU,
+                                       _PU]),
     "path_intersect": (ctypes.c_int, [_P, _PF, c_u32, _PF, c_u32, ctypes.POINTER(PathSettings),
                                       _PI, _PF]),
     "path_sobol_table": (ctypes.c_int, [c_u32, c_u32, _PF]),

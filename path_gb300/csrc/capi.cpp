@@ -5,6 +5,7 @@
 #include "renderer.h"
 #include "scene.h"
 #include "sbvh.h"
+#include "wide.h"
 #include "settings.h"
 #include "workdiv.h"
 
@@ -289,6 +290,42 @@ path_status path_renderer_stats(const path_renderer *renderer, path_render_stats
   }
   *out = renderer->r.stats();
   return PATH_OK;
+}
+
+path_status path_wide_build(const float *triangles, uint32_t n, const path_settings *settings,
+                            uint32_t *sizes, void *nodes, uint32_t *leaf_refs,
+                            uint32_t *permutation) {
+  if ((n > 0 && !triangles) || !settings || !sizes) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    std::vector<pg::f3> a(n), b(n), c(n);
+    for (uint32_t i = 0; i < n; ++i) {
+      a[i] = load3(triangles + 9 * (size_t)i);
+      b[i] = load3(triangles + 9 * (size_t)i + 3);
+      c[i] = load3(triangles + 9 * (size_t)i + 6);
+    }
+    pg::SBVHSettings sb;
+    sb.overlap_threshold = settings->overlap_threshold;
+    sb.use_spatial_splits = settings->use_spatial_splits != 0;
+    sb.traversal_per_intersect_cost = settings->traversal_per_intersect_cost;
+    sb.target_objects = settings->target_objects;
+    pg::BinaryBVH bvh = pg::build_sbvh(a.data(), b.data(), c.data(), n, sb);
+    pg::WideBVH wide = pg::build_wide(bvh);
+    sizes[0] = (uint32_t)wide.nodes.size();
+    sizes[1] = (uint32_t)wide.tri_index.size();
+    sizes[2] = wide.depth;
+    if (nodes && !wide.nodes.empty()) {
+      std::memcpy(nodes, wide.nodes.data(), wide.nodes.size() * sizeof(pg::WideNode));
+    }
+    if (leaf_refs && !wide.tri_index.empty()) {
+      std::memcpy(leaf_refs, wide.tri_index.data(), wide.tri_index.size() * 4);
+    }
+    if (permutation && n > 0) {
+      std::memcpy(permutation, bvh.permutation.data(), (size_t)n * 4);
+    }
+    return PATH_OK;
+  });
 }
 
 path_status path_sbvh_build(const float *triangles, uint32_t n, const path_settings *settings,

@@ -59,6 +59,8 @@ static_assert(sizeof(WideNode) == 80, "WideNode is 80 bytes");
 
 constexpr uint32_t kMaxLeafTris = 7;      // 3-bit count in meta
 constexpr uint32_t kMaxNodeTris = 32;     // 5-bit offset in meta
+// node groups a wide traversal keeps waiting: at most one per tree level
+constexpr uint32_t kWideStackDepth = 64;
 
 // device status word codes (first error wins)
 enum DeviceStatus : uint32_t {
@@ -74,5 +76,7 @@ enum DeviceStatus : uint32_t {
 // termination setting never ends a path.  No path of the built settings
 // comes near it (NIters ends a path after iters + 1 vertices).
 constexpr uint32_t kMaxPathVertices = 4096;
+// most path steps of an OutputPerStep render
+constexpr uint32_t kMaxOutputSteps = 64;
 
 } // namespace pg

@@ -151,9 +151,7 @@ __device__ Hit trace_binary(const RenderParams &P, const ray &r, Counts &cnt) {
 // which covers the error of the fused form against the exact plane
 // p + q 2^e (an exactly representable float, see wide.cpp) several times
 // over.  Decoded boxes contain the binary SBVH's boxes, so every box the
-// reference's slab test accepts is accepted here too.  Leaves are tested in
-// slot order; internal hits are visited nearest first, the rest kept on a
-// stack of (node, entry distance) that is culled against the current best.
+// reference's slab test accepts is accepted here too.
 __device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i) {
   uint32_t w = i < 4 ? lo : hi;
   return (w >> (8 * (i & 3))) & 0xffu;
@@ -172,37 +170,79 @@ __device__ __forceinline__ float byte8_float(uint32_t lo, uint32_t hi, int i) {
   return byte_float(i < 4 ? lo : hi, i & 3);
 }
 
-constexpr int kWideStack = 128;
+constexpr int kWideStack = (int)kWideStackDepth;
 
-// traversal state of one ray through the wide BVH
+// Order-independent closest hit of the wide traversal: the smallest
+// distance wins and, at equal distance, the smallest BVH-order index, so the
+// result does not depend on the order in which nodes are visited.  With
+// best.ok false, best.t is the caller's distance limit (hits at or below it
+// are taken).
+__device__ __forceinline__ void fold_min(Hit &best, float t, bool back, uint32_t idx) {
+  if (t < best.t || (t == best.t && (!best.ok || idx < best.idx))) {
+    best.ok = true;
+    best.t = t;
+    best.back = back;
+    best.idx = idx;
+  }
+}
+
+// Traversal state of one ray through the wide BVH.  A node group is the set
+// of a visited node's internal children the ray still has to enter: their
+// first node index and the node's internal-slot mask (bits 0-7) plus the
+// entered children as bits 8-15 in ray order (bit 8 + (slot ^ oct)).  The
+// builder puts the child nearest the low corner of every axis in slot 0,
+// the one on the high side of axis a in slots with bit a set, so the lowest
+// ray-order bit is approximately the nearest child along the ray.
 struct WideWalk {
   ray r;
   f3 inv;
   Hit best;   // best.t is the pruning distance: tlimit until the first hit
-  uint32_t node;
+  uint32_t oct;
+  uint32_t ng_base, ng_bits;
   int sp;
   bool done;
 };
 
 // tlimit: hits beyond it are not wanted (shadow rays only need hits up to
 // just past the light); INF for extension rays.  Within the limit the
-// closest hit and the equal-distance rule are the same as without it.
+// closest hit is the same as without it.
 __device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, const ray &r,
                                            float tlimit) {
   w.r = r;
   w.inv = inv_dir(r.d);
   w.best = no_hit();
   w.best.t = tlimit;
-  w.node = 0;
+  w.oct = (w.inv.x < 0.f ? 1u : 0u) | (w.inv.y < 0.f ? 2u : 0u) | (w.inv.z < 0.f ? 4u : 0u);
+  // the root as the only child of a pseudo node in slot 0
+  w.ng_base = 0;
+  w.ng_bits = 1u | (1u << (8 + w.oct));
   w.sp = 0;
   w.done = P.n_wide_nodes == 0;
 }
 
-// visit w.node, then move to the next node or finish
+// One traversal step: enter the next child of the current node group, test
+// its eight slots, test the triangles of the leaf slots it hits, then make
+// its internal hits the current group (the rest of the old group waits on
+// the stack) or take a group from the stack.
 template <bool kCount>
-__device__ __forceinline__ void wide_visit(const RenderParams &P, WideWalk &w,
-                                           uint32_t *st_node, float *st_t, Counts &cnt) {
-  const uint4 *np = P.wide_nodes + 5 * (size_t)w.node;
+__device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
+                                          uint32_t *st_base, uint32_t *st_bits, Counts &cnt) {
+  const uint32_t j = __ffs(w.ng_bits >> 8) - 1;
+  w.ng_bits &= ~(1u << (8 + j));
+  const uint32_t slot = j ^ w.oct;
+  const uint32_t node = w.ng_base + __popc(w.ng_bits & ((1u << slot) - 1u));
+  if ((w.ng_bits >> 8) != 0) {
+    if (w.sp >= kWideStack) {
+      set_status(P.status, kStatusStackOverflow);
+      w.best = no_hit();
+      w.done = true;
+      return;
+    }
+    st_base[w.sp] = w.ng_base;
+    st_bits[w.sp] = w.ng_bits;
+    ++w.sp;
+  }
+  const uint4 *np = P.wide_nodes + 5 * (size_t)node;
   const uint4 n0 = __ldg(np);
   const uint4 n1 = __ldg(np + 1);
   const uint4 n2 = __ldg(np + 2);
@@ -226,26 +266,18 @@ __device__ __forceinline__ void wide_visit(const RenderParams &P, WideWalk &w,
   const float bny = by - ey, bfy = by + ey;
   const float bnz = bz - ez, bfz = bz + ez;
   const uint32_t imask = n0.w >> 24;
-  const uint32_t child_base = n1.x;
-  const uint32_t tri_base = n1.y;
   // near / far plane bytes per axis according to the direction's sign
-  const bool sx = inv.x < 0.f, sy = inv.y < 0.f, sz = inv.z < 0.f;
+  const bool sx = (w.oct & 1u) != 0, sy = (w.oct & 2u) != 0, sz = (w.oct & 4u) != 0;
   const uint32_t nxl = sx ? n3.z : n2.x, nxh = sx ? n3.w : n2.y;
   const uint32_t fxl = sx ? n2.x : n3.z, fxh = sx ? n2.y : n3.w;
   const uint32_t nyl = sy ? n4.x : n2.z, nyh = sy ? n4.y : n2.w;
   const uint32_t fyl = sy ? n2.z : n4.x, fyh = sy ? n2.w : n4.y;
   const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
   const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
-  float ct[8];
-  uint32_t cn[8];
-  int n_int = 0;
+  const float tcull = w.best.t;
+  uint32_t hits = 0, tmask = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const uint32_t meta = byte_of(n1.z, n1.w, i);
-    const bool internal = (imask >> i) & 1u;
-    if (!internal && meta == 0) {
-      continue;
-    }
     const float tnx = __fmaf_rn(byte8_float(nxl, nxh, i), ax, bnx);
     const float tfx = __fmaf_rn(byte8_float(fxl, fxh, i), ax, bfx);
     const float tny = __fmaf_rn(byte8_float(nyl, nyh, i), ay, bny);
@@ -254,68 +286,43 @@ __device__ __forceinline__ void wide_visit(const RenderParams &P, WideWalk &w,
     const float tfz = __fmaf_rn(byte8_float(fzl, fzh, i), az, bfz);
     const float tmin = fmaxf(fmaxf(tnx, tny), tnz);
     const float tmax = fminf(fminf(tfx, tfy), tfz);
-    if (!(tmin <= tmax) || tmax < 0.f || !(tmin < w.best.t)) {
-      continue;
-    }
-    if (internal) {
-      ct[n_int] = tmin;
-      cn[n_int] = child_base + meta;
-      ++n_int;
-    } else {
-      const uint32_t count = meta >> 5;
-      const uint32_t first = tri_base + (meta & 31u);
-      for (uint32_t k = 0; k < count; ++k) {
-        const float4 *tp = P.wide_tris + 3 * (size_t)(first + k);
-        const float4 a = __ldg(tp);
-        const float4 b = __ldg(tp + 1);
-        const float4 c = __ldg(tp + 2);
-        if (kCount) {
-          ++cnt.tris;
-        }
-        float t;
-        bool back;
-        if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), w.r, &t,
-                    &back) &&
-            (w.best.ok || t <= w.best.t)) {
-          fold(w.best, t, back, __float_as_uint(c.y));
-        }
-      }
+    const bool hit = tmin <= tmax && tmax >= 0.f && tmin <= tcull;
+    const uint32_t meta = byte_of(n1.z, n1.w, i);
+    if ((imask >> i) & 1u) {
+      hits |= (hit ? 1u : 0u) << (i ^ (int)w.oct);
+    } else if (hit) {
+      // leaf slot: meta = count << 5 | first triangle offset
+      tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
     }
   }
-  if (n_int > 0) {
-    // nearest internal hit next, the others on the stack far to near
-    for (int i = 1; i < n_int; ++i) {
-      const float kt = ct[i];
-      const uint32_t kn = cn[i];
-      int j = i - 1;
-      while (j >= 0 && ct[j] > kt) {
-        ct[j + 1] = ct[j];
-        cn[j + 1] = cn[j];
-        --j;
-      }
-      ct[j + 1] = kt;
-      cn[j + 1] = kn;
+  const uint32_t tri_base = n1.y;
+  while (tmask != 0) {
+    const uint32_t k = __ffs(tmask) - 1;
+    tmask &= tmask - 1u;
+    const float4 *tp = P.wide_tris + 3 * (size_t)(tri_base + k);
+    const float4 a = __ldg(tp);
+    const float4 b = __ldg(tp + 1);
+    const float4 c = __ldg(tp + 2);
+    if (kCount) {
+      ++cnt.tris;
     }
-    if (w.sp + n_int - 1 > kWideStack) {
-      set_status(P.status, kStatusStackOverflow);
-      w.best = no_hit();
-      w.done = true;
-      return;
+    float t;
+    bool back;
+    if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), w.r, &t, &back)) {
+      fold_min(w.best, t, back, __float_as_uint(c.y));
     }
-    for (int i = n_int - 1; i >= 1; --i) {
-      st_node[w.sp] = cn[i];
-      st_t[w.sp] = ct[i];
-      ++w.sp;
-    }
-    w.node = cn[0];
+  }
+  if (hits != 0) {
+    w.ng_base = n1.x;
+    w.ng_bits = imask | (hits << 8);
     return;
   }
-  while (w.sp > 0) {
+  if (w.sp > 0) {
+    // a waiting group keeps the children it had; the next step culls them
     --w.sp;
-    if (st_t[w.sp] < w.best.t) {
-      w.node = st_node[w.sp];
-      return;
-    }
+    w.ng_base = st_base[w.sp];
+    w.ng_bits = st_bits[w.sp];
+    return;
   }
   w.done = true;
 }
@@ -324,10 +331,10 @@ template <bool kCount>
 __device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, float tlimit) {
   WideWalk w;
   wide_begin(P, w, r, tlimit);
-  uint32_t st_node[kWideStack];
-  float st_t[kWideStack];
+  uint32_t st_base[kWideStack];
+  uint32_t st_bits[kWideStack];
   while (!w.done) {
-    wide_visit<kCount>(P, w, st_node, st_t, cnt);
+    wide_step<kCount>(P, w, st_base, st_bits, cnt);
   }
   return w.best;
 }
@@ -804,16 +811,25 @@ struct PathState {
   Rng rng;
 };
 
-// camera ray of a sample (initial_ray_sample.h:36-56, 2 RNG draws)
+// camera ray of a sample (initial_ray_sample.h:36-56): 2 RNG draws for a
+// square image, the caller's ray for an InitialRays spec
 __device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sample_idx,
                                            uint32_t x, uint32_t y, PathState &s) {
   const uint32_t location = x + y * P.x_dim;
   s.rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
   s.rng.bound = P.dim_bound;
   s.rng.dim = fnv_hash(location) % P.init_dim_bound;
-  float xo = s.rng.next();
-  float yo = s.rng.next();
-  ray r = camera_ray(P, (float)x + xo, (float)y + yo);
+  ray r;
+  if (P.initial_rays != nullptr) {
+    // InitialRays: the caller's ray for this location, no RNG draw
+    const float *q = P.initial_rays + 6 * (size_t)x;
+    r.o = mk(q[0], q[1], q[2]);
+    r.d = mk(q[3], q[4], q[5]);
+  } else {
+    float xo = s.rng.next();
+    float yo = s.rng.next();
+    r = camera_ray(P, (float)x + xo, (float)y + yo);
+  }
   s.o = r.o;
   s.d = r.d;
   s.ld = mk(0.f, 0.f, 0.f);
@@ -911,28 +927,67 @@ __device__ __forceinline__ bool path_continues(const RenderParams &P, PathState 
   return cont;
 }
 
+// closest hits of a path's pending light and extension rays.  The first
+// step of an InitialIdxAndDir sample takes the caller's hit instead of
+// tracing (initial_ray_sample.h:58-74: distance 1, front side).
+template <uint32_t kTrav, bool kCount>
+__device__ __forceinline__ void step_hits(const RenderParams &P, const PathState &s,
+                                          bool first, uint32_t x, Counts &cnt, Hit &lh,
+                                          Hit &nh) {
+  lh = no_hit();
+  nh = no_hit();
+  if (s.has_light) {
+    ray lr;
+    lr.o = s.o;
+    lr.d = s.ld;
+    lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target));
+  }
+  if (first && P.initial_idx != nullptr) {
+    nh.t = 1.f;
+    nh.idx = P.initial_idx[x];
+    nh.ok = true;
+    nh.back = false;
+  } else if (s.has_next) {
+    ray r;
+    r.o = s.o;
+    r.d = s.d;
+    nh = trace<kTrav, kCount>(P, r, cnt, PG_INF);
+  }
+}
+
 // one camera sample of rendering_equation, traced in a loop
 template <uint32_t kTrav, bool kCount>
 __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
                                 uint32_t x, uint32_t y, Counts &cnt) {
   PathState s;
   path_begin(P, sample_idx, x, y, s);
+  bool first = true;
   while (true) {
-    Hit lh = no_hit(), nh = no_hit();
-    if (s.has_light) {
-      ray lr;
-      lr.o = s.o;
-      lr.d = s.ld;
-      lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target));
-    }
-    if (s.has_next) {
-      ray r;
-      r.o = s.o;
-      r.d = s.d;
-      nh = trace<kTrav, kCount>(P, r, cnt, PG_INF);
-    }
+    Hit lh, nh;
+    step_hits<kTrav, kCount>(P, s, first, x, cnt, lh, nh);
+    first = false;
     if (!path_continues(P, s, path_step(P, s, lh, nh))) {
       return s.total;
+    }
+  }
+}
+
+// OutputPerStep (rendering_equation.h:61-124): the radiance gathered in
+// step k is added to steps[k]; a path stops after P.n_steps steps
+template <uint32_t kTrav>
+__device__ void integrate_sample_steps(const RenderParams &P, uint32_t sample_idx,
+                                       uint32_t x, uint32_t y, rgb *steps) {
+  PathState s;
+  path_begin(P, sample_idx, x, y, s);
+  Counts cnt = {0, 0, 0};
+  for (uint32_t k = 0; k < P.n_steps; ++k) {
+    Hit lh, nh;
+    step_hits<kTrav, false>(P, s, k == 0, x, cnt, lh, nh);
+    const bool cont = path_step(P, s, lh, nh);
+    steps[k] = steps[k] + s.total;
+    s.total = zero_rgb();
+    if (!cont) {
+      return;
     }
   }
 }

@@ -29,7 +29,15 @@ struct RenderParams {
   uint32_t light_sampler, dir_sampler, term_prob, term_iters;
   float term_prob_prob, term_exp, term_min_prob;
   uint32_t back_cull, target_objects;
-  // image
+  // camera: film_to_world, or caller rays [x_dim][6] (InitialRays and
+  // InitialIdxAndDir specs)
+  const float *initial_rays;
+  // InitialIdxAndDir: BVH-order triangle hit at distance 1 per location
+  const uint32_t *initial_idx;
+  // OutputPerStep: n_steps > 0 writes step k's partial sums at
+  // out_rgb + k * step_stride (floats)
+  uint32_t n_steps;
+  size_t step_stride;
   float f2w[12];
   uint32_t x_dim, y_dim, spp;
   WorkDiv wd;
@@ -74,9 +82,12 @@ struct WaveParams {
 };
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
+// resident blocks per SM of the trace kernel compiled for min_blocks
+int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting);
 // one trace + shade iteration (three launches)
-cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity, uint32_t grid,
-                                       bool counting, cudaStream_t s);
+cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity,
+                                       uint32_t trace_grid, uint32_t shade_grid,
+                                       uint32_t min_blocks, bool counting, cudaStream_t s);
 // per-pixel sums of the sample buffer into p.out_rgb / p.out_bgra
 cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
                                  cudaStream_t s);
@@ -84,6 +95,9 @@ cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
 // integration megakernel over blocks [start_block, start_block + n_blocks)
 cudaError_t launch_render(const RenderParams &p, uint32_t traversal,
                           uint32_t n_blocks, bool counting, cudaStream_t s);
+// the mega kernel with OutputPerStep output (p.n_steps > 0)
+cudaError_t launch_render_steps(const RenderParams &p, uint32_t traversal,
+                                uint32_t n_blocks, cudaStream_t s);
 
 // one ReduceFloatRGB pass (reduce_float_rgb_impl.h:17-63)
 struct ReduceParams {

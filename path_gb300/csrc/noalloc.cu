@@ -98,9 +98,9 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
                        "Sobol table for this max_sample_size / samples_per not resident: "
                        "render once with path_render");
   }
-  if (st.traversal == PATH_TRAVERSAL_BINARY &&
-      (prep_.bvh.depth + 2 > 64 || st.target_objects + prep_.bvh.max_leaf_size - 1 > 10)) {
-    return Status::err(PATH_ERR_UNSUPPORTED, "SBVH too deep or leaves too large for binary traversal");
+  Status sf = traversal_fits(st);
+  if (!sf.good()) {
+    return sf;
   }
   WorkDiv wd;
   if (!make_workdiv(st.render_work_division, spp, spec.x_dim, spec.y_dim, wd) ||

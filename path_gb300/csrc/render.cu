@@ -39,6 +39,37 @@ __global__ void __launch_bounds__(256) k_render(const RenderParams P) {
   }
 }
 
+// the mega kernel with OutputPerStep output (mega_kernel/run_impl.h:
+// 160-185): per-thread step sums, one sub-block reduction per step
+template <uint32_t kTrav>
+__global__ void __launch_bounds__(256) k_render_steps(const RenderParams P) {
+  const uint32_t block = blockIdx.x + P.start_block;
+  const uint32_t tid = threadIdx.x;
+  const ThreadWork tw = thread_work(P.wd, block, tid);
+  rgb steps[kMaxOutputSteps];
+  for (uint32_t k = 0; k < P.n_steps; ++k) {
+    steps[k] = zero_rgb();
+  }
+  if (!tw.exit) {
+    for (uint32_t s = tw.start; s < tw.end; ++s) {
+      integrate_sample_steps<kTrav>(P, s, tw.x, tw.y, steps);
+    }
+  }
+  const uint32_t sbs = P.wd.sample_block_size;
+  const uint32_t nsb = P.wd.num_sample_blocks;
+  const size_t idx = (block % nsb) + (size_t)nsb * (tw.x + (size_t)tw.y * P.x_dim);
+  for (uint32_t k = 0; k < P.n_steps; ++k) {
+    rgb total = sub_block_reduce(steps[k], tid, sbs);
+    if (!tw.exit && tid % sbs == 0) {
+      if (nsb == 1) {
+        total = total / (float)P.spp;
+      }
+      write_pixel(P.out_rgb + k * P.step_stride, nullptr, false, idx, total);
+    }
+    __syncthreads(); // the next step reuses the reduction's shared memory
+  }
+}
+
 // ReduceFloatRGB pass (mega_kernel/reduce_float_rgb_impl.h:17-63)
 __global__ void __launch_bounds__(1024) k_reduce(const ReduceParams P) {
   const uint32_t block = blockIdx.x;
@@ -122,6 +153,17 @@ cudaError_t launch_render(const RenderParams &p, uint32_t traversal,
     } else {
       dev::k_render<kTravBinary, false><<<grid, block, 0, s>>>(p);
     }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_steps(const RenderParams &p, uint32_t traversal,
+                                uint32_t n_blocks, cudaStream_t s) {
+  const dim3 grid(n_blocks), block(p.wd.block_size);
+  if (traversal == kTravWide) {
+    dev::k_render_steps<kTravWide><<<grid, block, 0, s>>>(p);
+  } else {
+    dev::k_render_steps<kTravBinary><<<grid, block, 0, s>>>(p);
   }
   return cudaGetLastError();
 }

@@ -252,6 +252,10 @@ Status Renderer::prepare_scene(const FlatScene &flat, uint64_t id, uint64_t vers
   auto t0 = std::chrono::steady_clock::now();
   prep_.bvh = build_sbvh(flat.v0.data(), flat.v1.data(), flat.v2.data(), flat.v0.size(), sbvh);
   prep_.wide = build_wide(prep_.bvh);
+  prep_.orig_to_bvh.assign(prep_.bvh.permutation.size(), 0u);
+  for (size_t i = 0; i < prep_.bvh.permutation.size(); ++i) {
+    prep_.orig_to_bvh[prep_.bvh.permutation[i]] = (uint32_t)i;
+  }
   auto t1 = std::chrono::steady_clock::now();
   prep_.build_seconds = std::chrono::duration<double>(t1 - t0).count();
   prep_.scene_id = id;
@@ -305,6 +309,25 @@ void Renderer::fill_params(RenderParams &p) const {
   p.counters = counters_.as<unsigned long long>();
 }
 
+static_assert(kMaxOutputSteps == PATH_MAX_OUTPUT_STEPS, "step bound");
+
+// the resident BVH within the traversal kernels' fixed stacks
+Status Renderer::traversal_fits(const path_settings &st) const {
+  if (st.traversal == PATH_TRAVERSAL_WIDE8 && prep_.wide.depth + 1 > kWideStackDepth) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "wide BVH deeper than the traversal stack");
+  }
+  if (st.traversal == PATH_TRAVERSAL_BINARY) {
+    if (prep_.bvh.depth + 2 > 64) {
+      return Status::err(PATH_ERR_UNSUPPORTED, "SBVH deeper than the 64-entry traversal stack");
+    }
+    if (st.target_objects + prep_.bvh.max_leaf_size - 1 > 10) {
+      return Status::err(PATH_ERR_UNSUPPORTED,
+                         "target_objects + max leaf size - 1 exceeds the 10 candidates");
+    }
+  }
+  return Status::ok();
+}
+
 static Status check_settings(const path_settings &s) {
   if (s.kernel_approach != PATH_KERNEL_MEGA && s.kernel_approach != PATH_KERNEL_STREAMING) {
     return Status::err(PATH_ERR_ARGUMENT, "unknown kernel_approach");
@@ -334,14 +357,37 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   if (!sc.good()) {
     return sc;
   }
-  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE) {
-    return Status::err(PATH_ERR_UNSUPPORTED, "only SquareImage sample specs are built");
+  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE && spec.type != PATH_SAMPLE_INITIAL_RAYS &&
+      spec.type != PATH_SAMPLE_INITIAL_IDX_AND_DIR) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "unknown sample spec type");
   }
-  if (spec.x_dim == 0 || spec.y_dim == 0 || spp == 0) {
+  const bool idx_spec = spec.type == PATH_SAMPLE_INITIAL_IDX_AND_DIR;
+  const bool rays_spec = spec.type == PATH_SAMPLE_INITIAL_RAYS || idx_spec;
+  if (rays_spec && (spec.rays == nullptr || spec.n_rays == 0)) {
+    return Status::err(PATH_ERR_ARGUMENT, "InitialRays / InitialIdxAndDir spec without rays");
+  }
+  if (idx_spec && spec.idxs == nullptr) {
+    return Status::err(PATH_ERR_ARGUMENT, "InitialIdxAndDir spec without triangle indices");
+  }
+  const bool per_step = output.type == PATH_OUTPUT_PER_STEP;
+  if (per_step && (output.n_steps == 0 || output.n_steps > PATH_MAX_OUTPUT_STEPS)) {
+    return Status::err(PATH_ERR_ARGUMENT, "OutputPerStep needs 1.." +
+                                              std::to_string(PATH_MAX_OUTPUT_STEPS) + " steps");
+  }
+  if ((idx_spec || per_step) && st.kernel_approach != PATH_KERNEL_MEGA) {
+    // streaming/run_impl.h:65 and :455 leave both unimplemented
+    return Status::err(PATH_ERR_UNSUPPORTED,
+                       "InitialIdxAndDir and OutputPerStep need the MegaKernel approach");
+  }
+  // InitialRays / InitialIdxAndDir render one "pixel" per entry
+  // (mega_kernel/run_impl.h:56-67)
+  const uint32_t x_dim = rays_spec ? spec.n_rays : spec.x_dim;
+  const uint32_t y_dim = rays_spec ? 1u : spec.y_dim;
+  if (x_dim == 0 || y_dim == 0 || spp == 0) {
     return Status::err(PATH_ERR_ARGUMENT, "image size and samples_per must be positive");
   }
   if (output.data == nullptr ||
-      (output.type != PATH_OUTPUT_BGRA && output.type != PATH_OUTPUT_FLOAT_RGB)) {
+      (output.type != PATH_OUTPUT_BGRA && output.type != PATH_OUTPUT_FLOAT_RGB && !per_step)) {
     return Status::err(PATH_ERR_ARGUMENT, "output buffer missing or unknown output type");
   }
   for (size_t i = 0; i < scene.tri_material.size(); ++i) {
@@ -379,14 +425,9 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   if (st.kernel_approach == PATH_KERNEL_STREAMING && st.traversal != PATH_TRAVERSAL_WIDE8) {
     return Status::err(PATH_ERR_UNSUPPORTED, "the streaming approach traces the 8-wide BVH only");
   }
-  if (st.traversal == PATH_TRAVERSAL_BINARY) {
-    if (prep_.bvh.depth + 2 > 64) {
-      return Status::err(PATH_ERR_UNSUPPORTED, "SBVH deeper than the 64-entry traversal stack");
-    }
-    if (st.target_objects + prep_.bvh.max_leaf_size - 1 > 10) {
-      return Status::err(PATH_ERR_UNSUPPORTED,
-                         "target_objects + max leaf size - 1 exceeds the 10 candidates");
-    }
+  Status sf = traversal_fits(st);
+  if (!sf.good()) {
+    return sf;
   }
   uint64_t h2d = 0;
   if (!rebuilt && st.upload_scene_every_render) {
@@ -400,23 +441,43 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     return ss;
   }
   WorkDiv wd;
-  if (!make_workdiv(st.render_work_division, spp, spec.x_dim, spec.y_dim, wd)) {
+  if (!make_workdiv(st.render_work_division, spp, x_dim, y_dim, wd)) {
     return Status::err(PATH_ERR_ARGUMENT, "invalid render work division settings");
   }
   if (wd.block_size > 256) {
     return Status::err(PATH_ERR_UNSUPPORTED, "render block_size above 256");
   }
-  const size_t n_pix = (size_t)spec.x_dim * spec.y_dim;
+  const size_t n_pix = (size_t)x_dim * y_dim;
+  uint64_t spec_h2d = 0;
+  if (rays_spec) {
+    PG_TRY_CUDA(rays_.upload(spec.rays, n_pix * 24, stream_), "ray upload");
+    spec_h2d = n_pix * 24;
+  }
+  if (idx_spec) {
+    // scene-order triangle index -> BVH order (the device arrays' order)
+    std::vector<uint32_t> bvh_idx(n_pix);
+    for (size_t i = 0; i < n_pix; ++i) {
+      if (spec.idxs[i] >= prep_.orig_to_bvh.size()) {
+        return Status::err(PATH_ERR_ARGUMENT, "InitialIdxAndDir triangle index out of range");
+      }
+      bvh_idx[i] = prep_.orig_to_bvh[spec.idxs[i]];
+    }
+    PG_TRY_CUDA(idxs_.upload(bvh_idx.data(), n_pix * 4, stream_), "index upload");
+    spec_h2d += n_pix * 4;
+  }
   const bool bgra = output.type == PATH_OUTPUT_BGRA;
   const uint32_t nsb = wd.num_sample_blocks;
+  const uint32_t n_steps = per_step ? output.n_steps : 1u;
+  // one (partial-sum) image per output step, step_floats apart
+  const size_t step_floats = (size_t)nsb * n_pix * 3;
   float *direct_rgb = nullptr;
   if (!bgra && nsb == 1 && output.on_device) {
     direct_rgb = static_cast<float *>(output.data);
   } else {
-    PG_TRY_CUDA(out_a_.ensure((size_t)nsb * n_pix * 3 * 4), "output buffer");
+    PG_TRY_CUDA(out_a_.ensure(n_steps * step_floats * 4), "output buffer");
   }
   if (nsb > 1) {
-    PG_TRY_CUDA(out_b_.ensure((size_t)nsb * n_pix * 3 * 4), "reduce buffer");
+    PG_TRY_CUDA(out_b_.ensure(n_steps * step_floats * 4), "reduce buffer");
   }
   if (bgra && !output.on_device) {
     PG_TRY_CUDA(bgra_.ensure(n_pix * 4), "bgra buffer");
@@ -441,8 +502,12 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   p.back_cull = st.back_cull_emission;
   p.target_objects = st.target_objects;
   std::memcpy(p.f2w, spec.film_to_world, sizeof(p.f2w));
-  p.x_dim = spec.x_dim;
-  p.y_dim = spec.y_dim;
+  p.initial_rays = rays_spec ? rays_.as<const float>() : nullptr;
+  p.initial_idx = idx_spec ? idxs_.as<const uint32_t>() : nullptr;
+  p.n_steps = per_step ? n_steps : 0u;
+  p.step_stride = step_floats;
+  p.x_dim = x_dim;
+  p.y_dim = y_dim;
   p.spp = spp;
   p.wd = wd;
   p.out_rgb = direct_rgb ? direct_rgb : out_a_.as<float>();
@@ -458,10 +523,14 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
-    Status sw = run_wavefront(p, st.count_work != 0, &launches);
+    Status sw = run_wavefront(p, st.count_work != 0, st.trace_min_blocks, &launches);
     if (!sw.good()) {
       return sw;
     }
+  } else if (per_step) {
+    PG_TRY_CUDA(launch_render_steps(p, st.traversal, wd.total_blocks(), stream_),
+                "render kernel");
+    ++launches;
   } else {
     PG_TRY_CUDA(launch_render(p, st.traversal, wd.total_blocks(), st.count_work != 0, stream_),
                 "render kernel");
@@ -479,14 +548,16 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     if (!make_workdiv(st.reduce_work_division, factor, xd, 1, rp.wd)) {
       return Status::err(PATH_ERR_ARGUMENT, "invalid reduce work division settings");
     }
-    rp.in = in;
-    rp.out = other;
     rp.reduction_factor = factor;
     rp.spp = spp;
     rp.output_bgra = bgra ? 1 : 0;
     rp.out_bgra = bgra_dev;
-    PG_TRY_CUDA(launch_reduce(rp, stream_), "reduce kernel");
-    ++launches;
+    for (uint32_t k = 0; k < n_steps; ++k) {
+      rp.in = in + k * step_floats;
+      rp.out = other + k * step_floats;
+      PG_TRY_CUDA(launch_reduce(rp, stream_), "reduce kernel");
+      ++launches;
+    }
     factor = rp.wd.num_sample_blocks;
     elems = (size_t)xd * factor;
     std::swap(in, other);
@@ -499,15 +570,18 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
                   "output copy");
     }
   } else if (in != output.data) {
-    PG_TRY_CUDA(cudaMemcpyAsync(output.data, in, n_pix * 12,
-                                output.on_device ? cudaMemcpyDeviceToDevice
-                                                 : cudaMemcpyDeviceToHost,
-                                stream_),
-                "output copy");
+    for (uint32_t k = 0; k < n_steps; ++k) {
+      PG_TRY_CUDA(cudaMemcpyAsync(static_cast<float *>(output.data) + k * n_pix * 3,
+                                  in + k * step_floats, n_pix * 12,
+                                  output.on_device ? cudaMemcpyDeviceToDevice
+                                                   : cudaMemcpyDeviceToHost,
+                                  stream_),
+                  "output copy");
+    }
   }
   uint64_t d2h = 0;
   if (!output.on_device) {
-    d2h = bgra ? n_pix * 4 : n_pix * 12;
+    d2h = bgra ? n_pix * 4 : n_steps * n_pix * 12;
   }
   uint32_t status = 0;
   unsigned long long counts[3] = {0, 0, 0};
@@ -532,7 +606,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   stats_.device_status = status;
   stats_.num_bvh_nodes = (uint32_t)prep_.bvh.nodes.size();
   stats_.num_wide_nodes = (uint32_t)prep_.wide.nodes.size();
-  stats_.h2d_bytes = h2d;
+  stats_.h2d_bytes = h2d + spec_h2d;
   stats_.d2h_bytes = d2h;
   if (seconds) {
     *seconds = stats_.seconds;
@@ -547,7 +621,8 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
 
 // wavefront render of the whole image into p.out_rgb / p.out_bgra (see
 // wavefront.cu); the host checks the live-slot count every few iterations
-Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t *launches) {
+Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t min_blocks,
+                               uint32_t *launches) {
   if (num_sms_ == 0) {
     int dev = 0;
     PG_TRY_CUDA(cudaGetDevice(&dev), "device");
@@ -594,12 +669,15 @@ Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t *l
               "queue init");
   PG_TRY_CUDA(launch_wavefront_init(w, n_slots, stream_), "wavefront init");
   *launches += 1;
-  const uint32_t grid = (uint32_t)num_sms_ * 8;
+  const uint32_t trace_grid =
+      (uint32_t)num_sms_ * (uint32_t)wavefront_trace_blocks_per_sm(min_blocks, counting);
+  const uint32_t shade_grid = (uint32_t)num_sms_ * 4;
   uint32_t parity = 0;
   volatile uint32_t *live = h + 12;
   for (uint32_t round = 0;; ++round) {
     for (int k = 0; k < 4; ++k) {
-      PG_TRY_CUDA(launch_wavefront_iteration(w, parity, grid, counting, stream_),
+      PG_TRY_CUDA(launch_wavefront_iteration(w, parity, trace_grid, shade_grid, min_blocks,
+                                             counting, stream_),
                   "wavefront iteration");
       *launches += 3;
       parity ^= 1u;
@@ -653,6 +731,10 @@ Status Renderer::intersect(const float *tris, uint32_t n_tris, const float *rays
   Status su = upload_geometry(flat, mats);
   if (!su.good()) {
     return su;
+  }
+  Status sf = traversal_fits(st);
+  if (!sf.good()) {
+    return sf;
   }
   DeviceBuffer d_rays, d_idx, d_t;
   PG_TRY_CUDA(d_rays.upload(rays, (size_t)n_rays * 24, stream_), "rays");

@@ -71,6 +71,7 @@ struct PreparedScene {
   bool valid = false;
   BinaryBVH bvh;
   WideBVH wide;
+  std::vector<uint32_t> orig_to_bvh; // inverse of bvh.permutation
   uint32_t n_tris = 0, n_lights = 0;
   double build_seconds = 0.0;
 };
@@ -101,6 +102,7 @@ private:
   Status copy_staged(uint64_t *bytes);
   Status prepare_sobol(uint32_t dim_bound, uint32_t count);
   void fill_params(RenderParams &p) const;
+  Status traversal_fits(const path_settings &st) const;
 
   bool initialised_ = false;
   cudaStream_t stream_ = nullptr;
@@ -113,9 +115,10 @@ private:
       st_lights_, st_cdf_, st_perm_;
   DeviceBuffer sobol_dirs_, sobol_scramble_, sobol_table_;
   uint32_t sobol_bound_ = 0, sobol_count_ = 0;
-  DeviceBuffer out_a_, out_b_, bgra_, status_, counters_;
+  DeviceBuffer out_a_, out_b_, bgra_, status_, counters_, rays_, idxs_;
   // wavefront state
-  Status run_wavefront(const RenderParams &p, bool counting, uint32_t *launches);
+  Status run_wavefront(const RenderParams &p, bool counting, uint32_t min_blocks,
+                       uint32_t *launches);
   DeviceBuffer wf_slots_, wf_queues_, wf_samples_;
   PinnedBuffer wf_host_;
   int num_sms_ = 0;

@@ -113,11 +113,11 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
 }
 
 // Persistent trace: each lane walks one ray through the wide BVH one node
-// per step; when a quarter of a warp's lanes are idle they take new queue
-// entries together (one atomic per warp), so lanes rarely wait on the
-// longest ray of a batch.
-template <bool kCount>
-__global__ void __launch_bounds__(256) k_wf_trace(const WaveParams W) {
+// (and the triangles of its leaf slots) per step; when a quarter of a warp's
+// lanes are idle they take new queue entries together (one atomic per
+// warp), so lanes rarely wait on the longest ray of a batch.
+template <bool kCount, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->rays;
   Counts cnt = {0, 0, 0};
@@ -126,8 +126,8 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WaveParams W) {
   bool have = false;
   bool drained = false;
   uint32_t entry = 0;
-  uint32_t st_node[kWideStack];
-  float st_t[kWideStack];
+  uint32_t st_base[kWideStack];
+  uint32_t st_bits[kWideStack];
   while (true) {
     const uint32_t idle = __ballot_sync(kFull, !have);
     if (!drained && __popc(idle) >= 8) {
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WaveParams W) {
     }
     if (have) {
       if (!w.done) {
-        wide_visit<kCount>(W.P, w, st_node, st_t, cnt);
+        wide_step<kCount>(W.P, w, st_base, st_bits, cnt);
       }
       if (w.done) {
         const uint32_t slot = entry >> 1;
@@ -306,15 +306,42 @@ cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity, uint32_t grid,
-                                       bool counting, cudaStream_t s) {
-  if (counting) {
-    dev::k_wf_trace<true><<<grid, 256, 0, s>>>(w);
-  } else {
-    dev::k_wf_trace<false><<<grid, 256, 0, s>>>(w);
+namespace {
+template <bool kCount>
+void *trace_kernel(uint32_t min_blocks) {
+  switch (min_blocks) {
+  case 3:
+    return (void *)dev::k_wf_trace<kCount, 3>;
+  case 5:
+    return (void *)dev::k_wf_trace<kCount, 5>;
+  case 6:
+    return (void *)dev::k_wf_trace<kCount, 6>;
+  default:
+    return (void *)dev::k_wf_trace<kCount, 4>;
+  }
+}
+} // namespace
+
+int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting) {
+  int n = 0;
+  void *k = counting ? trace_kernel<true>(min_blocks) : trace_kernel<false>(min_blocks);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, 0) != cudaSuccess || n < 1) {
+    n = 1;
+  }
+  return n;
+}
+
+cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity,
+                                       uint32_t trace_grid, uint32_t shade_grid,
+                                       uint32_t min_blocks, bool counting, cudaStream_t s) {
+  void *k = counting ? trace_kernel<true>(min_blocks) : trace_kernel<false>(min_blocks);
+  void *args[] = {const_cast<WaveParams *>(&w)};
+  cudaError_t e = cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args, 0, s);
+  if (e != cudaSuccess) {
+    return e;
   }
   dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
-  dev::k_wf_shade<<<grid, 256, 0, s>>>(w, parity);
+  dev::k_wf_shade<<<shade_grid, 256, 0, s>>>(w, parity);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 // Compressed 8-wide BVH construction (see wide.h).
 #include "wide.h"
 
+#include <array>
 #include <cmath>
 #include <cstring>
 
@@ -60,6 +61,68 @@ float exp_scale(uint8_t e) {
   float f;
   std::memcpy(&f, &bits, sizeof(f));
   return f;
+}
+
+// one slot of a wide node: an internal child, or (part of) a binary leaf
+struct Slot {
+  uint32_t bin;
+  bool leaf;
+  uint32_t first, count; // leaf: range in the binary leaf
+};
+
+// Places the (at most eight) slots so that slot bit a set means "on the high
+// side of axis a": every slot direction d(s) = (+-1, +-1, +-1) takes the
+// child whose centre lies furthest along d(s) from the node's centre,
+// greedily by that score.  A ray with direction-sign octant o then meets
+// the children roughly in the order of the slots o ^ 0, o ^ 1, ..., o ^ 7
+// (nearest first), which the traversal uses instead of sorting.
+std::array<int, 8> order_slots(const BinaryBVH &bvh, const std::vector<Slot> &slots,
+                               const box &all) {
+  std::array<int, 8> at;
+  at.fill(-1);
+  const size_t n = slots.size();
+  double centre[3];
+  for (int a = 0; a < 3; ++a) {
+    centre[a] = 0.5 * ((double)all.lo.get(a) + (double)all.hi.get(a));
+  }
+  std::vector<std::array<double, 8>> score(n);
+  for (size_t k = 0; k < n; ++k) {
+    const box &b = bvh.nodes[slots[k].bin].aabb;
+    double c[3];
+    for (int a = 0; a < 3; ++a) {
+      c[a] = 0.5 * ((double)b.lo.get(a) + (double)b.hi.get(a)) - centre[a];
+    }
+    for (int s = 0; s < 8; ++s) {
+      double v = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        v += ((s >> a) & 1) ? c[a] : -c[a];
+      }
+      score[k][(size_t)s] = v;
+    }
+  }
+  std::vector<bool> placed(n, false);
+  for (size_t round = 0; round < n; ++round) {
+    double best = 0.0;
+    int bk = -1, bs = -1;
+    for (size_t k = 0; k < n; ++k) {
+      if (placed[k]) {
+        continue;
+      }
+      for (int s = 0; s < 8; ++s) {
+        if (at[(size_t)s] >= 0) {
+          continue;
+        }
+        if (bk < 0 || score[k][(size_t)s] > best) {
+          best = score[k][(size_t)s];
+          bk = (int)k;
+          bs = s;
+        }
+      }
+    }
+    placed[(size_t)bk] = true;
+    at[(size_t)bs] = bk;
+  }
+  return at;
 }
 
 } // namespace
@@ -131,11 +194,6 @@ WideBVH build_wide(const BinaryBVH &bvh) {
     }
     // leaves larger than a slot can hold are split across slots with the
     // same box; leaves that no longer fit get a node of their own
-    struct Slot {
-      uint32_t bin;
-      bool leaf;
-      uint32_t first, count; // leaf: range in the binary leaf
-    };
     std::vector<Slot> slots;
     for (const Child &c : kids) {
       if (!c.leaf) {
@@ -182,17 +240,19 @@ WideBVH build_wide(const BinaryBVH &bvh) {
     uint32_t child_base = (uint32_t)out.nodes.size();
     wn.child_base = child_base;
     wn.tri_base = (uint32_t)out.tri_index.size();
+    // slot order: slot bit a set = high side of axis a (see order_slots)
+    const std::array<int, 8> at = order_slots(bvh, slots, all);
     uint32_t rank = 0, tri_off = 0;
     std::vector<Job> children;
     for (size_t i = 0; i < 8; ++i) {
-      if (i >= slots.size()) {
+      if (at[i] < 0) {
         for (int a = 0; a < 3; ++a) {
           wn.qlo[a][i] = 255;
           wn.qhi[a][i] = 0;
         }
         continue;
       }
-      const Slot &s = slots[i];
+      const Slot &s = slots[(size_t)at[i]];
       const box &cb = bvh.nodes[s.bin].aabb;
       for (int a = 0; a < 3; ++a) {
         float sc = exp_scale(wn.e[a]);

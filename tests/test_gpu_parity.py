@@ -273,3 +273,145 @@ def test_streaming_equals_megakernel_full_cornell(lib):
     s.kernel_approach = 1
     wave = _render_gpu(sc, s, 16, 256, 256, f2w)
     assert np.array_equal(bits(mega), bits(wave))
+
+
+def _camera_rays(rng, n, f2w):
+    """Rays through random film points of the Cornell camera."""
+    m = np.asarray(f2w, np.float64).reshape(3, 4)
+    film = np.stack([rng.uniform(-1, 1, n), rng.uniform(-1, 1, n), -np.ones(n)], 1)
+    world = film @ m[:, :3].T + m[:, 3]
+    d = world - m[:, 3]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([np.tile(m[:, 3], (n, 1)), d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("approach", ["mega_binary", "mega_wide", "streaming"])
+def test_initial_rays_match_oracle(lib, oracle, approach):
+    """SampleSpecType::InitialRays: one output per caller ray, location x =
+    ray index, no camera draws from the RNG."""
+    rng = np.random.default_rng(5)
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "binary" if approach == "mega_binary" else "wide")
+    if approach == "streaming":
+        s.kernel_approach = 1
+    rays = _camera_rays(rng, 3001, scenes.cornell_camera(64, 64))
+    out = np.zeros((len(rays), 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.InitialRays(rays), out, sc, 8, s)
+    assert r.stats()["device_status"] == 0
+    ref = ol.render_rays(ol.SceneArrays(sc.export()), ol.settings_from(s, reduce_order=1), 8,
+                         rays)
+    assert rel_rmse(out, ref) <= RMSE_TOL
+    if approach == "mega_binary":
+        assert np.array_equal(bits(out), bits(ref))
+
+
+@pytest.mark.parametrize("case", ["binary", "wide", "sample_blocks"])
+def test_output_per_step_matches_oracle(lib, oracle, case):
+    """OutputType::OutputPerStep: step k's radiance per pixel, paths cut
+    after n_steps steps (rendering_equation.h:61-124)."""
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "wide" if case == "wide" else "binary")
+    spp, w, h, n_steps = 16, 48, 40, 4
+    if case == "sample_blocks":
+        s.render_work_division.block_size = 32
+        s.render_work_division.force_target_samples = 1
+        s.render_work_division.forced_target_samples_per_thread = 1
+        spp, w, h = 64, 16, 16
+    f2w = scenes.cornell_camera(w, h)
+    out = np.zeros((n_steps, h, w, 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), api.OutputPerStep(out), sc,
+             spp, s)
+    assert r.stats()["device_status"] == 0
+    ref = ol.render_steps(ol.SceneArrays(sc.export()), ol.settings_from(s, reduce_order=1), spp,
+                          w, h, f2w, n_steps)
+    assert rel_rmse(out, ref) <= RMSE_TOL
+    if case != "wide":
+        assert np.array_equal(bits(out), bits(ref))
+
+
+def test_output_per_step_device_output(lib):
+    import torch
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "binary")
+    f2w = scenes.cornell_camera(32, 32)
+    host = np.zeros((3, 32, 32, 3), np.float32)
+    api.Renderer().render(api.ExecutionModel.GPU, api.SquareImage(32, 32, f2w),
+                          api.OutputPerStep(host), sc, 8, s)
+    dev = torch.zeros((3, 32, 32, 3), dtype=torch.float32, device="cuda")
+    api.Renderer().render(api.ExecutionModel.GPU, api.SquareImage(32, 32, f2w),
+                          api.OutputPerStep(dev), sc, 8, s)
+    torch.cuda.synchronize()
+    assert np.array_equal(bits(dev.cpu().numpy()), bits(host))
+
+
+def _idx_and_dir_case(rng, sc, n):
+    tris = sc.export()["triangles"].reshape(-1, 3, 3).astype(np.float64)
+    ti = rng.integers(0, len(tris), n)
+    bary = rng.dirichlet([1, 1, 1], n)
+    p = np.einsum("nk,nkj->nj", bary, tris[ti])
+    nrm = np.cross(tris[ti, 1] - tris[ti, 0], tris[ti, 2] - tris[ti, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = -nrm + 0.3 * rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return ti.astype(np.uint32), np.concatenate([p - d, d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("traversal", ["binary", "wide"])
+def test_initial_idx_and_dir_matches_oracle(lib, oracle, traversal):
+    """SampleSpecType::InitialIdxAndDir: each path starts at the caller's
+    triangle hit (distance 1, front side) without tracing the first ray."""
+    rng = np.random.default_rng(8)
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, traversal)
+    idxs, rays = _idx_and_dir_case(rng, sc, 2000)
+    out = np.zeros((len(rays), 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.InitialIdxAndDir(idxs, rays), out, sc, 8, s)
+    assert r.stats()["device_status"] == 0
+    ref = ol.render_rays(ol.SceneArrays(sc.export()), ol.settings_from(s, reduce_order=1), 8,
+                         rays, idxs=idxs)
+    assert rel_rmse(out, ref) <= RMSE_TOL
+    if traversal == "binary":
+        assert np.array_equal(bits(out), bits(ref))
+    # the same spec with OutputPerStep
+    steps = np.zeros((3, len(rays), 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.InitialIdxAndDir(idxs, rays), api.OutputPerStep(steps),
+             sc, 8, s)
+    ref_steps = ol.render_rays(ol.SceneArrays(sc.export()), ol.settings_from(s, reduce_order=1),
+                               8, rays, idxs=idxs, n_steps=3)
+    assert rel_rmse(steps, ref_steps) <= RMSE_TOL
+
+
+def test_wide_closest_hit_is_order_independent(lib, oracle):
+    """The 8-wide traversal returns the smallest distance and, among equal
+    distances, the smallest BVH-order index: rays onto the shared vertices
+    and edges of a grid meet several triangles at exactly the same t."""
+    quads = []
+    for i in range(8):
+        for j in range(8):
+            a, b, c, e = (i, j, 0), (i + 1, j, 0), (i + 1, j + 1, 0), (i, j + 1, 0)
+            quads += [a + b + c, a + c + e]
+    tris = np.array(quads, np.float32)
+    pts = np.stack(np.meshgrid(np.arange(1, 8) * 1.0, np.arange(1, 8) * 0.5), -1).reshape(-1, 2)
+    rays = np.concatenate([pts, np.ones((len(pts), 1)), np.tile([0.0, 0.0, -1.0], (len(pts), 1))],
+                          1).astype(np.float32)
+    s = api.Settings()
+    s.traversal = 1
+    w = api.wide_build(tris, s)
+    perm = w["permutation"]
+    nt, nr = len(tris), len(rays)
+    t_all, _ = ol.triangle_intersect(np.repeat(tris[perm], nr, 0), np.tile(rays, (nt, 1)))
+    t_all = t_all.reshape(nt, nr)
+    got, gt = api.Renderer().intersect(tris, rays, s)
+    ties = 0
+    for r in range(nr):
+        col = t_all[:, r]
+        ok = np.isfinite(col)
+        assert ok.any()
+        tmin = col[ok].min()
+        ties += int((col == tmin).sum() > 1)
+        assert got[r] == perm[np.flatnonzero(col == tmin).min()]
+        assert gt[r] == tmin
+    assert ties > 10

@@ -181,6 +181,24 @@ def test_render_rejects_bad_requests_before_touching_the_gpu(lib):
     with pytest.raises(capi.PathError) as e:
         r.render(api.ExecutionModel.GPU, spec, out, sc, 0, api.Settings())
     assert e.value.status == 1
+    with pytest.raises(capi.PathError) as e:
+        r.render(api.ExecutionModel.GPU, api.InitialRays(np.zeros((0, 6))), out, sc, 4,
+                 api.Settings())
+    assert e.value.status == 1
+    steps = np.zeros((65, 8, 8, 3), np.float32)
+    with pytest.raises(capi.PathError) as e:
+        r.render(api.ExecutionModel.GPU, spec, api.OutputPerStep(steps), sc, 4, api.Settings())
+    assert e.value.status == 1
+    # OutputPerStep and InitialIdxAndDir are MegaKernel-only, as in the reference
+    s = api.Settings()
+    s.kernel_approach = 1
+    with pytest.raises(capi.PathError) as e:
+        r.render(api.ExecutionModel.GPU, spec, api.OutputPerStep(steps[:2]), sc, 4, s)
+    assert e.value.status == 5
+    idx_spec = api.InitialIdxAndDir(np.zeros(2, np.uint32), np.zeros((2, 6), np.float32))
+    with pytest.raises(capi.PathError) as e:
+        r.render(api.ExecutionModel.GPU, idx_spec, out, sc, 4, s)
+    assert e.value.status == 5
 
 
 def test_scene_rejects_bad_material_index(lib):

@@ -270,3 +270,32 @@ def test_sobol_table_is_a_net(oracle):
             vals = np.sort(cells[:, d])
             # a value exactly 1.0 is mapped to 0.0, which can merge two cells
             assert len(np.unique(vals)) >= (1 << m) - 1
+
+
+def test_oracle_initial_rays_trace_the_given_rays():
+    """InitialRays location x renders spec[x]: a ray leaving the box returns
+    zero radiance, one into the box does not."""
+    from path_gb300 import scenes
+    sc = scenes.cornell_box()
+    arr = ol.SceneArrays(sc.export())
+    st = ol.settings_from(scenes.path_settings(5, "binary"), reduce_order=1)
+    rays = np.array([[0, 0, 3.5, 0, 0, 1], [0, 0, 3.5, 0, 0, -1]], np.float32)
+    out = ol.render_rays(arr, st, 4, rays)
+    assert np.all(out[0] == 0)
+    assert np.all(out[1] > 0)
+
+
+def test_oracle_output_per_step_sums_to_the_image():
+    """OutputPerStep splits each sample's radiance by path step: with more
+    steps than any path takes, the steps sum to the FloatRGB image (up to
+    float rounding), and fewer steps give a prefix of the same steps."""
+    from path_gb300 import scenes
+    sc = scenes.cornell_box()
+    arr = ol.SceneArrays(sc.export())
+    st = ol.settings_from(scenes.path_settings(5, "binary"), reduce_order=1)
+    f2w = scenes.cornell_camera(24, 24)
+    img, _ = ol.render(arr, st, 8, 24, 24, f2w)
+    steps = ol.render_steps(arr, st, 8, 24, 24, f2w, 8)
+    assert np.allclose(steps.sum(0), img, rtol=1e-5, atol=1e-6)
+    assert np.all(steps[6:] == 0)  # NIters{4}: at most 5 bounces + 1 light pass
+    assert np.array_equal(ol.render_steps(arr, st, 8, 24, 24, f2w, 2), steps[:2])
