@@ -151,6 +151,11 @@ typedef struct {
   const float *rays;      /* INITIAL_*: [n_rays][6] origin, unit direction */
   uint32_t n_rays;
   const uint32_t *idxs;   /* INITIAL_IDX_AND_DIR: [n_rays] triangle index */
+  /* SQUARE_IMAGE: render only image rows [row_start, row_end) (a band, for
+   * sharding one image over several GPUs; both 0 = every row).  A band's
+   * pixels are computed exactly as in the whole-image render; output rows
+   * outside the band are left untouched.  GB300 addition. */
+  uint32_t row_start, row_end;
 } path_sample_spec;
 
 typedef enum {

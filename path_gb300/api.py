@@ -162,12 +162,14 @@ def camera_transform(look, up, pos, height_angle_deg, width_height_ratio):
 
 
 class SquareImage:
-    """render::SquareImageSpec."""
+    """render::SquareImageSpec; ``rows=(start, end)`` renders only that band
+    of rows (bit-identical to the same rows of the whole render)."""
 
-    def __init__(self, x_dim, y_dim, film_to_world):
+    def __init__(self, x_dim, y_dim, film_to_world, rows=None):
         self.x_dim = int(x_dim)
         self.y_dim = int(y_dim)
         self.film_to_world = np.asarray(film_to_world, np.float32).reshape(12)
+        self.rows = rows
 
     def to_c(self):
         s = capi.SampleSpec()
@@ -175,6 +177,8 @@ class SquareImage:
         s.x_dim = self.x_dim
         s.y_dim = self.y_dim
         s.film_to_world[:] = [float(v) for v in self.film_to_world]
+        if self.rows is not None:
+            s.row_start, s.row_end = int(self.rows[0]), int(self.rows[1])
         return s
 
 

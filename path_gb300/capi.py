@@ -49,7 +49,8 @@ class PathSettings(ctypes.Structure):
 class SampleSpec(ctypes.Structure):
     _fields_ = [("type", c_u32), ("x_dim", c_u32), ("y_dim", c_u32),
                 ("film_to_world", c_f32 * 12), ("rays", ctypes.POINTER(c_f32)),
-                ("n_rays", c_u32), ("idxs", ctypes.POINTER(c_u32))]
+                ("n_rays", c_u32), ("idxs", ctypes.POINTER(c_u32)), ("row_start", c_u32),
+                ("row_end", c_u32)]
 
 
 class Output(ctypes.Structure):

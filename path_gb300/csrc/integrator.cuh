@@ -220,13 +220,18 @@ __device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, c
   w.done = P.n_wide_nodes == 0;
 }
 
-// One traversal step: enter the next child of the current node group, test
-// its eight slots, test the triangles of the leaf slots it hits, then make
-// its internal hits the current group (the rest of the old group waits on
-// the stack) or take a group from the stack.
+// Enter the next child of the current node group and test its eight slots;
+// the triangles of the leaf slots it hits are returned as a mask over the
+// node's triangle block (tri_base + bit).  Its internal hits become the
+// current group (the rest of the old group waits on the stack), or a group
+// is taken from the stack, or the walk ends (w.done) once the returned
+// triangles are tested.
 template <bool kCount>
-__device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
-                                          uint32_t *st_base, uint32_t *st_bits, Counts &cnt) {
+__device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
+                                          uint32_t *st_base, uint32_t *st_bits, Counts &cnt,
+                                          uint32_t &tri_base, uint32_t &tmask) {
+  tmask = 0;
+  tri_base = 0;
   const uint32_t j = __ffs(w.ng_bits >> 8) - 1;
   w.ng_bits &= ~(1u << (8 + j));
   const uint32_t slot = j ^ w.oct;
@@ -275,7 +280,7 @@ __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
   const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
   const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
   const float tcull = w.best.t;
-  uint32_t hits = 0, tmask = 0;
+  uint32_t hits = 0, tm = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const float tnx = __fmaf_rn(byte8_float(nxl, nxh, i), ax, bnx);
@@ -292,26 +297,11 @@ __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
       hits |= (hit ? 1u : 0u) << (i ^ (int)w.oct);
     } else if (hit) {
       // leaf slot: meta = count << 5 | first triangle offset
-      tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+      tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
     }
   }
-  const uint32_t tri_base = n1.y;
-  while (tmask != 0) {
-    const uint32_t k = __ffs(tmask) - 1;
-    tmask &= tmask - 1u;
-    const float4 *tp = P.wide_tris + 3 * (size_t)(tri_base + k);
-    const float4 a = __ldg(tp);
-    const float4 b = __ldg(tp + 1);
-    const float4 c = __ldg(tp + 2);
-    if (kCount) {
-      ++cnt.tris;
-    }
-    float t;
-    bool back;
-    if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), w.r, &t, &back)) {
-      fold_min(w.best, t, back, __float_as_uint(c.y));
-    }
-  }
+  tri_base = n1.y;
+  tmask = tm;
   if (hits != 0) {
     w.ng_base = n1.x;
     w.ng_bits = imask | (hits << 8);
@@ -325,6 +315,36 @@ __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
     return;
   }
   w.done = true;
+}
+
+// Moller-Trumbore on wide-leaf triangle k; folds a hit into best
+__device__ __forceinline__ void wide_tri(const RenderParams &P, const ray &r, uint32_t k,
+                                         Hit &best) {
+  const float4 *tp = P.wide_tris + 3 * (size_t)k;
+  const float4 a = __ldg(tp);
+  const float4 b = __ldg(tp + 1);
+  const float4 c = __ldg(tp + 2);
+  float t;
+  bool back;
+  if (tri_hit(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), r, &t, &back)) {
+    fold_min(best, t, back, __float_as_uint(c.y));
+  }
+}
+
+// one traversal step of a lone lane: a node and its triangles
+template <bool kCount>
+__device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
+                                          uint32_t *st_base, uint32_t *st_bits, Counts &cnt) {
+  uint32_t tri_base, tmask;
+  wide_node<kCount>(P, w, st_base, st_bits, cnt, tri_base, tmask);
+  while (tmask != 0) {
+    const uint32_t k = __ffs(tmask) - 1;
+    tmask &= tmask - 1u;
+    if (kCount) {
+      ++cnt.tris;
+    }
+    wide_tri(P, w.r, tri_base + k, w.best);
+  }
 }
 
 template <bool kCount>
@@ -993,6 +1013,16 @@ __device__ void integrate_sample_steps(const RenderParams &P, uint32_t sample_id
 }
 
 // ---------------------------------------------------------------------------
+// WorkDivision thread info; threads of rows outside the rendered band exit
+__device__ __forceinline__ ThreadWork band_work(const RenderParams &P, uint32_t block,
+                                               uint32_t tid) {
+  ThreadWork tw = thread_work(P.wd, block, tid);
+  if (tw.y < P.row_lo || tw.y >= P.row_hi) {
+    tw.exit = true;
+  }
+  return tw;
+}
+
 // reduction over sample_block_size lanes (include/lib/cuda/reduce.cuh:35-102)
 __device__ __forceinline__ rgb warp_reduce(rgb v, uint32_t width) {
   for (uint32_t off = width / 2; off > 0; off /= 2) {

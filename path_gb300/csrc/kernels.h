@@ -48,6 +48,8 @@ struct RenderParams {
   uint32_t *status;   // first in-kernel error code
   unsigned long long *counters; // [3] rays, nodes, triangles (counting runs)
   uint32_t start_block;
+  // image rows [row_lo, row_hi) are rendered; threads of other rows exit
+  uint32_t row_lo, row_hi;
 };
 
 enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
@@ -76,8 +78,9 @@ struct WaveParams {
   uint32_t *rays;      // ray queue: slot << 1 | (1 for the light ray)
   WaveQueues *q;
   unsigned long long *next_sample;
-  unsigned long long total_samples;
-  float *sample_rgb;   // [total_samples][3]
+  unsigned long long first_sample; // first sample id of the rendered rows
+  unsigned long long total_samples; // one past the last sample id
+  float *sample_rgb;   // [total_samples - first_sample][3]
   uint32_t n_slots;
 };
 
@@ -90,7 +93,7 @@ cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity,
                                        uint32_t min_blocks, bool counting, cudaStream_t s);
 // per-pixel sums of the sample buffer into p.out_rgb / p.out_bgra
 cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
-                                 cudaStream_t s);
+                                 uint32_t n_blocks, cudaStream_t s);
 
 // integration megakernel over blocks [start_block, start_block + n_blocks)
 cudaError_t launch_render(const RenderParams &p, uint32_t traversal,

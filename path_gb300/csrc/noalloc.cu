@@ -72,7 +72,8 @@ size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output &output,
                                 const Scene &scene, uint32_t spp, const path_settings &st,
                                 void *scratch, size_t scratch_bytes, double *seconds) {
-  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE || spec.x_dim == 0 || spec.y_dim == 0 ||
+  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE || spec.row_start != 0 || spec.row_end != 0 ||
+      spec.x_dim == 0 || spec.y_dim == 0 ||
       spp == 0) {
     return Status::err(PATH_ERR_ARGUMENT, "a square image with positive size and spp is needed");
   }
@@ -155,6 +156,8 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   p.out_bgra = bgra ? static_cast<uint8_t *>(output.data) : nullptr;
   p.output_bgra = bgra ? 1 : 0;
   p.start_block = 0;
+  p.row_lo = 0;
+  p.row_hi = spec.y_dim;
 
   auto t0 = std::chrono::steady_clock::now();
   uint32_t launches = 0;

@@ -14,7 +14,7 @@ template <uint32_t kTrav, bool kCount>
 __global__ void __launch_bounds__(256) k_render(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
-  const ThreadWork tw = thread_work(P.wd, block, tid);
+  const ThreadWork tw = band_work(P, block, tid);
   Counts cnt = {0, 0, 0};
   rgb total = zero_rgb();
   if (!tw.exit) {
@@ -45,7 +45,7 @@ template <uint32_t kTrav>
 __global__ void __launch_bounds__(256) k_render_steps(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
-  const ThreadWork tw = thread_work(P.wd, block, tid);
+  const ThreadWork tw = band_work(P, block, tid);
   rgb steps[kMaxOutputSteps];
   for (uint32_t k = 0; k < P.n_steps; ++k) {
     steps[k] = zero_rgb();

@@ -386,6 +386,15 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   if (x_dim == 0 || y_dim == 0 || spp == 0) {
     return Status::err(PATH_ERR_ARGUMENT, "image size and samples_per must be positive");
   }
+  // the band of rows this call renders (the whole image by default)
+  uint32_t row_lo = 0, row_hi = y_dim;
+  if (!rays_spec && (spec.row_start != 0 || spec.row_end != 0)) {
+    if (spec.row_start >= spec.row_end || spec.row_end > y_dim) {
+      return Status::err(PATH_ERR_ARGUMENT, "row band must satisfy start < end <= y_dim");
+    }
+    row_lo = spec.row_start;
+    row_hi = spec.row_end;
+  }
   if (output.data == nullptr ||
       (output.type != PATH_OUTPUT_BGRA && output.type != PATH_OUTPUT_FLOAT_RGB && !per_step)) {
     return Status::err(PATH_ERR_ARGUMENT, "output buffer missing or unknown output type");
@@ -516,31 +525,42 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
                            : nullptr;
   p.out_bgra = bgra_dev;
   p.output_bgra = bgra ? 1 : 0;
-  p.start_block = 0;
+  // blocks are ordered (sample block, x block, y block): a band of rows is
+  // the contiguous block range of the y blocks it touches
+  const uint32_t blocks_per_yblock = wd.num_sample_blocks * wd.num_x_blocks;
+  const uint32_t yb0 = row_lo / wd.y_block_size;
+  const uint32_t yb1 = (row_hi + wd.y_block_size - 1) / wd.y_block_size;
+  const uint32_t n_blocks = (yb1 - yb0) * blocks_per_yblock;
+  p.start_block = yb0 * blocks_per_yblock;
+  p.row_lo = row_lo;
+  p.row_hi = row_hi;
+  const size_t pix0 = (size_t)row_lo * x_dim;           // first band pixel
+  const size_t n_band = (size_t)(row_hi - row_lo) * x_dim;
 
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "pre-render sync");
   auto t0 = std::chrono::steady_clock::now();
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
-    Status sw = run_wavefront(p, st.count_work != 0, st.trace_min_blocks, &launches);
+    Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks, &launches);
     if (!sw.good()) {
       return sw;
     }
   } else if (per_step) {
-    PG_TRY_CUDA(launch_render_steps(p, st.traversal, wd.total_blocks(), stream_),
+    PG_TRY_CUDA(launch_render_steps(p, st.traversal, n_blocks, stream_),
                 "render kernel");
     ++launches;
   } else {
-    PG_TRY_CUDA(launch_render(p, st.traversal, wd.total_blocks(), st.count_work != 0, stream_),
+    PG_TRY_CUDA(launch_render(p, st.traversal, n_blocks, st.count_work != 0, stream_),
                 "render kernel");
     ++launches;
   }
-  // ReduceFloatRGB passes
+  // ReduceFloatRGB passes over the band's pixels: with `factor` partial sums
+  // per pixel, pixel j's sums start at float (pix0 + j) * factor * 3
   uint32_t factor = nsb;
   float *in = p.out_rgb;
   float *other = out_b_.as<float>();
-  size_t elems = (size_t)nsb * n_pix;
+  size_t elems = (size_t)nsb * n_band;
   while (factor != 1) {
     ReduceParams rp;
     std::memset(&rp, 0, sizeof(rp));
@@ -551,10 +571,11 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     rp.reduction_factor = factor;
     rp.spp = spp;
     rp.output_bgra = bgra ? 1 : 0;
-    rp.out_bgra = bgra_dev;
+    rp.out_bgra = bgra_dev ? bgra_dev + pix0 * 4 : nullptr;
+    const uint32_t next_factor = rp.wd.num_sample_blocks;
     for (uint32_t k = 0; k < n_steps; ++k) {
-      rp.in = in + k * step_floats;
-      rp.out = other + k * step_floats;
+      rp.in = in + k * step_floats + pix0 * factor * 3;
+      rp.out = other + k * step_floats + pix0 * next_factor * 3;
       PG_TRY_CUDA(launch_reduce(rp, stream_), "reduce kernel");
       ++launches;
     }
@@ -565,14 +586,15 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   PG_TRY_CUDA(cudaEventRecord(ev_stop_, stream_), "event");
   if (bgra) {
     if (!output.on_device) {
-      PG_TRY_CUDA(cudaMemcpyAsync(output.data, bgra_dev, n_pix * 4, cudaMemcpyDeviceToHost,
+      PG_TRY_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(output.data) + pix0 * 4,
+                                  bgra_dev + pix0 * 4, n_band * 4, cudaMemcpyDeviceToHost,
                                   stream_),
                   "output copy");
     }
   } else if (in != output.data) {
     for (uint32_t k = 0; k < n_steps; ++k) {
-      PG_TRY_CUDA(cudaMemcpyAsync(static_cast<float *>(output.data) + k * n_pix * 3,
-                                  in + k * step_floats, n_pix * 12,
+      PG_TRY_CUDA(cudaMemcpyAsync(static_cast<float *>(output.data) + k * n_pix * 3 + pix0 * 3,
+                                  in + k * step_floats + pix0 * 3, n_band * 12,
                                   output.on_device ? cudaMemcpyDeviceToDevice
                                                    : cudaMemcpyDeviceToHost,
                                   stream_),
@@ -581,7 +603,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   }
   uint64_t d2h = 0;
   if (!output.on_device) {
-    d2h = bgra ? n_pix * 4 : n_steps * n_pix * 12;
+    d2h = bgra ? n_band * 4 : n_steps * n_band * 12;
   }
   uint32_t status = 0;
   unsigned long long counts[3] = {0, 0, 0};
@@ -621,14 +643,17 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
 
 // wavefront render of the whole image into p.out_rgb / p.out_bgra (see
 // wavefront.cu); the host checks the live-slot count every few iterations
-Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t min_blocks,
-                               uint32_t *launches) {
+Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool counting,
+                               uint32_t min_blocks, uint32_t *launches) {
   if (num_sms_ == 0) {
     int dev = 0;
     PG_TRY_CUDA(cudaGetDevice(&dev), "device");
     PG_TRY_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev), "sm count");
   }
-  const unsigned long long total = (unsigned long long)p.x_dim * p.y_dim * p.spp;
+  // sample ids are pixel-major: the band's samples are one contiguous range
+  const unsigned long long first = (unsigned long long)p.row_lo * p.x_dim * p.spp;
+  const unsigned long long total =
+      (unsigned long long)(p.row_hi - p.row_lo) * p.x_dim * p.spp;
   const uint32_t n_slots = (uint32_t)std::min<unsigned long long>(total, 1ull << 21);
   auto a256 = [](size_t n) { return (n + 255) & ~size_t(255); };
   const size_t f4 = a256((size_t)n_slots * 16), u2 = a256((size_t)n_slots * 8),
@@ -655,7 +680,8 @@ Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t mi
   w.rays = reinterpret_cast<uint32_t *>(b + 7 * f4 + 2 * u2 + 2 * u1);
   w.q = wf_queues_.as<WaveQueues>();
   w.next_sample = reinterpret_cast<unsigned long long *>(wf_queues_.as<unsigned char>() + 32);
-  w.total_samples = total;
+  w.first_sample = first;
+  w.total_samples = first + total;
   w.sample_rgb = wf_samples_.as<float>();
   w.n_slots = n_slots;
   // queue heads: n_slots live slots, one extension ray each
@@ -663,7 +689,7 @@ Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t mi
   std::memset(h, 0, 64);
   h[0] = n_slots;
   h[2] = n_slots;
-  unsigned long long next = n_slots;
+  unsigned long long next = first + n_slots;
   std::memcpy(h + 8, &next, sizeof(next));
   PG_TRY_CUDA(cudaMemcpyAsync(wf_queues_.get(), h, 48, cudaMemcpyHostToDevice, stream_),
               "queue init");
@@ -693,7 +719,7 @@ Status Renderer::run_wavefront(const RenderParams &p, bool counting, uint32_t mi
       return Status::err(PATH_ERR_DEVICE_TIMEOUT, "wavefront did not drain");
     }
   }
-  PG_TRY_CUDA(launch_wavefront_sum(p, w.sample_rgb, stream_), "sample sum");
+  PG_TRY_CUDA(launch_wavefront_sum(p, w.sample_rgb, n_blocks, stream_), "sample sum");
   *launches += 1;
   return Status::ok();
 }

@@ -117,8 +117,8 @@ private:
   uint32_t sobol_bound_ = 0, sobol_count_ = 0;
   DeviceBuffer out_a_, out_b_, bgra_, status_, counters_, rays_, idxs_;
   // wavefront state
-  Status run_wavefront(const RenderParams &p, bool counting, uint32_t min_blocks,
-                       uint32_t *launches);
+  Status run_wavefront(const RenderParams &p, uint32_t n_blocks, bool counting,
+                       uint32_t min_blocks, uint32_t *launches);
   DeviceBuffer wf_slots_, wf_queues_, wf_samples_;
   PinnedBuffer wf_host_;
   int num_sms_ = 0;

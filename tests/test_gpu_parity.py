@@ -415,3 +415,31 @@ def test_wide_closest_hit_is_order_independent(lib, oracle):
         assert got[r] == perm[np.flatnonzero(col == tmin).min()]
         assert gt[r] == tmin
     assert ties > 10
+
+
+@pytest.mark.parametrize("case", ["mega_binary", "mega_wide", "streaming", "sample_blocks",
+                                  "bgra"])
+def test_row_band_equals_the_same_rows_of_the_whole_render(lib, case):
+    """SquareImage(rows=...) computes a band exactly as the whole-image render
+    does (the unit of sharding one image over GPUs) and leaves other rows."""
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "binary" if case == "mega_binary" else "wide")
+    spp, w, h = 8, 40, 36
+    if case == "streaming":
+        s.kernel_approach = 1
+    if case == "sample_blocks":
+        s.render_work_division.block_size = 32
+        s.render_work_division.force_target_samples = 1
+        s.render_work_division.forced_target_samples_per_thread = 1
+        spp = 64
+    f2w = scenes.cornell_camera(w, h)
+    bgra = case == "bgra"
+    whole = _render_gpu(sc, s, spp, w, h, f2w, bgra=bgra)
+    for lo, hi in [(0, 5), (5, 17), (17, 36), (3, 4)]:
+        band = np.full_like(whole, 7)
+        r = api.Renderer()
+        r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w, rows=(lo, hi)), band, sc,
+                 spp, s)
+        assert r.stats()["device_status"] == 0
+        assert np.array_equal(band[lo:hi], whole[lo:hi])
+        assert np.all(band[:lo] == 7) and np.all(band[hi:] == 7)
