@@ -110,6 +110,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _profiled_traffic(kernel, args):
+    """DRAM bytes per launch of the dominant kernel, from the committed ncu
+    summary of this workload (a line 'dram_bytes_per_launch: N' in
+    profiles/<kernel>_dram_<workload>.txt), or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_dram_{args.workload}.txt")
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("dram_bytes_per_launch:"):
+                    return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 def make_workload(name, size=None, spp_override=None):
     from path_gb300 import scenes
     if name == "large_mesh":
@@ -169,18 +184,89 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, rank, world, local_rank):
+    """The batched workload: seeded random scenes (room + 1-40 boxes and
+    spheres, 50k-200k triangles, diffuse / GGX / dielectric, resolution in
+    {64..256}^2, 8-128 spp, depth 6) in one path_render_batch call, launch
+    shape from path_batch_autotune."""
+    import torch
+    import torch.distributed as dist
+    from path_gb300 import api, scenes
+    t0 = time.time()
+    batch = scenes.batch_scenes(args.scenes, seed=0)
+    gen_s = time.time() - t0
+    settings = scenes.path_settings(6, "wide")
+    outs = [np.zeros((h, w, 3), np.float32) for _, w, h, _ in batch]
+    items = [(sc, api.SquareImage(w, h, scenes.cornell_camera(w, h)), o, spp)
+             for (sc, w, h, spp), o in zip(batch, outs)]
+    samples = sum(w * h * spp for _, w, h, spp in batch)
+    tris = sum(sc.sizes()["triangles"] for sc, _, _, _ in batch)
+    r = api.Renderer()
+    t0 = time.time()
+    tuning = r.autotune_batch(items, settings, sample_budget=1 << 24)
+    setup_s = time.time() - t0
+    build_s = r.stats()["bvh_build_seconds"]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        r.render_batch(items, settings, tuning)
+    kernel_ms, wall, launches = [], [], 0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r.render_batch(items, settings, tuning)
+            wall.append(time.perf_counter() - t)
+            st = r.stats()
+            kernel_ms.append(st["kernel_ms"])
+            launches += st["gpu_launches"]
+    torch.cuda.synchronize()
+    total_ms, e2e_total = sum(kernel_ms), sum(wall)
+    if world > 1:
+        t = torch.tensor([total_ms, e2e_total], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+    line = {
+        "metric": METRIC, "value": world * samples * args.steps / (total_ms / 1e3) / 1e6,
+        "unit": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched: {len(batch)} seeded scenes, {tris} triangles, "
+                               f"{samples} samples, depth 6",
+                   "tuning": tuning, "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * samples * args.steps / e2e_total / 1e6, "unit": METRIC,
+                "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(o.nbytes for o in outs))},
+        "gpu_launches": int(launches),
+        "setup_s": setup_s, "bvh_build_s": build_s, "scene_generation_s": gen_s,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="large_mesh", choices=["large_mesh", "cornell"])
+    ap.add_argument("--workload", default="large_mesh",
+                    choices=["large_mesh", "cornell", "batched"])
+    ap.add_argument("--scenes", type=int, default=256, help="batched workload: scene count")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
                     help="wavefront (streaming) or megakernel integration")
     ap.add_argument("--cpu-rows", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-megakernel", action="store_true",
+                    help="skip the megakernel comparison render")
     ap.add_argument("--size", type=int, default=None,
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
@@ -204,6 +290,9 @@ def main():
 
     from path_gb300 import api, build, scenes
     build.build()
+    if args.workload == "batched":
+        run_batched(args, rank, world, local_rank)
+        return
     scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, args.traversal)
     settings.kernel_approach = 1 if args.approach == "streaming" else 0
@@ -224,9 +313,11 @@ def main():
     counts = r.stats()
 
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    streaming = args.approach == "streaming"
+    settings.time_kernels = 1 if streaming else 0
     for _ in range(args.warmup):
         r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, settings)
-    kernel_ms, launches = [], 0
+    kernel_ms, trace_ms, trace_launches, launches = [], [], 0, 0
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -237,12 +328,15 @@ def main():
             r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, settings)
             st = r.stats()
             kernel_ms.append(st["kernel_ms"])
+            trace_ms.append(st["trace_ms"])
+            trace_launches += st["trace_launches"]
             launches += st["gpu_launches"]
         torch.cuda.synchronize()
         # end to end through the C ABI with host buffers
         host_out = np.zeros((h, w, 3), np.float32)
         es = settings.copy()
         es.upload_scene_every_render = 1
+        es.time_kernels = 0
         for _ in range(2):
             r.render(api.ExecutionModel.GPU, spec, host_out, scene, spp, es)
         e2e_s, h2d, d2h = [], 0, 0
@@ -269,9 +363,26 @@ def main():
 
     peak, peak_kind = _peaks()
     mean_ms = total_ms / args.steps
-    alg_bytes = counts["nodes_visited"] * 80 + counts["triangles_tested"] * 48 + \
-        counts["rays_traced"] * 96
-    achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    if streaming:
+        # dominant kernel: the persistent trace.  Per ray it reads its origin
+        # and direction (32 B) and writes its hit (8 B); per visit 80 B of
+        # wide node, per test 48 B of triangle.
+        alg_bytes = counts["nodes_visited"] * 80 + counts["triangles_tested"] * 48 + \
+            counts["rays_traced"] * 40
+        launches_per_render = trace_launches / args.steps
+        kern_ms = sum(trace_ms) / args.steps
+        kernel_name = "k_wf_trace"
+    else:
+        # the megakernel does everything: traversal plus 96 B of shading data
+        # (triangle normals + material) per traced ray
+        alg_bytes = counts["nodes_visited"] * 80 + counts["triangles_tested"] * 48 + \
+            counts["rays_traced"] * 96
+        launches_per_render = 1
+        kern_ms = mean_ms
+        kernel_name = "k_render"
+    achieved = alg_bytes / (kern_ms / 1e3) / 1e9
+    traffic = _profiled_traffic(kernel_name, args) if args.size is None and \
+        args.spp is None else None
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms,
@@ -287,15 +398,30 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": int(alg_bytes)},
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_kind": peak_kind, "kernel": kernel_name,
+                     "launches_per_step": launches_per_render,
+                     "kernel_ms_per_step": kern_ms,
+                     "algorithmic_bytes_per_launch": alg_bytes / launches_per_render},
         "mrays_per_s": counts["rays_traced"] / (mean_ms / 1e3) / 1e6,
         "work_counts": {"rays": counts["rays_traced"], "wide_nodes": counts["nodes_visited"],
                         "triangles": counts["triangles_tested"]},
         "setup_s": setup_s, "bvh_build_s": st0["bvh_build_seconds"],
         "clocks": clocks.summary(),
     }
+    if streaming and args.size is None and args.spp is None and not args.no_megakernel:
+        # the same render through the megakernel (identical image), for the
+        # wavefront-versus-megakernel comparison of this workload
+        ms = settings.copy()
+        ms.kernel_approach = 0
+        ms.time_kernels = 0
+        r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, ms)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, ms)
+        mk = r.stats()["kernel_ms"]
+        line["megakernel"] = {"value": samples / (mk / 1e3) / 1e6, "unit": METRIC,
+                              "ms_per_step": mk, "steps": 1}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n, secs = cpu_sample(scene, settings, spp, w, h, f2w, args.cpu_rows, threads)

@@ -129,7 +129,9 @@ typedef struct {
   uint32_t trace_min_blocks; /* streaming trace kernel: resident 256-thread
                                 blocks per SM it is compiled for (3..6, 0 =
                                 default 4); fewer registers per thread above 3 */
-  uint32_t reserved[3];
+  uint32_t time_kernels;     /* 1: time the streaming trace launches with CUDA
+                                events (path_render_stats.trace_ms) */
+  uint32_t reserved[2];
 } path_settings;
 
 typedef enum {
@@ -198,6 +200,9 @@ typedef struct {
   uint32_t num_wide_nodes;
   uint64_t h2d_bytes;        /* host -> device bytes copied by this render */
   uint64_t d2h_bytes;        /* device -> host bytes copied by this render */
+  double trace_ms;           /* time_kernels: summed event time of the
+                                streaming trace launches */
+  uint32_t trace_launches;   /* streaming trace launches of this render */
 } path_render_stats;
 
 /* ---- errors ---- */
@@ -218,6 +223,11 @@ void path_scene_destroy(path_scene *scene);
 path_status path_scene_add_material(path_scene *scene,
                                     const path_material *material,
                                     uint32_t *material_idx);
+/* replaces material material_idx in place (GB300 addition: parameter
+ * updates for differentiation); a renderer holding the scene re-uploads its
+ * materials and light table on the next render without rebuilding the BVH */
+path_status path_scene_set_material(path_scene *scene, uint32_t material_idx,
+                                    const path_material *material);
 /* triangles: [n][3][3]; normals: [n][3][3] vertex normals or NULL for the
  * face normal (scenefile_loader.cpp:280-284); material_idx per triangle.
  * Adds one mesh with an identity instance; emissive clusters follow
@@ -260,6 +270,64 @@ path_status path_render(path_renderer *renderer, uint32_t exec_model,
                         uint32_t show_progress, double *seconds);
 path_status path_renderer_stats(const path_renderer *renderer,
                                 path_render_stats *out);
+
+/* ---- adjoint (GB300 addition; the reference has no derivatives) ---- */
+/* Gradients of a loss of the rendered image with respect to each material's
+ * parameters, by path replay: a streaming forward render of (spec, scene,
+ * samples_per, settings), then the same paths re-run from their Sobol
+ * indices, accumulating per vertex the radiance that flowed through it times
+ * d log f / d(parameter).  d_image = dLoss/d(FloatRGB image), [y][x][3]
+ * floats (device memory if d_image_on_device).  d_params receives, per
+ * material, 7 doubles: d/d(reflectance r, g, b) (Diffuse albedo, GGX F0),
+ * d/d(GGX roughness), d/d(emission r, g, b).  Sampling densities and the
+ * light-selection table are held fixed (the detached estimator); other BSDF
+ * types transport light but get zero reflectance / roughness gradients.
+ * Square images and the 8-wide BVH only. */
+path_status path_render_adjoint(path_renderer *renderer, const path_sample_spec *sample_spec,
+                                const path_scene *scene, uint32_t samples_per,
+                                const path_settings *settings, const float *d_image,
+                                uint32_t d_image_on_device, double *d_params,
+                                double *seconds);
+
+/* ---- batched render (GB300 addition; the reference renders one scene per
+ * call) ---- */
+/* One image of a batch: a scene, its square-image camera, samples per pixel
+ * and where the image goes (FLOAT_RGB or BGRA, host or device memory). */
+typedef struct {
+  const path_scene *scene;
+  uint32_t x_dim, y_dim;
+  float film_to_world[12];
+  uint32_t samples_per;
+  path_output output;
+} path_batch_item;
+
+/* Launch shape of a batched render.  Every choice gives the same images
+ * (bit for bit); they only change speed.  Zero fields take the defaults in
+ * brackets. */
+typedef struct {
+  uint32_t slots_log2;          /* paths in flight = 2^slots_log2 [21] */
+  uint32_t trace_min_blocks;    /* trace kernel variant, 3..6 [4] */
+  uint32_t shade_ctas_per_sm;   /* shade grid = SMs x this [4] */
+  uint32_t iterations_per_graph; /* trace/shade iterations per CUDA-graph
+                                    launch between live-path checks [4] */
+} path_batch_tuning;
+
+/* Renders every item: all scenes' geometry in one device arena, all their
+ * samples through one persistent wavefront (one trace and one shade launch
+ * per iteration for the whole batch, replayed as a CUDA graph), then each
+ * image summed per pixel in the reference's order, so each image equals the
+ * single-scene streaming render of the same item.  Uses the streaming
+ * approach and the 8-wide BVH whatever settings->kernel_approach says;
+ * tuning may be NULL (defaults).  The scenes' BVHs are cached until a
+ * scene's contents or the batch's scene list change. */
+path_status path_render_batch(path_renderer *renderer, const path_batch_item *items,
+                              uint32_t n_items, const path_settings *settings,
+                              const path_batch_tuning *tuning, double *seconds);
+/* Times candidate launch shapes on the batch's first samples (at most
+ * sample_budget of them, no image output) and returns the fastest. */
+path_status path_batch_autotune(path_renderer *renderer, const path_batch_item *items,
+                                uint32_t n_items, const path_settings *settings,
+                                uint64_t sample_budget, path_batch_tuning *out);
 
 /* ---- accel / intersection (TriangleAccel concept,
  * include/intersect/accel/accel.h:35-77) ---- */

@@ -280,6 +280,64 @@ class Renderer:
                                            ctypes.byref(secs)))
         return secs.value
 
+    @staticmethod
+    def _output_c(output):
+        """(capi.Output, array) for a numpy or torch FloatRGB / BGRA image."""
+        o = capi.Output()
+        if hasattr(output, "data_ptr"):
+            import torch
+            if not output.is_contiguous():
+                raise ValueError("output tensor must be contiguous")
+            o.type = capi.OUTPUT_BGRA if output.dtype == torch.uint8 else capi.OUTPUT_FLOAT_RGB
+            o.data = output.data_ptr()
+            o.on_device = 1 if output.is_cuda else 0
+        else:
+            if not output.flags["C_CONTIGUOUS"]:
+                raise ValueError("output array must be C contiguous")
+            o.type = capi.OUTPUT_BGRA if output.dtype == np.uint8 else capi.OUTPUT_FLOAT_RGB
+            o.data = output.ctypes.data
+            o.on_device = 0
+        return o
+
+    @staticmethod
+    def _batch_c(items):
+        """items: sequence of (scene, SquareImage, output, samples_per)."""
+        arr = (capi.BatchItem * len(items))()
+        for k, (scene, spec, output, spp) in enumerate(items):
+            arr[k].scene = scene.handle
+            arr[k].x_dim = spec.x_dim
+            arr[k].y_dim = spec.y_dim
+            arr[k].film_to_world[:] = [float(v) for v in spec.film_to_world]
+            arr[k].samples_per = int(spp)
+            arr[k].output = Renderer._output_c(output)
+        return arr
+
+    def render_batch(self, items, settings, tuning=None):
+        """Batched render (path_render_batch): items are (scene, SquareImage,
+        output, samples_per); tuning a dict of path_batch_tuning fields or
+        None.  Returns seconds."""
+        arr = self._batch_c(items)
+        t = None
+        if tuning is not None:
+            t = capi.BatchTuning()
+            for k, v in tuning.items():
+                setattr(t, k, int(v))
+        secs = ctypes.c_double()
+        capi.check(capi.load().path_render_batch(self._h, arr, len(items),
+                                                 ctypes.byref(settings.raw),
+                                                 None if t is None else ctypes.byref(t),
+                                                 ctypes.byref(secs)))
+        return secs.value
+
+    def autotune_batch(self, items, settings, sample_budget=0):
+        """Fastest launch shape for the batch (path_batch_autotune), as a dict."""
+        arr = self._batch_c(items)
+        t = capi.BatchTuning()
+        capi.check(capi.load().path_batch_autotune(self._h, arr, len(items),
+                                                   ctypes.byref(settings.raw),
+                                                   int(sample_budget), ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in capi.BatchTuning._fields_}
+
     def stats(self):
         s = capi.RenderStats()
         capi.check(capi.load().path_renderer_stats(self._h, ctypes.byref(s)))

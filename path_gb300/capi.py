@@ -43,7 +43,7 @@ class PathSettings(ctypes.Structure):
                 ("back_cull_emission", c_u32), ("traversal", c_u32),
                 ("persistent_ctas_per_sm", c_u32), ("count_work", c_u32),
                 ("upload_scene_every_render", c_u32), ("trace_min_blocks", c_u32),
-                ("reserved", c_u32 * 3)]
+                ("time_kernels", c_u32), ("reserved", c_u32 * 2)]
 
 
 class SampleSpec(ctypes.Structure):
@@ -58,13 +58,24 @@ class Output(ctypes.Structure):
                 ("n_steps", c_u32)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("x_dim", c_u32), ("y_dim", c_u32),
+                ("film_to_world", c_f32 * 12), ("samples_per", c_u32), ("output", Output)]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("slots_log2", c_u32), ("trace_min_blocks", c_u32),
+                ("shade_ctas_per_sm", c_u32), ("iterations_per_graph", c_u32)]
+
+
 class RenderStats(ctypes.Structure):
     _fields_ = [("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double),
                 ("bvh_build_seconds", ctypes.c_double), ("rays_traced", ctypes.c_uint64),
                 ("nodes_visited", ctypes.c_uint64), ("triangles_tested", ctypes.c_uint64),
                 ("gpu_launches", c_u32), ("device_status", c_u32),
                 ("num_bvh_nodes", c_u32), ("num_wide_nodes", c_u32),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("trace_ms", ctypes.c_double), ("trace_launches", c_u32)]
 
 
 # enums
@@ -117,6 +128,18 @@ SIGNATURES = {
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),
+    "path_render_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), _P, c_u32,
+                                           ctypes.POINTER(PathSettings), _PF, c_u32,
+                                           ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]),
+    "path_scene_set_material": (ctypes.c_int, [_P, c_u32, ctypes.POINTER(PathMaterial)]),
+    "path_render_batch": (ctypes.c_int, [_P, ctypes.POINTER(BatchItem), c_u32,
+                                         ctypes.POINTER(PathSettings),
+                                         ctypes.POINTER(BatchTuning),
+                                         ctypes.POINTER(ctypes.c_double)]),
+    "path_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(BatchItem), c_u32,
+                                           ctypes.POINTER(PathSettings), ctypes.c_uint64,
+                                           ctypes.POINTER(BatchTuning)]),
     "path_render_noalloc": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), ctypes.POINTER(Output),
                                            _P, c_u32, ctypes.POINTER(PathSettings),
                                            ctypes.POINTER(ctypes.c_double)]),

@@ -127,6 +127,22 @@ path_status path_scene_add_material(path_scene *scene, const path_material *m,
   });
 }
 
+path_status path_scene_set_material(path_scene *scene, uint32_t material_idx,
+                                    const path_material *m) {
+  if (!scene || !m) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  if (m->type > PATH_BSDF_GGX) {
+    return fail(PATH_ERR_ARGUMENT, "unknown bsdf type");
+  }
+  if (material_idx >= scene->s.materials.size()) {
+    return fail(PATH_ERR_ARGUMENT, "material index out of range");
+  }
+  scene->s.materials[material_idx] = *m;
+  ++scene->s.material_version;
+  return PATH_OK;
+}
+
 // TriangleConstructor::add_triangle (src/scene/triangle_constructor.cpp:14-30):
 // face normals when none are given, and one emissive cluster per emissive
 // triangle
@@ -281,6 +297,71 @@ path_status path_render(path_renderer *renderer, uint32_t exec_model,
   return guarded([&] {
     return from(renderer->r.render(*sample_spec, *output, scene->s, samples_per, *settings,
                                    seconds));
+  });
+}
+
+path_status path_render_adjoint(path_renderer *renderer, const path_sample_spec *sample_spec,
+                                const path_scene *scene, uint32_t samples_per,
+                                const path_settings *settings, const float *d_image,
+                                uint32_t d_image_on_device, double *d_params,
+                                double *seconds) {
+  if (!renderer || !sample_spec || !scene || !settings || !d_image || !d_params) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    return from(renderer->r.render_adjoint(*sample_spec, scene->s, samples_per, *settings,
+                                           d_image, d_image_on_device != 0, d_params,
+                                           seconds));
+  });
+}
+
+static path_status batch_items(const path_batch_item *items, uint32_t n,
+                               std::vector<pg::BatchItem> &out) {
+  out.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!items[i].scene) {
+      return fail(PATH_ERR_ARGUMENT, "batch item without scene");
+    }
+    pg::BatchItem &b = out[i];
+    b.scene = &items[i].scene->s;
+    b.x_dim = items[i].x_dim;
+    b.y_dim = items[i].y_dim;
+    b.spp = items[i].samples_per;
+    std::memcpy(b.f2w, items[i].film_to_world, sizeof(b.f2w));
+    b.output = items[i].output;
+  }
+  return PATH_OK;
+}
+
+path_status path_render_batch(path_renderer *renderer, const path_batch_item *items,
+                              uint32_t n_items, const path_settings *settings,
+                              const path_batch_tuning *tuning, double *seconds) {
+  if (!renderer || (n_items > 0 && !items) || !settings) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    std::vector<pg::BatchItem> v;
+    path_status s = batch_items(items, n_items, v);
+    if (s != PATH_OK) {
+      return s;
+    }
+    return from(renderer->r.render_batch(v, *settings, tuning, seconds));
+  });
+}
+
+path_status path_batch_autotune(path_renderer *renderer, const path_batch_item *items,
+                                uint32_t n_items, const path_settings *settings,
+                                uint64_t sample_budget, path_batch_tuning *out) {
+  if (!renderer || (n_items > 0 && !items) || !settings || !out) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    std::vector<pg::BatchItem> v;
+    path_status s = batch_items(items, n_items, v);
+    if (s != PATH_OK) {
+      return s;
+    }
+    return from(renderer->r.autotune_batch(v, *settings, sample_budget, out));
   });
 }
 

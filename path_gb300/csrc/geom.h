@@ -70,6 +70,7 @@ PM_HD rgb mkrgb(float r, float g, float b) {
   return o;
 }
 PM_HD rgb operator+(rgb a, rgb b) { return mkrgb(a.r + b.r, a.g + b.g, a.b + b.b); }
+PM_HD rgb operator-(rgb a, rgb b) { return mkrgb(a.r - b.r, a.g - b.g, a.b - b.b); }
 PM_HD rgb operator*(rgb a, rgb b) { return mkrgb(a.r * b.r, a.g * b.g, a.b * b.b); }
 PM_HD rgb operator*(rgb a, float s) { return mkrgb(a.r * s, a.g * s, a.b * s); }
 PM_HD rgb operator/(rgb a, float s) { return mkrgb(a.r / s, a.g / s, a.b / s); }

@@ -172,6 +172,19 @@ __device__ __forceinline__ float byte8_float(uint32_t lo, uint32_t hi, int i) {
 
 constexpr int kWideStack = (int)kWideStackDepth;
 
+// three-operand minimum / maximum (one instruction on sm_100 and later)
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 // Order-independent closest hit of the wide traversal: the smallest
 // distance wins and, at equal distance, the smallest BVH-order index, so the
 // result does not depend on the order in which nodes are visited.  With
@@ -197,6 +210,7 @@ struct WideWalk {
   ray r;
   f3 inv;
   Hit best;   // best.t is the pruning distance: tlimit until the first hit
+  float light_target; // shadow rays: the light point's distance, else -INF
   uint32_t oct;
   uint32_t ng_base, ng_bits;
   int sp;
@@ -207,17 +221,28 @@ struct WideWalk {
 // just past the light); INF for extension rays.  Within the limit the
 // closest hit is the same as without it.
 __device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, const ray &r,
-                                           float tlimit) {
+                                           float tlimit, float light_target,
+                                           uint32_t root = 0) {
   w.r = r;
   w.inv = inv_dir(r.d);
   w.best = no_hit();
   w.best.t = tlimit;
+  w.light_target = light_target;
   w.oct = (w.inv.x < 0.f ? 1u : 0u) | (w.inv.y < 0.f ? 2u : 0u) | (w.inv.z < 0.f ? 4u : 0u);
   // the root as the only child of a pseudo node in slot 0
-  w.ng_base = 0;
+  w.ng_base = root;
   w.ng_bits = 1u | (1u << (8 + w.oct));
   w.sp = 0;
   w.done = P.n_wide_nodes == 0;
+}
+
+// A shadow ray only asks whether its closest hit lies within 1e-6 of the
+// light point (rendering_equation_iteration.h:22-27, 44-55).  A hit with
+// target - t > 1e-6 (in float, so every closer hit fails the same test)
+// settles that it does not: the walk may stop there, and the hit it
+// reports gives the same answer as the closest one.
+__device__ __forceinline__ bool shadow_settled(const WideWalk &w) {
+  return w.best.ok && w.light_target - w.best.t > 1e-6f;
 }
 
 // Enter the next child of the current node group and test its eight slots;
@@ -289,9 +314,10 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
     const float tfy = __fmaf_rn(byte8_float(fyl, fyh, i), ay, bfy);
     const float tnz = __fmaf_rn(byte8_float(nzl, nzh, i), az, bnz);
     const float tfz = __fmaf_rn(byte8_float(fzl, fzh, i), az, bfz);
-    const float tmin = fmaxf(fmaxf(tnx, tny), tnz);
-    const float tmax = fminf(fminf(tfx, tfy), tfz);
-    const bool hit = tmin <= tmax && tmax >= 0.f && tmin <= tcull;
+    // tmin <= tmax && tmax >= 0 && tmin <= tcull, as one comparison (tcull >= 0)
+    const float tmin = fmax3(tnx, tny, fmaxf(tnz, 0.f));
+    const float tmax = fmin3(tfx, tfy, fminf(tfz, tcull));
+    const bool hit = tmin <= tmax;
     const uint32_t meta = byte_of(n1.z, n1.w, i);
     if ((imask >> i) & 1u) {
       hits |= (hit ? 1u : 0u) << (i ^ (int)w.oct);
@@ -345,12 +371,16 @@ __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
     }
     wide_tri(P, w.r, tri_base + k, w.best);
   }
+  if (shadow_settled(w)) {
+    w.done = true;
+  }
 }
 
 template <bool kCount>
-__device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, float tlimit) {
+__device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, float tlimit,
+                          float light_target) {
   WideWalk w;
-  wide_begin(P, w, r, tlimit);
+  wide_begin(P, w, r, tlimit, light_target);
   uint32_t st_base[kWideStack];
   uint32_t st_bits[kWideStack];
   while (!w.done) {
@@ -363,12 +393,12 @@ __device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, floa
 // pruning exactly and ignores tlimit
 template <uint32_t kTrav, bool kCount>
 __device__ __forceinline__ Hit trace(const RenderParams &P, const ray &r, Counts &cnt,
-                                     float tlimit) {
+                                     float tlimit, float light_target) {
   if (kCount) {
     ++cnt.rays;
   }
   if (kTrav == kTravWide) {
-    return trace_wide<kCount>(P, r, cnt, tlimit);
+    return trace_wide<kCount>(P, r, cnt, tlimit, light_target);
   }
   return trace_binary<kCount>(P, r, cnt);
 }
@@ -543,6 +573,52 @@ __device__ rgb ggx_eval(const Mat &m, f3 in, f3 out, f3 n) {
   rgb f = schlick(m.specular, dot(wo, h));
   float scale = (d * g) / ((4.f * ci) * co);
   return f * scale;
+}
+
+// d log f / d(parameter) of a differentiable BSDF at (in, out, n): per
+// channel for the reflectance (Diffuse albedo, GGX F0) in `refl`, and for
+// the GGX roughness alpha in `rough`.  d log D/d a2 = 1/a2 - 2 ch^2/dd;
+// d log G1(c)/d a2 = -(1 - c^2) / (2 s (c + s)) with s = sqrt(a2 + (1-a2)c^2);
+// d/d alpha = 2 alpha d/d a2.  False for materials without these parameters
+// or directions where f vanishes.
+__device__ bool bsdf_log_grad(const Mat &m, f3 in, f3 out, f3 n, rgb &refl, float &rough) {
+  if (m.type == kDiffuse) {
+    refl = mkrgb(m.diffuse.r > 0.f ? 1.f / m.diffuse.r : 0.f,
+                 m.diffuse.g > 0.f ? 1.f / m.diffuse.g : 0.f,
+                 m.diffuse.b > 0.f ? 1.f / m.diffuse.b : 0.f);
+    rough = 0.f;
+    return true;
+  }
+  if (m.type != kGGX) {
+    return false;
+  }
+  f3 wo = -in;
+  if (dot(wo, n) < 0.f) {
+    n = -n;
+  }
+  float co = dot(wo, n);
+  float ci = dot(out, n);
+  if (!(co > 0.f) || !(ci > 0.f)) {
+    return false;
+  }
+  float a = m.roughness;
+  float a2 = a * a;
+  f3 h = normalize(wo + out);
+  float ch = dot(h, n);
+  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
+  float dlog_d = 1.f / a2 - (2.f * (ch * ch)) / dd;
+  float so = pm::sqrt(a2 + (1.f - a2) * (co * co));
+  float si = pm::sqrt(a2 + (1.f - a2) * (ci * ci));
+  float dlog_g = -(1.f - co * co) / ((2.f * so) * (co + so)) -
+                 (1.f - ci * ci) / ((2.f * si) * (ci + si));
+  rough = (2.f * a) * (dlog_d + dlog_g);
+  float c = dot(wo, h);
+  float mm = 1.f - c;
+  float m5 = ((mm * mm) * (mm * mm)) * mm;
+  rgb f = schlick(m.specular, c);
+  refl = mkrgb(f.r > 0.f ? (1.f - m5) / f.r : 0.f, f.g > 0.f ? (1.f - m5) / f.g : 0.f,
+               f.b > 0.f ? (1.f - m5) / f.b : 0.f);
+  return true;
 }
 
 __device__ rgb continuous_eval(const Mat &m, f3 in, f3 out, f3 n) {
@@ -721,24 +797,39 @@ struct LightSample {
   float target;
 };
 
-__device__ bool sample_light(const RenderParams &P, f3 pos, const Mat &m, f3 normal,
-                             Rng &rng, LightSample &out) {
-  if (P.n_lights == 0) {
+// the emissive triangles of one scene and their area x emission CDF
+struct LightSet {
+  const float4 *tris;
+  const float *cdf;
+  uint32_t n;
+};
+
+__device__ __forceinline__ LightSet lights_of(const RenderParams &P) {
+  LightSet l;
+  l.tris = P.light_tris;
+  l.cdf = P.light_cdf;
+  l.n = P.n_lights;
+  return l;
+}
+
+__device__ bool sample_light(const LightSet &L, f3 pos, const Mat &m, f3 normal, Rng &rng,
+                             LightSample &out) {
+  if (L.n == 0) {
     return false;
   }
   float search = rng.next();
   uint32_t idx = 0;
-  for (; idx < P.n_lights; ++idx) {
-    if (__ldg(P.light_cdf + idx) >= search) {
+  for (; idx < L.n; ++idx) {
+    if (__ldg(L.cdf + idx) >= search) {
       break;
     }
   }
-  if (idx >= P.n_lights) {
-    idx = P.n_lights - 1; // unreachable for a normalised table
+  if (idx >= L.n) {
+    idx = L.n - 1; // unreachable for a normalised table
   }
-  float4 a = __ldg(P.light_tris + 3 * idx);
-  float4 b = __ldg(P.light_tris + 3 * idx + 1);
-  float4 c = __ldg(P.light_tris + 3 * idx + 2);
+  float4 a = __ldg(L.tris + 3 * idx);
+  float4 b = __ldg(L.tris + 3 * idx + 1);
+  float4 c = __ldg(L.tris + 3 * idx + 2);
   f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
   float s = rng.next();
   float t = rng.next();
@@ -753,7 +844,7 @@ __device__ bool sample_light(const RenderParams &P, f3 pos, const Mat &m, f3 nor
   }
   f3 dir = normalize(dir_un);
   f3 tn = cross(e0, e1) * 0.5f;
-  float prob = __ldg(P.light_cdf + idx) - (idx == 0 ? 0.f : __ldg(P.light_cdf + idx - 1));
+  float prob = __ldg(L.cdf + idx) - (idx == 0 ? 0.f : __ldg(L.cdf + idx - 1));
   float nw = pm::fabs(dot(normal, dir) * dot(tn, dir));
   if (nw <= 1e-8f) {
     return false;
@@ -790,10 +881,24 @@ __device__ __forceinline__ float term_prob(const RenderParams &P, uint32_t iters
 }
 
 // camera ray (initial_ray_sample.h:16-56)
-__device__ __forceinline__ ray camera_ray(const RenderParams &P, float x, float y) {
-  f3 film = mk((2.0f * x) / (float)P.x_dim - 1.0f, (-2.0f * y) / (float)P.y_dim + 1.0f,
+// film_to_world and image size of one camera
+struct Camera {
+  const float *f2w;
+  uint32_t x_dim, y_dim;
+};
+
+__device__ __forceinline__ Camera camera_of(const RenderParams &P) {
+  Camera c;
+  c.f2w = P.f2w;
+  c.x_dim = P.x_dim;
+  c.y_dim = P.y_dim;
+  return c;
+}
+
+__device__ __forceinline__ ray camera_ray(const Camera &cam, float x, float y) {
+  f3 film = mk((2.0f * x) / (float)cam.x_dim - 1.0f, (-2.0f * y) / (float)cam.y_dim + 1.0f,
                -1.0f);
-  const float *m = P.f2w;
+  const float *m = cam.f2w;
   f3 world = mk(((m[0] * film.x + m[1] * film.y) + m[2] * film.z) + m[3],
                 ((m[4] * film.x + m[5] * film.y) + m[6] * film.z) + m[7],
                 ((m[8] * film.x + m[9] * film.y) + m[10] * film.z) + m[11]);
@@ -833,9 +938,10 @@ struct PathState {
 
 // camera ray of a sample (initial_ray_sample.h:36-56): 2 RNG draws for a
 // square image, the caller's ray for an InitialRays spec
-__device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sample_idx,
-                                           uint32_t x, uint32_t y, PathState &s) {
-  const uint32_t location = x + y * P.x_dim;
+__device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Camera &cam,
+                                               uint32_t sample_idx, uint32_t x, uint32_t y,
+                                               PathState &s) {
+  const uint32_t location = x + y * cam.x_dim;
   s.rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
   s.rng.bound = P.dim_bound;
   s.rng.dim = fnv_hash(location) % P.init_dim_bound;
@@ -848,7 +954,7 @@ __device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sampl
   } else {
     float xo = s.rng.next();
     float yo = s.rng.next();
-    r = camera_ray(P, (float)x + xo, (float)y + yo);
+    r = camera_ray(cam, (float)x + xo, (float)y + yo);
   }
   s.o = r.o;
   s.d = r.d;
@@ -863,18 +969,40 @@ __device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sampl
   s.has_light = false;
 }
 
+__device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sample_idx,
+                                           uint32_t x, uint32_t y, PathState &s) {
+  path_begin_cam(P, camera_of(P), sample_idx, x, y, s);
+}
+
 // One rendering_equation_iteration (rendering_equation_iteration.h:9-153)
 // given the closest hits of the pending light ray (lh) and extension ray
 // (nh).  Returns true while the path has rays left to trace; s.total is the
 // sample's radiance once it returns false.
-__device__ __noinline__ bool path_step(const RenderParams &P, PathState &s, const Hit &lh,
-                                       const Hit &nh) {
+// What one path_step did, for the adjoint replay: the radiance its pending
+// light ray and its hit's emission added (and from which materials), the
+// shaded vertex, and the directions its light sample and continuation took.
+struct StepTrace {
+  bool light_added, emit_added, hit, nee, continuous;
+  uint32_t light_mat, mat;
+  f3 in, normal, nee_dir, next_dir;
+};
+
+__device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L, PathState &s,
+                                       const Hit &lh, const Hit &nh,
+                                       StepTrace *tr = nullptr) {
   const bool performs_samples = P.light_sampler == 0;
   const bool cull = P.back_cull != 0;
+  if (tr != nullptr) {
+    tr->light_added = tr->emit_added = tr->hit = tr->nee = tr->continuous = false;
+  }
   if (s.has_light && lh.ok && pm::fabs(s.light_target - lh.t) <= 1e-6f &&
       (!cull || !lh.back)) {
     float4 c = __ldg(P.tri_data + 3 * lh.idx + 2);
     s.total = s.total + emission_of(P.materials + __float_as_uint(c.w)) * s.light_mult;
+    if (tr != nullptr) {
+      tr->light_added = true;
+      tr->light_mat = __float_as_uint(c.w);
+    }
   }
   if (!s.has_next || !nh.ok) {
     return false;
@@ -885,6 +1013,15 @@ __device__ __noinline__ bool path_step(const RenderParams &P, PathState &s, cons
   const Mat mat = load_mat(P.materials + mi);
   if ((!performs_samples || s.count_emission) && (!cull || !nh.back)) {
     s.total = s.total + s.multiplier * mat.emission;
+    if (tr != nullptr) {
+      tr->emit_added = true;
+    }
+  }
+  if (tr != nullptr) {
+    tr->hit = true;
+    tr->mat = mi;
+    tr->in = s.d;
+    tr->normal = normal;
   }
   bool new_has_light = false;
   rgb new_light_mult = zero_rgb();
@@ -893,12 +1030,16 @@ __device__ __noinline__ bool path_step(const RenderParams &P, PathState &s, cons
   float pc = prob_continuous(mat);
   if (pc > 0.f && performs_samples) {
     LightSample ls;
-    if (sample_light(P, point, mat, normal, s.rng, ls)) {
+    if (sample_light(L, point, mat, normal, s.rng, ls)) {
       rgb f = continuous_eval(mat, s.d, ls.dir, normal);
       new_light_mult = ((s.multiplier * f) * pc) / ls.mult;
       new_light_target = ls.target;
       new_ld = ls.dir;
       new_has_light = true;
+      if (tr != nullptr) {
+        tr->nee = true;
+        tr->nee_dir = ls.dir;
+      }
     }
   }
   bool take_discrete;
@@ -916,6 +1057,10 @@ __device__ __noinline__ bool path_step(const RenderParams &P, PathState &s, cons
     smp = continuous_sample(mat, s.d, normal, s.rng);
   } else {
     smp = uniform_dir_sample(mat, s.d, normal, s.rng);
+  }
+  if (tr != nullptr) {
+    tr->continuous = !take_discrete;
+    tr->next_dir = smp.dir;
   }
   rgb new_multiplier = s.multiplier * smp.mult;
   float p = term_prob(P, s.iters, new_multiplier);
@@ -960,7 +1105,7 @@ __device__ __forceinline__ void step_hits(const RenderParams &P, const PathState
     ray lr;
     lr.o = s.o;
     lr.d = s.ld;
-    lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target));
+    lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target), s.light_target);
   }
   if (first && P.initial_idx != nullptr) {
     nh.t = 1.f;
@@ -971,7 +1116,7 @@ __device__ __forceinline__ void step_hits(const RenderParams &P, const PathState
     ray r;
     r.o = s.o;
     r.d = s.d;
-    nh = trace<kTrav, kCount>(P, r, cnt, PG_INF);
+    nh = trace<kTrav, kCount>(P, r, cnt, PG_INF, -PG_INF);
   }
 }
 
@@ -986,7 +1131,7 @@ __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
     Hit lh, nh;
     step_hits<kTrav, kCount>(P, s, first, x, cnt, lh, nh);
     first = false;
-    if (!path_continues(P, s, path_step(P, s, lh, nh))) {
+    if (!path_continues(P, s, path_step(P, lights_of(P), s, lh, nh))) {
       return s.total;
     }
   }
@@ -1003,7 +1148,7 @@ __device__ void integrate_sample_steps(const RenderParams &P, uint32_t sample_id
   for (uint32_t k = 0; k < P.n_steps; ++k) {
     Hit lh, nh;
     step_hits<kTrav, false>(P, s, k == 0, x, cnt, lh, nh);
-    const bool cont = path_step(P, s, lh, nh);
+    const bool cont = path_step(P, lights_of(P), s, lh, nh);
     steps[k] = steps[k] + s.total;
     s.total = zero_rgb();
     if (!cont) {

@@ -63,6 +63,17 @@ struct WaveQueues {
   uint32_t pad[3];
 };
 
+// one scene of a batched render: its camera, samples and place in the
+// concatenated geometry (wide nodes, triangles, materials, lights)
+struct BatchScene {
+  float f2w[12];
+  uint32_t x_dim, y_dim, spp;
+  uint32_t root;               // wide-node index of the scene's root
+  uint32_t light_off, n_lights; // its emissive triangles in the light table
+  uint32_t pad[2];
+  unsigned long long first_sample; // global id of its first sample
+};
+
 // wavefront render state (device pointers); slot arrays hold PathState
 struct WaveParams {
   RenderParams P;
@@ -82,15 +93,29 @@ struct WaveParams {
   unsigned long long total_samples; // one past the last sample id
   float *sample_rgb;   // [total_samples - first_sample][3]
   uint32_t n_slots;
+  // batched render: sample ids run over the scenes in order (nullptr: the
+  // single scene of P)
+  const BatchScene *scenes;
+  uint32_t n_scenes;
+  // adjoint replay (gradient shading only).  sample_rgb then holds the
+  // forward render's per-sample radiance and is only read.
+  const float *d_image;  // dLoss / d(pixel radiance), [x_dim * y_dim][3]
+  float4 *pend_refl;     // pending vertex: d log f / d(reflectance rgb, roughness)
+                         // along its continuation
+  float4 *pend_nee;      // ... along its light sample
+  uint32_t *pend_mat;    // its material, 0xffffffff when none
+  double *d_params;      // [materials][7]: reflectance rgb, roughness, emission rgb
 };
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
 // resident blocks per SM of the trace kernel compiled for min_blocks
 int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting);
-// one trace + shade iteration (three launches)
-cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity,
-                                       uint32_t trace_grid, uint32_t shade_grid,
-                                       uint32_t min_blocks, bool counting, cudaStream_t s);
+// one wavefront iteration: trace the queued rays, then reset the queues
+// and shade (launch_wavefront_shade)
+cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
+                                   uint32_t min_blocks, bool counting, cudaStream_t s);
+cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_t shade_grid,
+                                   cudaStream_t s, bool grad = false);
 // per-pixel sums of the sample buffer into p.out_rgb / p.out_bgra
 cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
                                  uint32_t n_blocks, cudaStream_t s);

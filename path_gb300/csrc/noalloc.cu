@@ -87,6 +87,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   }
   if (!initialised_ || !prep_.valid || prep_.scene_id != scene.id ||
       prep_.scene_version != scene.version ||
+      prep_.material_version != scene.material_version ||
       prep_.sbvh.overlap_threshold != st.overlap_threshold ||
       prep_.sbvh.use_spatial_splits != (st.use_spatial_splits != 0) ||
       prep_.sbvh.traversal_per_intersect_cost != st.traversal_per_intersect_cost ||

@@ -106,7 +106,7 @@ __global__ void k_intersect(const RenderParams P, const float *rays, uint32_t n,
   r.o = mk(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
   r.d = mk(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
   Counts cnt = {0, 0, 0};
-  Hit h = trace<kTrav, false>(P, r, cnt, PG_INF);
+  Hit h = trace<kTrav, false>(P, r, cnt, PG_INF, -PG_INF);
   idx_out[i] = h.ok ? (int32_t)bvh_to_orig[h.idx] : -1;
   t_out[i] = h.ok ? h.t : __int_as_float(0x7fc00000);
 }

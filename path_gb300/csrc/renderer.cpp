@@ -96,6 +96,9 @@ Renderer::~Renderer() {
     cudaStreamSynchronize(stream_);
     cudaEventDestroy(ev_start_);
     cudaEventDestroy(ev_stop_);
+    for (cudaEvent_t e : trace_ev_) {
+      cudaEventDestroy(e);
+    }
     cudaStreamDestroy(stream_);
   }
 }
@@ -117,7 +120,7 @@ Status Renderer::init() {
   return Status::ok();
 }
 
-static DevMaterial to_dev(const path_material &m) {
+DevMaterial to_dev(const path_material &m) {
   DevMaterial d;
   std::memset(&d, 0, sizeof(d));
   d.type = m.type;
@@ -139,7 +142,7 @@ static DevMaterial to_dev(const path_material &m) {
   return d;
 }
 
-static void put_tri(float *dst, f3 v0, f3 v1, f3 v2, uint32_t extra_bits) {
+void put_tri(float *dst, f3 v0, f3 v1, f3 v2, uint32_t extra_bits) {
   f3 e1 = v1 - v0, e2 = v2 - v0;
   float vals[12] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y, e2.z, 0.f, 0.f, 0.f};
   std::memcpy(&vals[10], &extra_bits, sizeof(extra_bits));
@@ -194,17 +197,7 @@ Status Renderer::upload_geometry(const FlatScene &flat,
     put_tri(&wtris[12 * k], flat.v0[o], flat.v1[o], flat.v2[o], 0);
     std::memcpy(&wtris[12 * k + 9], &b, sizeof(b));
   }
-  DevMaterial *dm = st_mats_.as<DevMaterial>();
-  for (size_t i = 0; i < mats.size(); ++i) {
-    dm[i] = to_dev(mats[i]);
-  }
-  float *lt = st_lights_.as<float>();
-  for (size_t i = 0; i < flat.light_v0.size(); ++i) {
-    put_tri(&lt[12 * i], flat.light_v0[i], flat.light_v1[i], flat.light_v2[i], 0);
-  }
-  if (!flat.light_cdf.empty()) {
-    std::memcpy(st_cdf_.get(), flat.light_cdf.data(), flat.light_cdf.size() * 4);
-  }
+  stage_materials(flat, mats);
   if (!bvh.permutation.empty()) {
     std::memcpy(st_perm_.get(), bvh.permutation.data(), bvh.permutation.size() * 4);
   }
@@ -216,6 +209,38 @@ Status Renderer::upload_geometry(const FlatScene &flat,
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "upload sync");
   prep_.n_tris = (uint32_t)n;
   prep_.n_lights = (uint32_t)flat.light_v0.size();
+  return Status::ok();
+}
+
+// materials and the light table (which depends on emission) into staging
+void Renderer::stage_materials(const FlatScene &flat, const std::vector<path_material> &mats) {
+  DevMaterial *dm = st_mats_.as<DevMaterial>();
+  for (size_t i = 0; i < mats.size(); ++i) {
+    dm[i] = to_dev(mats[i]);
+  }
+  float *lt = st_lights_.as<float>();
+  for (size_t i = 0; i < flat.light_v0.size(); ++i) {
+    put_tri(&lt[12 * i], flat.light_v0[i], flat.light_v1[i], flat.light_v2[i], 0);
+  }
+  if (!flat.light_cdf.empty()) {
+    std::memcpy(st_cdf_.get(), flat.light_cdf.data(), flat.light_cdf.size() * 4);
+  }
+}
+
+// after an in-place material edit: new materials and light table, same BVH
+Status Renderer::refresh_materials(const Scene &scene, uint64_t *bytes) {
+  FlatScene flat = flatten(scene);
+  PG_TRY_CUDA(st_mats_.ensure(scene.materials.size() * sizeof(DevMaterial)), "staging");
+  PG_TRY_CUDA(st_lights_.ensure(flat.light_v0.size() * 48), "staging");
+  PG_TRY_CUDA(st_cdf_.ensure(flat.light_cdf.size() * 4), "staging");
+  stage_materials(flat, scene.materials);
+  PG_TRY_CUDA(materials_.upload(st_mats_.get(), st_mats_.bytes, stream_), "material upload");
+  PG_TRY_CUDA(light_tris_.upload(st_lights_.get(), st_lights_.bytes, stream_), "light upload");
+  PG_TRY_CUDA(light_cdf_.upload(st_cdf_.get(), st_cdf_.bytes, stream_), "light upload");
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "upload sync");
+  *bytes += st_mats_.bytes + st_lights_.bytes + st_cdf_.bytes;
+  prep_.n_lights = (uint32_t)flat.light_v0.size();
+  prep_.material_version = scene.material_version;
   return Status::ok();
 }
 
@@ -311,6 +336,18 @@ void Renderer::fill_params(RenderParams &p) const {
 
 static_assert(kMaxOutputSteps == PATH_MAX_OUTPUT_STEPS, "step bound");
 
+// i-th event of the trace-timing pool (created on first use)
+cudaEvent_t Renderer::trace_event(size_t i) {
+  while (trace_ev_.size() <= i) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      return nullptr;
+    }
+    trace_ev_.push_back(e);
+  }
+  return trace_ev_[i];
+}
+
 // the resident BVH within the traversal kernels' fixed stacks
 Status Renderer::traversal_fits(const path_settings &st) const {
   if (st.traversal == PATH_TRAVERSAL_WIDE8 && prep_.wide.depth + 1 > kWideStackDepth) {
@@ -328,7 +365,7 @@ Status Renderer::traversal_fits(const path_settings &st) const {
   return Status::ok();
 }
 
-static Status check_settings(const path_settings &s) {
+Status check_settings(const path_settings &s) {
   if (s.kernel_approach != PATH_KERNEL_MEGA && s.kernel_approach != PATH_KERNEL_STREAMING) {
     return Status::err(PATH_ERR_ARGUMENT, "unknown kernel_approach");
   }
@@ -429,7 +466,15 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     if (!su.good()) {
       return su;
     }
+    prep_.material_version = scene.material_version;
     prep_.valid = true;
+  }
+  uint64_t h2d = 0;
+  if (!rebuilt && prep_.material_version != scene.material_version) {
+    Status sm = refresh_materials(scene, &h2d);
+    if (!sm.good()) {
+      return sm;
+    }
   }
   if (st.kernel_approach == PATH_KERNEL_STREAMING && st.traversal != PATH_TRAVERSAL_WIDE8) {
     return Status::err(PATH_ERR_UNSUPPORTED, "the streaming approach traces the 8-wide BVH only");
@@ -438,7 +483,6 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   if (!sf.good()) {
     return sf;
   }
-  uint64_t h2d = 0;
   if (!rebuilt && st.upload_scene_every_render) {
     Status sr = copy_staged(&h2d);
     if (!sr.good()) {
@@ -537,12 +581,15 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   const size_t pix0 = (size_t)row_lo * x_dim;           // first band pixel
   const size_t n_band = (size_t)(row_hi - row_lo) * x_dim;
 
+  last_params_ = p;
+  last_blocks_ = n_blocks;
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "pre-render sync");
   auto t0 = std::chrono::steady_clock::now();
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
-    Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks, &launches);
+    Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks,
+                              st.time_kernels != 0, &launches);
     if (!sw.good()) {
       return sw;
     }
@@ -630,6 +677,16 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   stats_.num_wide_nodes = (uint32_t)prep_.wide.nodes.size();
   stats_.h2d_bytes = h2d + spec_h2d;
   stats_.d2h_bytes = d2h;
+  if (st.kernel_approach == PATH_KERNEL_STREAMING) {
+    stats_.trace_launches = trace_launches_;
+    double tms = 0.0;
+    for (uint32_t i = 0; i < trace_timed_; ++i) {
+      float e = 0.f;
+      PG_TRY_CUDA(cudaEventElapsedTime(&e, trace_ev_[2 * i], trace_ev_[2 * i + 1]), "event");
+      tms += e;
+    }
+    stats_.trace_ms = tms;
+  }
   if (seconds) {
     *seconds = stats_.seconds;
   }
@@ -644,7 +701,10 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
 // wavefront render of the whole image into p.out_rgb / p.out_bgra (see
 // wavefront.cu); the host checks the live-slot count every few iterations
 Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool counting,
-                               uint32_t min_blocks, uint32_t *launches) {
+                               uint32_t min_blocks, bool time_trace, uint32_t *launches,
+                               const AdjointState *adj) {
+  trace_timed_ = 0;
+  trace_launches_ = 0;
   if (num_sms_ == 0) {
     int dev = 0;
     PG_TRY_CUDA(cudaGetDevice(&dev), "device");
@@ -684,6 +744,18 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   w.total_samples = first + total;
   w.sample_rgb = wf_samples_.as<float>();
   w.n_slots = n_slots;
+  const bool grad = adj != nullptr;
+  if (grad) {
+    // replay: the forward pass's per-sample radiance stays in wf_samples_
+    PG_TRY_CUDA(adj_pend_.ensure((size_t)n_slots * 36 + 512), "adjoint slots");
+    unsigned char *pb = adj_pend_.as<unsigned char>();
+    w.d_image = adj->d_image;
+    w.pend_refl = reinterpret_cast<float4 *>(pb);
+    w.pend_nee = reinterpret_cast<float4 *>(pb + a256((size_t)n_slots * 16));
+    w.pend_mat = reinterpret_cast<uint32_t *>(pb + 2 * a256((size_t)n_slots * 16));
+    w.d_params = adj->d_params;
+    PG_TRY_CUDA(cudaMemsetAsync(w.pend_mat, 0xff, (size_t)n_slots * 4, stream_), "adjoint init");
+  }
   // queue heads: n_slots live slots, one extension ray each
   uint32_t *h = wf_host_.as<uint32_t>();
   std::memset(h, 0, 64);
@@ -702,10 +774,19 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   volatile uint32_t *live = h + 12;
   for (uint32_t round = 0;; ++round) {
     for (int k = 0; k < 4; ++k) {
-      PG_TRY_CUDA(launch_wavefront_iteration(w, parity, trace_grid, shade_grid, min_blocks,
-                                             counting, stream_),
-                  "wavefront iteration");
+      if (time_trace) {
+        PG_TRY_CUDA(cudaEventRecord(trace_event(2 * trace_timed_), stream_), "event");
+      }
+      PG_TRY_CUDA(launch_wavefront_trace(w, trace_grid, min_blocks, counting, stream_),
+                  "wavefront trace");
+      if (time_trace) {
+        PG_TRY_CUDA(cudaEventRecord(trace_event(2 * trace_timed_ + 1), stream_), "event");
+        ++trace_timed_;
+      }
+      PG_TRY_CUDA(launch_wavefront_shade(w, parity, shade_grid, stream_, grad),
+                  "wavefront shade");
       *launches += 3;
+      ++trace_launches_;
       parity ^= 1u;
     }
     PG_TRY_CUDA(cudaMemcpyAsync(h + 12, &w.q->active[parity], 4, cudaMemcpyDeviceToHost,
@@ -718,6 +799,9 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
     if (round > 4 * kMaxPathVertices) {
       return Status::err(PATH_ERR_DEVICE_TIMEOUT, "wavefront did not drain");
     }
+  }
+  if (grad) {
+    return Status::ok();
   }
   PG_TRY_CUDA(launch_wavefront_sum(p, w.sample_rgb, n_blocks, stream_), "sample sum");
   *launches += 1;
@@ -785,6 +869,93 @@ Status Renderer::intersect(const float *tris, uint32_t n_tris, const float *rays
   PG_TRY_CUDA(cudaMemcpyAsync(&status, status_.get(), 4, cudaMemcpyDeviceToHost, stream_),
               "status copy");
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "intersect sync");
+  if (status != 0) {
+    return Status::err(PATH_ERR_DEVICE_TIMEOUT,
+                       "kernel reported device status " + std::to_string(status));
+  }
+  return Status::ok();
+}
+
+} // namespace pg
+
+namespace pg {
+
+// Adjoint of the streaming render: a forward render (its per-sample
+// radiance stays resident), then a replay of the same paths with gradient
+// shading; d_params[materials][7] = dLoss/d(reflectance rgb, roughness,
+// emission rgb) for dLoss/d(image) = d_image.
+Status Renderer::render_adjoint(const path_sample_spec &spec, const Scene &scene, uint32_t spp,
+                                const path_settings &st_in, const float *d_image,
+                                bool d_image_on_device, double *d_params, double *seconds) {
+  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE || spec.row_start != 0 || spec.row_end != 0) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the adjoint renders whole square images");
+  }
+  if (d_image == nullptr || d_params == nullptr) {
+    return Status::err(PATH_ERR_ARGUMENT, "null adjoint buffer");
+  }
+  if (st_in.traversal != PATH_TRAVERSAL_WIDE8) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the adjoint replays the streaming render, which "
+                                             "traces the 8-wide BVH");
+  }
+  path_settings st = st_in;
+  st.kernel_approach = PATH_KERNEL_STREAMING;
+  st.count_work = 0;
+  st.time_kernels = 0;
+  const size_t n_pix = (size_t)spec.x_dim * spec.y_dim;
+  auto t0 = std::chrono::steady_clock::now();
+  Status s0 = init();
+  if (!s0.good()) {
+    return s0;
+  }
+  PG_TRY_CUDA(adj_image_.ensure(std::max<size_t>(n_pix, 1) * 12), "adjoint image");
+  path_output o{};
+  o.type = PATH_OUTPUT_FLOAT_RGB;
+  o.data = adj_image_.get();
+  o.on_device = 1;
+  Status sf = render(spec, o, scene, spp, st, nullptr);
+  if (!sf.good()) {
+    return sf;
+  }
+  const float fwd_ms = (float)stats_.kernel_ms;
+  const size_t n_mat = scene.materials.size();
+  PG_TRY_CUDA(adj_params_.ensure(std::max<size_t>(n_mat, 1) * 7 * 8), "adjoint params");
+  PG_TRY_CUDA(cudaMemsetAsync(adj_params_.get(), 0, std::max<size_t>(n_mat, 1) * 7 * 8, stream_),
+              "adjoint params");
+  const float *dimg = d_image;
+  if (!d_image_on_device) {
+    PG_TRY_CUDA(adj_dimage_.upload(d_image, n_pix * 12, stream_), "adjoint image upload");
+    dimg = adj_dimage_.as<const float>();
+  }
+  AdjointState adj;
+  adj.d_image = dimg;
+  adj.d_params = adj_params_.as<double>();
+  PG_TRY_CUDA(cudaMemsetAsync(status_.get(), 0, 4, stream_), "status reset");
+  PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
+  uint32_t launches = 0;
+  Status sr = run_wavefront(last_params_, last_blocks_, false, st.trace_min_blocks, false,
+                            &launches, &adj);
+  if (!sr.good()) {
+    return sr;
+  }
+  PG_TRY_CUDA(cudaEventRecord(ev_stop_, stream_), "event");
+  PG_TRY_CUDA(cudaMemcpyAsync(d_params, adj_params_.get(), n_mat * 7 * 8,
+                              cudaMemcpyDeviceToHost, stream_),
+              "gradient copy");
+  uint32_t status = 0;
+  PG_TRY_CUDA(cudaMemcpyAsync(&status, status_.get(), 4, cudaMemcpyDeviceToHost, stream_),
+              "status copy");
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "adjoint sync");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev_start_, ev_stop_);
+  stats_.kernel_ms = fwd_ms + ms;
+  stats_.trace_ms = ms; // the replay alone
+  stats_.device_status = status;
+  stats_.gpu_launches += launches;
+  stats_.seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (seconds) {
+    *seconds = stats_.seconds;
+  }
   if (status != 0) {
     return Status::err(PATH_ERR_DEVICE_TIMEOUT,
                        "kernel reported device status " + std::to_string(status));

@@ -13,6 +13,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -66,13 +67,40 @@ Status cuda_status(cudaError_t e, const char *what);
 
 // host copies of the scene's device arrays (kept for tests and reuse)
 struct PreparedScene {
-  uint64_t scene_id = 0, scene_version = 0;
+  uint64_t scene_id = 0, scene_version = 0, material_version = 0;
   SBVHSettings sbvh;
   bool valid = false;
   BinaryBVH bvh;
   WideBVH wide;
   std::vector<uint32_t> orig_to_bvh; // inverse of bvh.permutation
   uint32_t n_tris = 0, n_lights = 0;
+  double build_seconds = 0.0;
+};
+
+// device form of a material (UnionBSDF parameters + precomputed values)
+DevMaterial to_dev(const path_material &m);
+// triangle as (v0, e1 = v1 - v0, e2 = v2 - v0) in 12 floats; extra_bits in
+// float 10
+void put_tri(float *dst, f3 v0, f3 v1, f3 v2, uint32_t extra_bits);
+// settings every render accepts (enum ranges, supported RNG, bounds)
+Status check_settings(const path_settings &s);
+
+// one image of a batched render (path_batch_item)
+struct BatchItem {
+  const Scene *scene;
+  uint32_t x_dim, y_dim, spp;
+  float f2w[12];
+  path_output output;
+};
+
+// geometry of a batch's scenes, concatenated on the device
+struct PreparedBatch {
+  bool valid = false;
+  std::vector<std::array<uint64_t, 3>> key; // (scene id, version, material version)
+  SBVHSettings sbvh;
+  std::vector<uint32_t> root, light_off, n_lights, n_tris;
+  uint32_t n_wide_nodes = 0;
+  uint64_t total_tris = 0;
   double build_seconds = 0.0;
 };
 
@@ -88,6 +116,15 @@ public:
                    uint32_t n_rays, const path_settings &settings, int32_t *idx,
                    float *t);
   const path_render_stats &stats() const { return stats_; }
+  // adjoint of the streaming render: parameter gradients for dLoss/dImage
+  Status render_adjoint(const path_sample_spec &spec, const Scene &scene, uint32_t spp,
+                        const path_settings &settings, const float *d_image,
+                        bool d_image_on_device, double *d_params, double *seconds);
+  // batched render and its launch-shape autotuner (defined in batch.cpp)
+  Status render_batch(const std::vector<BatchItem> &items, const path_settings &settings,
+                      const path_batch_tuning *tuning, double *seconds);
+  Status autotune_batch(const std::vector<BatchItem> &items, const path_settings &settings,
+                        uint64_t sample_budget, path_batch_tuning *out);
   // render that allocates nothing; scratch is device memory the caller owns
   // (defined in noalloc.cu)
   Status render_noalloc(const path_sample_spec &spec, const path_output &output,
@@ -100,6 +137,8 @@ private:
                        const SBVHSettings &sbvh, bool force);
   Status upload_geometry(const FlatScene &flat, const std::vector<path_material> &mats);
   Status copy_staged(uint64_t *bytes);
+  void stage_materials(const FlatScene &flat, const std::vector<path_material> &mats);
+  Status refresh_materials(const Scene &scene, uint64_t *bytes);
   Status prepare_sobol(uint32_t dim_bound, uint32_t count);
   void fill_params(RenderParams &p) const;
   Status traversal_fits(const path_settings &st) const;
@@ -107,6 +146,8 @@ private:
   bool initialised_ = false;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
+  std::vector<cudaEvent_t> trace_ev_; // event pairs around streaming trace launches
+  uint32_t trace_timed_ = 0, trace_launches_ = 0;
   PreparedScene prep_;
   DeviceBuffer tris_, tri_data_, bin_nodes_, extra_, wide_nodes_, wide_tris_,
       materials_, light_tris_, light_cdf_, perm_;
@@ -117,12 +158,30 @@ private:
   uint32_t sobol_bound_ = 0, sobol_count_ = 0;
   DeviceBuffer out_a_, out_b_, bgra_, status_, counters_, rays_, idxs_;
   // wavefront state
+  struct AdjointState {
+    const float *d_image;
+    double *d_params;
+  };
   Status run_wavefront(const RenderParams &p, uint32_t n_blocks, bool counting,
-                       uint32_t min_blocks, uint32_t *launches);
+                       uint32_t min_blocks, bool time_trace, uint32_t *launches,
+                       const AdjointState *adj = nullptr);
+  RenderParams last_params_{};
+  uint32_t last_blocks_ = 0;
+  DeviceBuffer adj_image_, adj_dimage_, adj_params_, adj_pend_;
+  cudaEvent_t trace_event(size_t i);
   DeviceBuffer wf_slots_, wf_queues_, wf_samples_;
   PinnedBuffer wf_host_;
   int num_sms_ = 0;
   path_render_stats stats_{};
+  // batched render
+  Status check_batch(const std::vector<BatchItem> &items, const path_settings &st) const;
+  Status prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb);
+  Status run_batch(const std::vector<BatchItem> &items, const path_settings &st,
+                   const path_batch_tuning &tu, uint64_t sample_limit, bool with_images,
+                   float *kernel_ms, uint32_t *launches);
+  PreparedBatch batch_;
+  DeviceBuffer b_wnodes_, b_wtris_, b_tris_, b_data_, b_mats_, b_lights_, b_cdf_, b_scenes_,
+      b_part_a_, b_part_b_, b_bgra_;
 };
 
 } // namespace pg

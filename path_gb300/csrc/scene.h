@@ -27,7 +27,8 @@ struct Scene {
   std::vector<uint32_t> instance_mesh;
   std::vector<uint32_t> clusters; // [c][3] material, start, end
   std::vector<path_material> materials;
-  uint64_t version = 0;
+  uint64_t version = 0;          // geometry (and material list) edits
+  uint64_t material_version = 0; // in-place material parameter edits
   uint64_t id = 0;
 
   uint32_t n_tris() const { return (uint32_t)tri_material.size(); }

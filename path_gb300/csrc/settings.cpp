@@ -382,7 +382,10 @@ bool settings_from_yaml_text(const std::string &text, path_settings &s,
         return false;
       }
     }
-    if (!read_u32(get(g, "persistent_ctas_per_sm"), s.persistent_ctas_per_sm, err)) {
+    if (!read_u32(get(g, "persistent_ctas_per_sm"), s.persistent_ctas_per_sm, err) ||
+        !read_u32(get(g, "trace_min_blocks"), s.trace_min_blocks, err) ||
+        !read_bool(get(g, "count_work"), s.count_work, err) ||
+        !read_bool(get(g, "time_kernels"), s.time_kernels, err)) {
       return false;
     }
   }

@@ -42,36 +42,72 @@ __device__ __forceinline__ Hit unpack_hit(uint2 v) {
   return h;
 }
 
-// the pixel and sample index of a linear sample id (pixel-major order)
-__device__ __forceinline__ void sample_coords(const RenderParams &P, unsigned long long id,
-                                              uint32_t &x, uint32_t &y, uint32_t &s) {
-  unsigned long long pixel = id / P.spp;
-  s = (uint32_t)(id - pixel * P.spp);
-  x = (uint32_t)(pixel % P.x_dim);
-  y = (uint32_t)(pixel / P.x_dim);
+// the pixel and sample index of a scene-local sample id (pixel-major order)
+__device__ __forceinline__ void sample_coords(unsigned long long id, uint32_t spp,
+                                              uint32_t x_dim, uint32_t &x, uint32_t &y,
+                                              uint32_t &s) {
+  unsigned long long pixel = id / spp;
+  s = (uint32_t)(id - pixel * spp);
+  x = (uint32_t)(pixel % x_dim);
+  y = (uint32_t)(pixel / x_dim);
 }
 
+// the scene of a global sample id in a batched render: the last scene whose
+// first sample is at or below it
+__device__ __forceinline__ uint32_t scene_of(const WaveParams &W, unsigned long long id) {
+  uint32_t lo = 0, hi = W.n_scenes;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (W.scenes[mid].first_sample <= id) {
+      lo = mid;
+    } else {
+      hi = mid;
+    }
+  }
+  return lo;
+}
+
+// Slot state: o (xyz, light target), d and ld (xyz, scene root node bits in
+// w, read by the trace kernel), multipliers, radiance so far, and
+// (id low word, id bits 32-39 | scene << 8, RNG dimension, iters | flags << 24).
 __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
-                                           const PathState &s, unsigned long long id) {
+                                           const PathState &s, unsigned long long id,
+                                           uint32_t scene, uint32_t root) {
   W.o[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.light_target);
-  W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, 0.f);
-  W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, 0.f);
+  W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, __uint_as_float(root));
+  W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, __uint_as_float(root));
   W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
   W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
   W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
   uint32_t flags = (s.has_next ? kFlagNext : 0u) | (s.has_light ? kFlagLight : 0u) |
                    (s.count_emission ? kFlagEmission : 0u);
-  W.state[slot] = make_uint4((uint32_t)id, (uint32_t)(id >> 32), s.rng.dim,
-                             s.iters | (flags << 24));
+  W.state[slot] = make_uint4((uint32_t)id, ((uint32_t)(id >> 32) & 0xffu) | (scene << 8),
+                             s.rng.dim, s.iters | (flags << 24));
+}
+
+// the lights of a slot's scene
+__device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t scene) {
+  if (W.scenes == nullptr) {
+    return lights_of(W.P);
+  }
+  const BatchScene &b = W.scenes[scene];
+  LightSet l;
+  l.tris = W.P.light_tris + 3 * (size_t)b.light_off;
+  l.cdf = W.P.light_cdf + b.light_off;
+  l.n = b.n_lights;
+  return l;
 }
 
 __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
-                                                        PathState &s) {
+                                                        PathState &s, uint32_t &scene,
+                                                        uint32_t &root) {
   const RenderParams &P = W.P;
   float4 o = W.o[slot], d = W.d[slot], ld = W.ld[slot];
   float4 m = W.mult[slot], lm = W.lmult[slot], t = W.total[slot];
   uint4 st = W.state[slot];
-  unsigned long long id = (unsigned long long)st.x | ((unsigned long long)st.y << 32);
+  unsigned long long id = (unsigned long long)st.x | ((unsigned long long)(st.y & 0xffu) << 32);
+  scene = st.y >> 8;
+  root = __float_as_uint(d.w);
   s.o = mk(o.x, o.y, o.z);
   s.light_target = o.w;
   s.d = mk(d.x, d.y, d.z);
@@ -84,8 +120,13 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
   s.has_next = (flags & kFlagNext) != 0;
   s.has_light = (flags & kFlagLight) != 0;
   s.count_emission = (flags & kFlagEmission) != 0;
-  uint32_t x, y, smp;
-  sample_coords(P, id, x, y, smp);
+  unsigned long long local = id;
+  uint32_t spp = P.spp;
+  if (W.scenes != nullptr) {
+    local = id - W.scenes[scene].first_sample;
+    spp = W.scenes[scene].spp;
+  }
+  const uint32_t smp = (uint32_t)(local % spp);
   s.rng.row = P.sobol + (size_t)smp * P.dim_bound;
   s.rng.bound = P.dim_bound;
   s.rng.dim = st.z;
@@ -94,11 +135,23 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
 
 __device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
                                              unsigned long long id) {
-  uint32_t x, y, smp;
-  sample_coords(W.P, id, x, y, smp);
+  uint32_t x, y, smp, scene = 0, root = 0;
   PathState s;
-  path_begin(W.P, smp, x, y, s);
-  store_path(W, slot, s, id);
+  if (W.scenes == nullptr) {
+    sample_coords(id, W.P.spp, W.P.x_dim, x, y, smp);
+    path_begin(W.P, smp, x, y, s);
+  } else {
+    scene = scene_of(W, id);
+    const BatchScene &b = W.scenes[scene];
+    sample_coords(id - b.first_sample, b.spp, b.x_dim, x, y, smp);
+    Camera cam;
+    cam.f2w = b.f2w;
+    cam.x_dim = b.x_dim;
+    cam.y_dim = b.y_dim;
+    path_begin_cam(W.P, cam, smp, x, y, s);
+    root = b.root;
+  }
+  store_path(W, slot, s, id, scene, root);
 }
 
 // position of set bit r (0-based) of m; m has more than r set bits
@@ -195,6 +248,9 @@ __device__ __forceinline__ void warp_triangles(const RenderParams &P, WideWalk &
   if (mine != ~0ull) {
     const uint32_t lo = (uint32_t)mine;
     fold_min(w.best, __uint_as_float((uint32_t)(mine >> 32)), (lo & 1u) != 0, lo >> 1);
+    if (shadow_settled(w)) {
+      w.done = true;
+    }
   }
 }
 
@@ -245,7 +301,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
           ray r;
           r.o = mk(o.x, o.y, o.z);
           r.d = mk(d.x, d.y, d.z);
-          wide_begin(W.P, w, r, light ? light_bound(o.w) : PG_INF);
+          wide_begin(W.P, w, r, light ? light_bound(o.w) : PG_INF, light ? o.w : -PG_INF,
+                     __float_as_uint(d.w));
           have = true;
           if (kCount) {
             ++cnt.rays;
@@ -295,6 +352,44 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool pred, ui
   return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
+constexpr uint32_t kNoMaterial = 0xffffffffu;
+
+// Adds v[0..N) to d_params[mat][off..off+N) for every lane's material: lanes
+// of one material are summed across the warp first (shuffle butterfly),
+// then one FP64 atomic per value.  All 32 lanes call this; kNoMaterial
+// lanes add nothing.
+template <int N>
+__device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float (&v)[N],
+                                          int off, uint32_t lane) {
+  uint32_t todo = __ballot_sync(kFull, mat != kNoMaterial);
+  while (todo != 0) {
+    const uint32_t leader = __ffs(todo) - 1;
+    const uint32_t m = __shfl_sync(kFull, mat, leader);
+    const bool mine = mat == m && ((todo >> lane) & 1u) != 0;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      float x = mine ? v[k] : 0.f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(kFull, x, o);
+      }
+      if (lane == leader) {
+        atomicAdd(out + (size_t)m * 7 + off + k, (double)x);
+      }
+    }
+    todo &= ~__ballot_sync(kFull, mine);
+  }
+}
+
+// One rendering_equation_iteration per live slot.  With kGrad the same
+// iteration is replayed for the adjoint (path replay: same Sobol draws,
+// same rays) and its derivative terms are accumulated: the forward
+// radiance L of the sample (sample_rgb) minus what has been gathered gives
+// the radiance that flowed through each vertex's continuation, which times
+// d log f / d(parameter) of that vertex is its parameter gradient; the
+// light sample adds its own term, and emission terms are linear.  Sampling
+// densities and the light table are held fixed (detached estimator).
+template <bool kGrad>
 __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t parity) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->active[parity];
@@ -313,25 +408,104 @@ __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t p
     const bool valid = i < count;
     uint32_t slot = 0;
     bool live = false, finished = false, want_next = false, want_light = false;
+    uint32_t gm_vertex = kNoMaterial, gm_light = kNoMaterial, gm_emit = kNoMaterial;
+    float gv_vertex[4] = {0.f, 0.f, 0.f, 0.f};
+    float gv_light[3] = {0.f, 0.f, 0.f}, gv_emit[3] = {0.f, 0.f, 0.f};
     if (valid) {
       slot = in[i];
       PathState s;
-      unsigned long long id = load_path(W, slot, s);
+      uint32_t scene, root;
+      unsigned long long id = load_path(W, slot, s, scene, root);
       Hit lh = s.has_light ? unpack_hit(W.hit_light[slot]) : no_hit();
       Hit nh = s.has_next ? unpack_hit(W.hit_ext[slot]) : no_hit();
-      bool cont = path_continues(W.P, s, path_step(W.P, s, lh, nh));
-      if (cont) {
-        store_path(W, slot, s, id);
-        live = true;
-        want_next = s.has_next;
-        want_light = s.has_light;
+      if (!kGrad) {
+        bool cont = path_continues(W.P, s, path_step(W.P, scene_lights(W, scene), s, lh, nh));
+        if (cont) {
+          store_path(W, slot, s, id, scene, root);
+          live = true;
+          want_next = s.has_next;
+          want_light = s.has_light;
+        } else {
+          float *dst = W.sample_rgb + 3 * (id - W.first_sample);
+          dst[0] = s.total.r;
+          dst[1] = s.total.g;
+          dst[2] = s.total.b;
+          finished = true;
+        }
       } else {
-        float *dst = W.sample_rgb + 3 * (id - W.first_sample);
-        dst[0] = s.total.r;
-        dst[1] = s.total.g;
-        dst[2] = s.total.b;
-        finished = true;
+        const RenderParams &P = W.P;
+        const float *lf = W.sample_rgb + 3 * (id - W.first_sample);
+        const rgb l_sample = mkrgb(lf[0], lf[1], lf[2]);
+        const unsigned long long pixel = id / P.spp;
+        const float *gp = W.d_image + 3 * pixel;
+        const float inv_spp = 1.f / (float)P.spp;
+        const rgb g = mkrgb(gp[0] * inv_spp, gp[1] * inv_spp, gp[2] * inv_spp);
+        const rgb beta = s.multiplier, lmult = s.light_mult;
+        StepTrace tr;
+        bool cont = path_continues(P, s, path_step(P, scene_lights(W, scene), s, lh, nh, &tr));
+        const uint32_t pm = W.pend_mat[slot];
+        rgb nee_add = zero_rgb(), emit_add = zero_rgb();
+        if (tr.light_added) {
+          nee_add = emission_of(P.materials + tr.light_mat) * lmult;
+          gm_light = tr.light_mat;
+          gv_light[0] = g.r * lmult.r;
+          gv_light[1] = g.g * lmult.g;
+          gv_light[2] = g.b * lmult.b;
+        }
+        if (tr.emit_added) {
+          emit_add = beta * emission_of(P.materials + tr.mat);
+          gm_emit = tr.mat;
+          gv_emit[0] = g.r * beta.r;
+          gv_emit[1] = g.g * beta.g;
+          gv_emit[2] = g.b * beta.b;
+        }
+        if (pm != kNoMaterial) {
+          // radiance through the pending vertex's continuation, and its
+          // light sample's contribution (resolved by this step)
+          const float4 pr = W.pend_refl[slot], pn = W.pend_nee[slot];
+          const rgb rest = l_sample - (s.total - emit_add);
+          gm_vertex = pm;
+          gv_vertex[0] = g.r * (rest.r * pr.x + nee_add.r * pn.x);
+          gv_vertex[1] = g.g * (rest.g * pr.y + nee_add.g * pn.y);
+          gv_vertex[2] = g.b * (rest.b * pr.z + nee_add.b * pn.z);
+          gv_vertex[3] = (g.r * (rest.r * pr.w + nee_add.r * pn.w) +
+                          g.g * (rest.g * pr.w + nee_add.g * pn.w)) +
+                         g.b * (rest.b * pr.w + nee_add.b * pn.w);
+        }
+        uint32_t npm = kNoMaterial;
+        if (cont && tr.hit) {
+          const Mat mat = load_mat(P.materials + tr.mat);
+          rgb r1 = zero_rgb(), r2 = zero_rgb();
+          float a1 = 0.f, a2 = 0.f;
+          bool any = false;
+          if (tr.continuous && s.has_next &&
+              bsdf_log_grad(mat, tr.in, tr.next_dir, tr.normal, r1, a1)) {
+            any = true;
+          }
+          if (tr.nee && bsdf_log_grad(mat, tr.in, tr.nee_dir, tr.normal, r2, a2)) {
+            any = true;
+          }
+          if (any) {
+            npm = tr.mat;
+            W.pend_refl[slot] = make_float4(r1.r, r1.g, r1.b, a1);
+            W.pend_nee[slot] = make_float4(r2.r, r2.g, r2.b, a2);
+          }
+        }
+        W.pend_mat[slot] = npm;
+        if (cont) {
+          store_path(W, slot, s, id, scene, root);
+          live = true;
+          want_next = s.has_next;
+          want_light = s.has_light;
+        } else {
+          finished = true;
+        }
       }
+    }
+    if (kGrad) {
+      warp_grad<4>(W.d_params, gm_vertex, gv_vertex, 0, lane);
+      warp_grad<3>(W.d_params, gm_light, gv_light, 4, lane);
+      warp_grad<3>(W.d_params, gm_emit, gv_emit, 4, lane);
     }
     __syncwarp();
     // finished slots take the next sample index (one atomic per warp)
@@ -346,6 +520,9 @@ __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t p
         unsigned long long id = first + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
         if (id < W.total_samples) {
           begin_sample(W, slot, id);
+          if (kGrad) {
+            W.pend_mat[slot] = kNoMaterial;
+          }
           live = true;
           want_next = true;
           want_light = false;
@@ -429,17 +606,21 @@ int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting) {
   return n;
 }
 
-cudaError_t launch_wavefront_iteration(const WaveParams &w, uint32_t parity,
-                                       uint32_t trace_grid, uint32_t shade_grid,
-                                       uint32_t min_blocks, bool counting, cudaStream_t s) {
+cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
+                                   uint32_t min_blocks, bool counting, cudaStream_t s) {
   void *k = counting ? trace_kernel<true>(min_blocks) : trace_kernel<false>(min_blocks);
   void *args[] = {const_cast<WaveParams *>(&w)};
-  cudaError_t e = cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args, 0, s);
-  if (e != cudaSuccess) {
-    return e;
-  }
+  return cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args, 0, s);
+}
+
+cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_t shade_grid,
+                                   cudaStream_t s, bool grad) {
   dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
-  dev::k_wf_shade<<<shade_grid, 256, 0, s>>>(w, parity);
+  if (grad) {
+    dev::k_wf_shade<true><<<shade_grid, 256, 0, s>>>(w, parity);
+  } else {
+    dev::k_wf_shade<false><<<shade_grid, 256, 0, s>>>(w, parity);
+  }
   return cudaGetLastError();
 }
 

@@ -255,3 +255,91 @@ def path_settings(max_depth, traversal="wide"):
     s.back_cull_emission = 1
     s.traversal = 1 if traversal == "wide" else 0
     return s
+
+
+# ---------------------------------------------------------------------------
+# batched workload
+
+def _sphere_grid(m, radius, centre):
+    """Latitude-longitude sphere with m x m cells (vectorised): positions and
+    analytic normals, outward winding; 2 m (m - 1) triangles."""
+    th = np.linspace(0, np.pi, m + 1)
+    ph = np.linspace(0, 2 * np.pi, m + 1)
+    t, p = np.meshgrid(th, ph, indexing="ij")
+    u = np.stack([np.sin(t) * np.cos(p), np.cos(t), np.sin(t) * np.sin(p)], -1)
+    a, b = u[:-1, :-1], u[:-1, 1:]
+    c, d = u[1:, 1:], u[1:, :-1]
+    upper = np.stack([a, b, d], 2)[1:].reshape(-1, 3, 3)        # skip the north cap row
+    lower = np.stack([b, c, d], 2)[:-1].reshape(-1, 3, 3)       # skip the south cap row
+    n = np.concatenate([upper, lower])
+    fn = np.cross(n[:, 1] - n[:, 0], n[:, 2] - n[:, 0])
+    flip = np.einsum("ij,ij->i", fn, n.mean(axis=1)) < 0
+    n[flip] = n[flip][:, ::-1]
+    pos = n * radius + np.asarray(centre)
+    return pos.reshape(-1, 9).astype(np.float32), n.reshape(-1, 9).astype(np.float32)
+
+
+def batch_scene(rng):
+    """One scene of the batched workload: the room, one ceiling light with
+    emission U[5, 20], and 1-40 random boxes and tessellated spheres whose
+    triangles total about T (log-uniform in [50k, 200k]); each object's
+    material is diffuse, GGX (roughness U[0.05, 0.8]) or dielectric (IOR
+    U[1.3, 1.7]) with equal probability.  Returns (scene, x_dim, y_dim, spp)
+    with a square resolution from {64, 128, 192, 256} and spp log-uniform in
+    [8, 128]."""
+    scene = api.Scene()
+    white = scene.add_material(api.material("Diffuse", diffuse=WHITE))
+    red = scene.add_material(api.material("Diffuse", diffuse=RED))
+    green = scene.add_material(api.material("Diffuse", diffuse=GREEN))
+    e = float(rng.uniform(5, 20))
+    light = scene.add_material(api.material("Diffuse", diffuse=(0.78, 0.78, 0.78),
+                                            emission=(e, e, e)))
+    walls, light_tris = room_triangles()
+    tris, mats = [], []
+    for name, ts in walls.items():
+        m = red if name == "left" else green if name == "right" else white
+        tris += ts
+        mats += [m] * len(ts)
+    tris += light_tris
+    mats += [light] * len(light_tris)
+    scene.add_mesh(np.stack(tris).reshape(-1, 9), np.array(mats, np.uint32))
+
+    def random_material():
+        k = rng.integers(3)
+        if k == 0:
+            return scene.add_material(api.material("Diffuse",
+                                                   diffuse=tuple(rng.uniform(0.1, 0.9, 3))))
+        if k == 1:
+            return scene.add_material(api.material("GGX", specular=(0.04, 0.04, 0.04),
+                                                   roughness=float(rng.uniform(0.05, 0.8))))
+        return scene.add_material(api.material("DielectricRefractive", specular=(1, 1, 1),
+                                               ior=float(rng.uniform(1.3, 1.7))))
+
+    target = math.exp(rng.uniform(math.log(50e3), math.log(200e3)))
+    n_obj = int(rng.integers(1, 41))
+    is_sphere = rng.random(n_obj) < 0.5
+    is_sphere[0] = True  # at least one sphere carries the triangle budget
+    n_sph = int(is_sphere.sum())
+    budget = max(target - 12 * (n_obj - n_sph), 2 * 4 * 3 * n_sph)
+    m = max(4, int(round(math.sqrt(budget / (2 * n_sph)))))
+    for k in range(n_obj):
+        mat = random_material()
+        if is_sphere[k]:
+            r = float(rng.uniform(0.08, 0.3))
+            c = (rng.uniform(-1 + r, 1 - r), rng.uniform(-1 + r, 0.6 - r), rng.uniform(-1 + r, 0.9))
+            t, nrm = _sphere_grid(m, r, c)
+            scene.add_mesh(t, np.full(len(t), mat, np.uint32), normals=nrm)
+        else:
+            w, h, d = rng.uniform(0.1, 0.5, 3)
+            b = _box(w, h, d, float(rng.uniform(0, 90)),
+                     (rng.uniform(-0.8, 0.8), rng.uniform(-0.8, 0.8)))
+            scene.add_mesh(b.reshape(-1, 9), np.full(len(b), mat, np.uint32))
+    res = int(rng.choice([64, 128, 192, 256]))
+    spp = int(round(math.exp(rng.uniform(math.log(8), math.log(128)))))
+    return scene, res, res, spp
+
+
+def batch_scenes(n=256, seed=0):
+    """The batched workload: n seeded scenes (see batch_scene), depth 6."""
+    rng = np.random.default_rng(seed)
+    return [batch_scene(rng) for _ in range(n)]
