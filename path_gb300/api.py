@@ -117,6 +117,10 @@ class Scene:
             self._h, _fptr(tris), None if nrm is None else _fptr(nrm), _uptr(mats),
             tris.shape[0], None if xf is None else _fptr(xf)))
 
+    def set_material(self, idx, m):
+        """Replace material idx in place (no BVH rebuild on the next render)."""
+        capi.check(capi.load().path_scene_set_material(self._h, int(idx), ctypes.byref(m)))
+
     def sizes(self):
         s = (ctypes.c_uint32 * 5)()
         capi.check(capi.load().path_scene_sizes(self._h, s))
@@ -279,6 +283,30 @@ class Renderer:
                                            ctypes.byref(settings.raw), int(show_progress),
                                            ctypes.byref(secs)))
         return secs.value
+
+    def render_adjoint(self, sample_spec, scene, samples_per, settings, d_image):
+        """path_render_adjoint: dLoss/d(material parameters) as float64
+        [materials, 7] (reflectance rgb, roughness, emission rgb) for
+        dLoss/d(image) = d_image ([H, W, 3] float32, numpy or torch)."""
+        n_mat = scene.sizes()["materials"]
+        out = np.zeros((max(n_mat, 1), 7), np.float64)
+        spec = sample_spec.to_c()
+        secs = ctypes.c_double()
+        if hasattr(d_image, "data_ptr"):
+            d_image = d_image.contiguous()
+            ptr = ctypes.cast(d_image.data_ptr(), ctypes.POINTER(ctypes.c_float))
+            on_dev = 1 if d_image.is_cuda else 0
+            keep = d_image
+        else:
+            keep = np.ascontiguousarray(d_image, np.float32)
+            ptr = _fptr(keep)
+            on_dev = 0
+        capi.check(capi.load().path_render_adjoint(
+            self._h, ctypes.byref(spec), scene.handle, int(samples_per),
+            ctypes.byref(settings.raw), ptr, on_dev,
+            out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(secs)))
+        del keep
+        return out[:n_mat]
 
     @staticmethod
     def _output_c(output):

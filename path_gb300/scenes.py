@@ -343,3 +343,90 @@ def batch_scenes(n=256, seed=0):
     """The batched workload: n seeded scenes (see batch_scene), depth 6."""
     rng = np.random.default_rng(seed)
     return [batch_scene(rng) for _ in range(n)]
+
+
+# ---------------------------------------------------------------------------
+# differentiation workload
+
+def _grid_quad(a, b, c, d, n):
+    """Quad a-b-c-d as an n x n grid of quads: (triangles [2n^2, 9],
+    cell centres [2n^2, 3])."""
+    a, b, c, d = (np.asarray(v, np.float64) for v in (a, b, c, d))
+    tris, cen = [], []
+    for i in range(n):
+        for j in range(n):
+            u0, u1, v0, v1 = i / n, (i + 1) / n, j / n, (j + 1) / n
+
+            def at(u, v):
+                return (1 - u) * (1 - v) * a + u * (1 - v) * b + u * v * c + (1 - u) * v * d
+            p = [at(u0, v0), at(u1, v0), at(u1, v1), at(u0, v1)]
+            for t in ([p[0], p[1], p[2]], [p[0], p[2], p[3]]):
+                tris.append(np.concatenate(t))
+                cen.append(np.mean(t, axis=0))
+    return np.array(tris, np.float32), np.array(cen)
+
+
+def patch_cornell(seed=1, n_materials=16):
+    """The Cornell geometry with walls and boxes split into patches of
+    n_materials materials: floor, ceiling, left and right walls in two
+    halves, the back wall in three strips, each box's top and sides, and the
+    ceiling light.  Patch materials alternate Diffuse and GGX with albedo /
+    F0 U[0.1, 0.9] and roughness U[0.1, 0.7]; the light emits 15.  Returns
+    (scene, materials as capi.PathMaterial list)."""
+    assert n_materials == 16
+    rng = np.random.default_rng(seed)
+    scene = api.Scene()
+    mats = []
+
+    def add(kind, **kw):
+        m = api.material(kind, **kw)
+        mats.append(m)
+        return scene.add_material(m)
+
+    patch_ids = []
+    for k in range(15):
+        refl = tuple(float(v) for v in rng.uniform(0.1, 0.9, 3))
+        if k % 2 == 0:
+            patch_ids.append(add("Diffuse", diffuse=refl))
+        else:
+            patch_ids.append(add("GGX", specular=refl, roughness=float(rng.uniform(0.1, 0.7))))
+    light = add("Diffuse", diffuse=(0.78, 0.78, 0.78), emission=LIGHT_EMISSION)
+    p = lambda x, y, z: (x, y, z)  # noqa: E731
+    walls = [
+        (p(-1, -1, -1), p(-1, -1, 1), p(1, -1, 1), p(1, -1, -1), 0, 2),   # floor: x halves
+        (p(-1, 1, -1), p(1, 1, -1), p(1, 1, 1), p(-1, 1, 1), 2, 2),       # ceiling
+        (p(-1, -1, -1), p(1, -1, -1), p(1, 1, -1), p(-1, 1, -1), 4, 3),   # back: 3 strips
+        (p(-1, -1, -1), p(-1, 1, -1), p(-1, 1, 1), p(-1, -1, 1), 7, 2),   # left: z halves
+        (p(1, -1, -1), p(1, -1, 1), p(1, 1, 1), p(1, 1, -1), 9, 2),       # right
+    ]
+    for a, b, c, d, first, parts in walls:
+        tris, cen = _grid_quad(a, b, c, d, 6)
+        axis = 2 if first in (7, 9) else 0
+        x = (cen[:, axis] + 1.0) / 2.0
+        idx = np.minimum((x * parts).astype(int), parts - 1)
+        scene.add_mesh(tris, np.array([patch_ids[first + i] for i in idx], np.uint32))
+    for (w, h, d, ang, cxz), first in (((0.6, 0.6, 0.6, -18.0, (0.33, 0.37)), 11),
+                                       ((0.6, 1.2, 0.6, 18.0, (-0.33, -0.3)), 13)):
+        b = _box(w, h, d, ang, cxz)
+        # faces: bottom, top, then four sides (two triangles each)
+        m = [patch_ids[first]] * 2 + [patch_ids[first + 1]] * 2 + [patch_ids[first]] * 8
+        scene.add_mesh(b.reshape(-1, 9), np.array(m, np.uint32))
+    _, light_tris = room_triangles()
+    scene.add_mesh(np.stack(light_tris).reshape(-1, 9), np.full(2, light, np.uint32))
+    return scene, mats
+
+
+def perturbed_params(params, materials, seed=2, scale=0.1):
+    """Target parameters: each active parameter scaled by U[1 - scale,
+    1 + scale] (roughness and reflectance kept in [0.05, 0.95])."""
+    from . import capi
+    rng = np.random.default_rng(seed)
+    out = np.array(params, np.float64)
+    for i, m in enumerate(materials):
+        f = rng.uniform(1 - scale, 1 + scale, 7)
+        if m.type in (capi.BSDF["Diffuse"], capi.BSDF["GGX"]):
+            out[i, 0:3] = np.clip(out[i, 0:3] * f[0:3], 0.05, 0.95)
+        if m.type == capi.BSDF["GGX"]:
+            out[i, 3] = np.clip(out[i, 3] * f[3], 0.05, 0.95)
+        out[i, 4:7] = out[i, 4:7] * f[4:7]
+    return out
