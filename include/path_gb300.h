@@ -271,6 +271,12 @@ path_status path_render(path_renderer *renderer, uint32_t exec_model,
 path_status path_renderer_stats(const path_renderer *renderer,
                                 path_render_stats *out);
 
+/* tensor-core self-test (GB300 addition): d [128][n] = a [128][k] . b [n][k]^T
+ * with BF16 a, b (raw 16-bit patterns, row-major) and FP32 d, computed by
+ * one tcgen05 MMA tile; k, n multiples of 16 in [16, 128]; host buffers */
+path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k, uint32_t n,
+                               float *d);
+
 /* ---- adjoint (GB300 addition; the reference has no derivatives) ---- */
 /* Gradients of a loss of the rendered image with respect to each material's
  * parameters, by path replay: a streaming forward render of (spec, scene,

@@ -469,3 +469,27 @@ def work_division(wd_settings, samples_per, x_dim, y_dim):
              "sample_block_size", "x_block_size", "y_block_size", "num_sample_blocks",
              "num_x_blocks", "num_y_blocks", "x_dim", "y_dim"]
     return dict(zip(names, list(out)))
+
+
+def bf16_bits(x):
+    """float32 array -> BF16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return u.astype(np.uint16)
+
+
+def bf16_value(bits):
+    return (np.asarray(bits, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def debug_tc_gemm(a, b):
+    """One tcgen05 tile: a [128][k], b [n][k] (rounded to BF16) -> a . b^T in
+    FP32, and the BF16-rounded operands."""
+    ab = bf16_bits(a)
+    bb = bf16_bits(b)
+    k, n = ab.shape[1], bb.shape[0]
+    d = np.zeros((128, n), np.float32)
+    p16 = ctypes.POINTER(ctypes.c_uint16)
+    capi.check(capi.load().path_debug_tc_gemm(ab.ctypes.data_as(p16), bb.ctypes.data_as(p16),
+                                              k, n, _fptr(d)))
+    return d, bf16_value(ab), bf16_value(bb)

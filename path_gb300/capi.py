@@ -128,6 +128,8 @@ SIGNATURES = {
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),
+    "path_debug_tc_gemm": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint16),
+                                          ctypes.POINTER(ctypes.c_uint16), c_u32, c_u32, _PF]),
     "path_render_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), _P, c_u32,
                                            ctypes.POINTER(PathSettings), _PF, c_u32,
                                            ctypes.POINTER(ctypes.c_double),

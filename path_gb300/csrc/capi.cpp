@@ -300,6 +300,37 @@ path_status path_render(path_renderer *renderer, uint32_t exec_model,
   });
 }
 
+path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k, uint32_t n,
+                               float *d) {
+  if (!a || !b || !d) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  if (k % 16 != 0 || n % 16 != 0 || k < 16 || n < 16 || k > 128 || n > 128) {
+    return fail(PATH_ERR_ARGUMENT, "k and n must be multiples of 16 in [16, 128]");
+  }
+  return guarded([&]() -> path_status {
+    pg::DeviceBuffer da, db, dd, derr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaSuccess;
+    uint32_t err = 0;
+    if ((e = da.upload(a, (size_t)128 * k * 2, s)) != cudaSuccess ||
+        (e = db.upload(b, (size_t)n * k * 2, s)) != cudaSuccess ||
+        (e = dd.ensure((size_t)128 * n * 4)) != cudaSuccess ||
+        (e = derr.upload(&err, 4, s)) != cudaSuccess ||
+        (e = pg::launch_tc_gemm(da.get(), db.get(), dd.as<float>(), k, n, derr.as<uint32_t>(),
+                                s)) != cudaSuccess ||
+        (e = cudaMemcpy(d, dd.get(), (size_t)128 * n * 4, cudaMemcpyDeviceToHost)) !=
+            cudaSuccess ||
+        (e = cudaMemcpy(&err, derr.get(), 4, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+      return from(pg::cuda_status(e, "tensor-core test"));
+    }
+    if (err != 0) {
+      return fail(PATH_ERR_DEVICE_TIMEOUT, "tensor-core MMA did not complete");
+    }
+    return PATH_OK;
+  });
+}
+
 path_status path_render_adjoint(path_renderer *renderer, const path_sample_spec *sample_spec,
                                 const path_scene *scene, uint32_t samples_per,
                                 const path_settings *settings, const float *d_image,

@@ -156,4 +156,9 @@ cudaError_t launch_sobol_curand(const uint32_t *dirs, const uint32_t *scramble,
 cudaError_t launch_pmath(uint32_t fn, const float *x, const float *y,
                          float *out, uint32_t n, cudaStream_t s);
 
+// tensor-core self-test: D [128][n] = A [128][k] . B [n][k]^T (BF16 in, FP32
+// out), one CTA; err set when the MMA did not complete
+cudaError_t launch_tc_gemm(const void *a, const void *b, float *d, uint32_t k_dim,
+                           uint32_t n_dim, uint32_t *err, cudaStream_t s);
+
 } // namespace pg
