@@ -295,6 +295,30 @@ path_status path_render_adjoint(path_renderer *renderer, const path_sample_spec 
                                 uint32_t d_image_on_device, double *d_params,
                                 double *seconds);
 
+/* ---- neural radiance cache (GB300 addition) ----
+ * A multiresolution hash-grid encoding of position (16 levels x 2 features,
+ * 2^19 entries per level) plus direction, normal and albedo feeds a BF16 MLP
+ * (48 -> 64 x5 ReLU -> 3, no biases) run on the tcgen05 tensor cores with
+ * FP32 accumulation; trained online with Adam on a relative L2 loss.
+ * Query records: [n][12] floats (position, direction, normal, albedo);
+ * training records: [n][16] floats (query, target radiance rgb, pad). */
+typedef struct path_cache path_cache;
+path_status path_cache_create(uint32_t seed, float learning_rate, path_cache **out);
+void path_cache_destroy(path_cache *cache);
+/* the scene box the hash grid covers */
+path_status path_cache_set_bounds(path_cache *cache, const float *lo, const float *hi);
+/* radiance [n][3] of n queries (host buffers) */
+path_status path_cache_query(path_cache *cache, const float *queries, uint32_t n, float *out);
+/* one training step on n records (host buffer): with apply_update 0 only the
+ * gradients are computed (path_cache_access reads them); loss = mean
+ * relative L2 loss before the step */
+path_status path_cache_train(path_cache *cache, const float *records, uint32_t n,
+                             uint32_t apply_update, float *loss);
+/* copies weights [20480], table [16][2^19][2], and their gradients to the
+ * host (set = 0) or weights and table from the host (set = 1); NULL skips */
+path_status path_cache_access(path_cache *cache, float *weights, float *table,
+                              float *grad_weights, float *grad_table, uint32_t set);
+
 /* ---- batched render (GB300 addition; the reference renders one scene per
  * call) ---- */
 /* One image of a batch: a scene, its square-image camera, samples per pixel

@@ -493,3 +493,62 @@ def debug_tc_gemm(a, b):
     capi.check(capi.load().path_debug_tc_gemm(ab.ctypes.data_as(p16), bb.ctypes.data_as(p16),
                                               k, n, _fptr(d)))
     return d, bf16_value(ab), bf16_value(bb)
+
+
+class RadianceCache:
+    """Neural radiance cache (path_cache_*): hash-grid encoding + BF16 MLP on
+    the tensor cores, trained online with Adam."""
+
+    N_WEIGHTS = 20480
+    LEVELS, TABLE = 16, 1 << 19
+
+    def __init__(self, seed=1, learning_rate=1e-2):
+        h = ctypes.c_void_p()
+        capi.check(capi.load().path_cache_create(int(seed), float(learning_rate),
+                                                 ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and capi._lib is not None:
+            capi._lib.path_cache_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_bounds(self, lo, hi):
+        lo = np.asarray(lo, np.float32)
+        hi = np.asarray(hi, np.float32)
+        capi.check(capi.load().path_cache_set_bounds(self._h, _fptr(lo), _fptr(hi)))
+
+    def query(self, queries):
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 12)
+        out = np.zeros((q.shape[0], 3), np.float32)
+        capi.check(capi.load().path_cache_query(self._h, _fptr(q), q.shape[0], _fptr(out)))
+        return out
+
+    def train(self, records, update=True):
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, 16)
+        loss = np.zeros(1, np.float32)
+        capi.check(capi.load().path_cache_train(self._h, _fptr(r), r.shape[0], int(update),
+                                                _fptr(loss)))
+        return float(loss[0])
+
+    def get(self, grads=False):
+        w = np.zeros(self.N_WEIGHTS, np.float32)
+        t = np.zeros((self.LEVELS, self.TABLE, 2), np.float32)
+        gw = np.zeros_like(w) if grads else None
+        gt = np.zeros_like(t) if grads else None
+        capi.check(capi.load().path_cache_access(
+            self._h, _fptr(w), _fptr(t), None if gw is None else _fptr(gw),
+            None if gt is None else _fptr(gt), 0))
+        return (w, t, gw, gt) if grads else (w, t)
+
+    def set(self, weights=None, table=None):
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        t = None if table is None else np.ascontiguousarray(table, np.float32)
+        capi.check(capi.load().path_cache_access(self._h, None if w is None else _fptr(w),
+                                                 None if t is None else _fptr(t), None, None,
+                                                 1))

@@ -23,8 +23,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["render.cu", "sobol.cu", "noalloc.cu", "wavefront.cu", "cache.cu"]
-CPP_SOURCES = ["capi.cpp", "renderer.cpp", "batch.cpp", "scene.cpp", "scene_load.cpp",
-               "sbvh.cpp", "wide.cpp", "settings.cpp"]
+CPP_SOURCES = ["capi.cpp", "renderer.cpp", "batch.cpp", "cache_host.cpp", "scene.cpp",
+               "scene_load.cpp", "sbvh.cpp", "wide.cpp", "settings.cpp"]
 
 INCLUDES = ["-I" + CSRC, "-I" + os.path.join(ROOT, "include"),
             "-I" + os.path.join(CUDA_HOME, "include")]

@@ -128,6 +128,12 @@ SIGNATURES = {
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),
+    "path_cache_create": (ctypes.c_int, [c_u32, c_f32, ctypes.POINTER(_P)]),
+    "path_cache_destroy": (None, [_P]),
+    "path_cache_set_bounds": (ctypes.c_int, [_P, _PF, _PF]),
+    "path_cache_query": (ctypes.c_int, [_P, _PF, c_u32, _PF]),
+    "path_cache_train": (ctypes.c_int, [_P, _PF, c_u32, c_u32, _PF]),
+    "path_cache_access": (ctypes.c_int, [_P, _PF, _PF, _PF, _PF, c_u32]),
     "path_debug_tc_gemm": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint16),
                                           ctypes.POINTER(ctypes.c_uint16), c_u32, c_u32, _PF]),
     "path_render_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), _P, c_u32,

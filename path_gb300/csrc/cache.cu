@@ -5,6 +5,7 @@
 // D = A . B^T, the operands staged in shared memory in the canonical
 // K-major layout of tc.cuh) and its self-test entry point.
 #include "kernels.h"
+#include "nrc.h"
 #include "tc.cuh"
 
 #include <cuda_bf16.h>
@@ -96,6 +97,514 @@ cudaError_t launch_tc_gemm(const void *a, const void *b, float *d, uint32_t k_di
   dev::k_tc_gemm<<<1, 128, smem, s>>>(static_cast<const __nv_bfloat16 *>(a),
                                       static_cast<const __nv_bfloat16 *>(b), d, k_dim, n_dim,
                                       err);
+  return cudaGetLastError();
+}
+
+} // namespace pg
+
+// ---------------------------------------------------------------------------
+// Radiance cache MLP and hash-grid encoding
+
+namespace pg {
+namespace dev {
+
+using tc::smem_offset;
+
+// one query row of the MLP: hash features of position, then direction,
+// normal, albedo (9 floats), zero padding to kNrcIn
+__device__ void nrc_encode(const NrcParams &C, const float *q, float *in) {
+  // q: position xyz, direction xyz, normal xyz, albedo rgb (12 floats)
+  float p[3];
+  for (int a = 0; a < 3; ++a) {
+    p[a] = (q[a] - C.lo[a]) * C.inv_extent[a];
+    p[a] = fminf(fmaxf(p[a], 0.f), 1.f);
+  }
+  for (uint32_t l = 0; l < kNrcLevels; ++l) {
+    const float res = C.level_res[l];
+    const uint32_t side = (uint32_t)res + 1;
+    float x[3], fr[3];
+    uint32_t c0[3];
+    for (int a = 0; a < 3; ++a) {
+      x[a] = p[a] * res;
+      const float fl = fminf(floorf(x[a]), res - 1.f); // cell in [0, res - 1]
+      c0[a] = (uint32_t)fl;
+      fr[a] = x[a] - fl;
+    }
+    float f0 = 0.f, f1 = 0.f;
+    for (uint32_t c = 0; c < 8; ++c) {
+      const uint32_t gx = c0[0] + (c & 1u), gy = c0[1] + ((c >> 1) & 1u),
+                     gz = c0[2] + ((c >> 2) & 1u);
+      const float w = ((c & 1u) ? fr[0] : 1.f - fr[0]) * (((c >> 1) & 1u) ? fr[1] : 1.f - fr[1]) *
+                      (((c >> 2) & 1u) ? fr[2] : 1.f - fr[2]);
+      const uint32_t idx = nrc_grid_index(gx, gy, gz, side);
+      const float2 e = __ldg(C.table + (size_t)l * kNrcTable + idx);
+      f0 += w * e.x;
+      f1 += w * e.y;
+    }
+    in[2 * l] = f0;
+    in[2 * l + 1] = f1;
+  }
+  for (int k = 0; k < 9; ++k) {
+    in[32 + k] = q[3 + k];
+  }
+  for (uint32_t k = 41; k < kNrcIn; ++k) {
+    in[k] = 0.f;
+  }
+}
+
+__device__ __forceinline__ void store_bf16(unsigned char *tile, uint32_t row, uint32_t k,
+                                           uint32_t k_dim, float v) {
+  *reinterpret_cast<__nv_bfloat16 *>(tile + smem_offset(row, k, k_dim)) = __float2bfloat16(v);
+}
+
+__device__ __forceinline__ float load_bf16(const unsigned char *tile, uint32_t row, uint32_t k,
+                                           uint32_t k_dim) {
+  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(tile + smem_offset(row, k, k_dim)));
+}
+
+// copy n bytes global -> shared with 16-byte loads (n a multiple of 16)
+__device__ __forceinline__ void copy16(unsigned char *dst, const unsigned char *src, uint32_t n,
+                                       uint32_t tid, uint32_t nthreads) {
+  for (uint32_t i = tid * 16; i < n; i += nthreads * 16) {
+    *reinterpret_cast<uint4 *>(dst + i) = __ldg(reinterpret_cast<const uint4 *>(src + i));
+  }
+}
+
+struct TcSync {
+  uint32_t mbar;
+  uint32_t phase;
+  bool ok;
+};
+
+// all threads: make shared-memory writes visible to the tensor core and
+// order earlier tensor-memory reads before the next MMA
+__device__ __forceinline__ void tc_barrier() {
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+}
+
+// thread 0 issues D (+)= A . B^T over k_dim, then everyone waits for it
+__device__ __forceinline__ void tc_layer(TcSync &s, uint32_t tid, uint32_t tmem_d,
+                                         const unsigned char *a, const unsigned char *b,
+                                         uint32_t k_dim, uint32_t n_dim, uint32_t accumulate) {
+  if (tid == 0 && s.ok) {
+    const uint32_t idesc = tc::idesc_bf16(128, n_dim);
+    for (uint32_t k0 = 0; k0 < k_dim; k0 += 16) {
+      tc::mma_bf16(tmem_d, tc::smem_desc(tc::smem_addr(a) + k0 * 16, k_dim),
+                   tc::smem_desc(tc::smem_addr(b) + k0 * 16, k_dim), idesc,
+                   (k0 > 0 || accumulate) ? 1u : 0u);
+    }
+  }
+}
+
+// thread 0 commits the issued MMAs; every thread waits (bounded) and the
+// CTA agrees on the outcome, so a wait that gave up stops all threads alike
+__device__ __forceinline__ void tc_wait(TcSync &s, uint32_t tid, uint32_t *err) {
+  if (tid == 0 && s.ok) {
+    tc::commit(s.mbar);
+  }
+  bool ok = s.ok;
+  if (ok) {
+    ok = tc::mbar_wait(s.mbar, s.phase, kTcWaitLimit);
+  }
+  s.phase ^= 1u;
+  s.ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  if (!s.ok && tid == 0 && err != nullptr) {
+    atomicExch(err, 1u);
+  }
+  tc::fence_after_sync();
+}
+
+// Inference: out[i] = MLP(encode(queries[i])) for i < n; persistent CTAs of
+// 128 threads over tiles of 128 queries.
+__global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const float *queries,
+                                                   uint32_t n, float *out, uint32_t *err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const uint32_t tid = threadIdx.x;
+  unsigned char *w = smem;                    // forward weights, kNrcWeightBytes
+  unsigned char *x0 = w + kNrcWeightBytes;    // [128][kNrcIn]
+  unsigned char *ha = x0 + 128 * kNrcIn * 2;  // [128][64]
+  unsigned char *hb = ha + 128 * kNrcHid * 2; // [128][64]
+  copy16(w, C.w_fwd, kNrcWeightBytes, tid, 128);
+  if (tid < 32) {
+    tc::tmem_alloc(tc::smem_addr(&tmem_base), 64);
+  }
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_addr(&mbar), 1);
+  }
+  tc_barrier();
+  TcSync sync{tc::smem_addr(&mbar), 0, true};
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_base = (tid / 32) * 32;
+  for (uint32_t tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
+    const uint32_t row = tid;
+    const uint32_t qi = tile * 128 + row;
+    float in[kNrcIn];
+    if (qi < n) {
+      nrc_encode(C, queries + (size_t)qi * 12, in);
+    } else {
+      for (uint32_t k = 0; k < kNrcIn; ++k) {
+        in[k] = 0.f;
+      }
+    }
+    for (uint32_t k = 0; k < kNrcIn; ++k) {
+      store_bf16(x0, row, k, kNrcIn, in[k]);
+    }
+    tc_barrier();
+    const unsigned char *a = x0;
+    for (uint32_t l = 0; l < kNrcLayers; ++l) {
+      const uint32_t k_dim = nrc_in_dim(l), n_dim = nrc_out_dim(l);
+      tc_layer(sync, tid, tmem, a, w + nrc_weight_offset(l) * 2, k_dim, n_dim, 0);
+      tc_wait(sync, tid, err);
+      if (!sync.ok) {
+        break;
+      }
+      unsigned char *dst = (l & 1) ? hb : ha;
+      for (uint32_t c0 = 0; c0 < n_dim; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + (lane_base << 16) + c0, v);
+        if (l + 1 < kNrcLayers) {
+          for (int j = 0; j < 16; ++j) {
+            store_bf16(dst, row, c0 + j, kNrcHid, fmaxf(v[j], 0.f));
+          }
+        } else if (qi < n) {
+          out[(size_t)qi * 3 + 0] = v[0];
+          out[(size_t)qi * 3 + 1] = v[1];
+          out[(size_t)qi * 3 + 2] = v[2];
+        }
+      }
+      tc_barrier();
+      a = dst;
+    }
+    if (!sync.ok) {
+      break;
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) {
+    tc::tmem_dealloc(tmem, 64);
+  }
+}
+
+
+// Training on tiles of 128 records (query: 12 floats, target: 3 floats,
+// padding: 1).  Forward as in inference, keeping each layer's input
+// transposed ([in][128], K-major) in this CTA's global scratch; relative L2
+// loss (pred - target)^2 / (pred^2 + 0.01) with the denominator held
+// constant; backward per layer: dW_l += dY_l^T . X_l (tensor memory,
+// accumulated over the CTA's tiles, dY^T padded to 128 rows with zeros) and
+// dX_l = dY_l . W_l, ReLU-masked into dY_{l-1}.  dLoss/d(hash features) of
+// every record goes to d_feat [n][32]; the CTA's dW is added to grad_w at
+// the end.  inv_batch scales the loss (1 / records of the step).
+__global__ void __launch_bounds__(128) k_nrc_train(const NrcParams C, const float *records,
+                                                   uint32_t n, float inv_batch, float *grad_w,
+                                                   float *d_feat, unsigned char *scratch,
+                                                   float *loss_out, uint32_t *err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const uint32_t tid = threadIdx.x;
+  unsigned char *wf = smem;                           // [out][in] tiles
+  unsigned char *wb = wf + kNrcWeightBytes;           // [in][out] tiles
+  unsigned char *x0 = wb + kNrcWeightBytes;           // [128][48]
+  unsigned char *pa = x0 + 128 * kNrcIn * 2;          // [128][64]
+  unsigned char *pb = pa + 128 * kNrcHid * 2;         // [128][64]
+  unsigned char *st = pb + 128 * kNrcHid * 2;         // X_l^T staging [64][128]
+  unsigned char *tt = st + kNrcHid * 128 * 2;         // dY^T [128][128], rows >= 64 zero
+  // this CTA's scratch: X_l^T of the six layers
+  unsigned char *scr = scratch + (size_t)blockIdx.x * (kNrcIn + 5 * kNrcHid) * 128 * 2;
+  auto scr_off = [](uint32_t l) -> uint32_t {
+    return l == 0 ? 0u : (kNrcIn + (l - 1) * kNrcHid) * 128 * 2;
+  };
+  copy16(wf, C.w_fwd, kNrcWeightBytes, tid, 128);
+  copy16(wb, C.w_bwd, kNrcWeightBytes, tid, 128);
+  for (uint32_t i = tid; i < 128 * 128 * 2 / 16; i += 128) {
+    reinterpret_cast<uint4 *>(tt)[i] = make_uint4(0, 0, 0, 0);
+  }
+  if (tid < 32) {
+    tc::tmem_alloc(tc::smem_addr(&tmem_base), 512);
+  }
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_addr(&mbar), 1);
+  }
+  tc_barrier();
+  TcSync sync{tc::smem_addr(&mbar), 0, true};
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_base = (tid / 32) * 32;
+  const uint32_t row = tid;
+  uint32_t tiles_done = 0;
+  float loss_sum = 0.f;
+  for (uint32_t tile = blockIdx.x; tile * 128 < n && sync.ok; tile += gridDim.x) {
+    const uint32_t ri = tile * 128 + row;
+    const bool valid = ri < n;
+    float in[kNrcIn];
+    float target[3] = {0.f, 0.f, 0.f};
+    if (valid) {
+      const float *rec = records + (size_t)ri * 16;
+      nrc_encode(C, rec, in);
+      target[0] = rec[12];
+      target[1] = rec[13];
+      target[2] = rec[14];
+    } else {
+      for (uint32_t k = 0; k < kNrcIn; ++k) {
+        in[k] = 0.f;
+      }
+    }
+    for (uint32_t k = 0; k < kNrcIn; ++k) {
+      store_bf16(x0, row, k, kNrcIn, in[k]);
+      store_bf16(scr + scr_off(0), k, row, 128, in[k]);
+    }
+    tc_barrier();
+    // forward
+    const unsigned char *a = x0;
+    for (uint32_t l = 0; l < kNrcLayers && sync.ok; ++l) {
+      const uint32_t k_dim = nrc_in_dim(l), n_dim = nrc_out_dim(l);
+      tc_layer(sync, tid, tmem, a, wf + nrc_weight_offset(l) * 2, k_dim, n_dim, 0);
+      tc_wait(sync, tid, err);
+      if (!sync.ok) {
+        break;
+      }
+      unsigned char *dst = (l & 1) ? pb : pa;
+      for (uint32_t c0 = 0; c0 < n_dim; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + (lane_base << 16) + c0, v);
+        if (l + 1 < kNrcLayers) {
+          for (int j = 0; j < 16; ++j) {
+            const float h = fmaxf(v[j], 0.f);
+            store_bf16(dst, row, c0 + j, kNrcHid, h);
+            store_bf16(scr + scr_off(l + 1), c0 + j, row, 128, h);
+          }
+        } else {
+          // output layer: dLoss/dpred into dY5 ([128][16]) and dY5^T
+          for (int j = 0; j < 16; ++j) {
+            float g = 0.f;
+            if (j < 3 && valid) {
+              const float pr = v[j];
+              const float den = pr * pr + 0.01f;
+              const float diff = pr - target[j];
+              g = 2.f * diff / den * inv_batch;
+              loss_sum += diff * diff / den * inv_batch;
+            }
+            store_bf16(dst, row, j, kNrcOut, g);
+            store_bf16(tt, j, row, 128, g);
+          }
+          for (uint32_t j = kNrcOut; j < kNrcHid; ++j) {
+            store_bf16(tt, j, row, 128, 0.f);
+          }
+        }
+      }
+      tc_barrier();
+      a = dst;
+    }
+    // backward; `a` holds dY5 in the A layout (K = 16)
+    unsigned char *dy = const_cast<unsigned char *>(a);
+    for (int l = (int)kNrcLayers - 1; l >= 0 && sync.ok; --l) {
+      const uint32_t in_l = nrc_in_dim((uint32_t)l), out_l = nrc_out_dim((uint32_t)l);
+      for (uint32_t i = tid * 16; i < in_l * 128 * 2; i += 128 * 16) {
+        *reinterpret_cast<uint4 *>(st + i) =
+            *reinterpret_cast<const uint4 *>(scr + scr_off((uint32_t)l) + i);
+      }
+      tc_barrier();
+      // dW_l (+)= dY_l^T . X_l ; dX_l = dY_l . W_l
+      tc_layer(sync, tid, tmem + nrc_dw_column((uint32_t)l), tt, st, 128, in_l,
+               tiles_done > 0 ? 1u : 0u);
+      tc_layer(sync, tid, tmem, dy, wb + nrc_weight_offset((uint32_t)l) * 2, out_l, in_l, 0);
+      tc_wait(sync, tid, err);
+      if (!sync.ok) {
+        break;
+      }
+      unsigned char *next = (dy == pa) ? pb : pa;
+      for (uint32_t c0 = 0; c0 < in_l; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + (lane_base << 16) + c0, v);
+        for (int j = 0; j < 16; ++j) {
+          const uint32_t i = c0 + j;
+          if (l > 0) {
+            const float x = load_bf16(st, i, row, 128); // X_l = H_l, ReLU output
+            const float g = x > 0.f ? v[j] : 0.f;
+            store_bf16(next, row, i, kNrcHid, g);
+            store_bf16(tt, i, row, 128, g);
+          } else if (valid && i < 2 * kNrcLevels) {
+            d_feat[(size_t)ri * 32 + i] = v[j];
+          }
+        }
+      }
+      tc_barrier();
+      dy = next;
+    }
+    ++tiles_done;
+  }
+  if (tiles_done > 0 && sync.ok) {
+    // this CTA's weight gradients, lane = output row
+    for (uint32_t l = 0; l < kNrcLayers; ++l) {
+      const uint32_t in_l = nrc_in_dim(l), out_l = nrc_out_dim(l);
+      const uint32_t rows = l + 1 == kNrcLayers ? 3u : out_l;
+      for (uint32_t c0 = 0; c0 < in_l; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + (lane_base << 16) + nrc_dw_column(l) + c0, v);
+        if (row < rows) {
+          for (int j = 0; j < 16; ++j) {
+            atomicAdd(grad_w + nrc_weight_offset(l) + row * in_l + c0 + j, v[j]);
+          }
+        }
+      }
+    }
+  }
+  if (loss_out != nullptr) {
+    atomicAdd(loss_out, loss_sum);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) {
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+// dLoss/d(hash table): each record's feature gradient spread over the
+// eight grid vertices of every level with the trilinear weights
+__global__ void k_nrc_grid_backward(const NrcParams C, const float *records, uint32_t n,
+                                    const float *d_feat, float2 *grad_table) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) {
+    return;
+  }
+  const float *q = records + (size_t)i * 16;
+  const float *g = d_feat + (size_t)i * 32;
+  float p[3];
+  for (int a = 0; a < 3; ++a) {
+    p[a] = fminf(fmaxf((q[a] - C.lo[a]) * C.inv_extent[a], 0.f), 1.f);
+  }
+  for (uint32_t l = 0; l < kNrcLevels; ++l) {
+    const float res = C.level_res[l];
+    const uint32_t side = (uint32_t)res + 1;
+    float fr[3];
+    uint32_t c0[3];
+    for (int a = 0; a < 3; ++a) {
+      const float x = p[a] * res;
+      const float fl = fminf(floorf(x), res - 1.f);
+      c0[a] = (uint32_t)fl;
+      fr[a] = x - fl;
+    }
+    for (uint32_t c = 0; c < 8; ++c) {
+      const uint32_t gx = c0[0] + (c & 1u), gy = c0[1] + ((c >> 1) & 1u),
+                     gz = c0[2] + ((c >> 2) & 1u);
+      const float w = ((c & 1u) ? fr[0] : 1.f - fr[0]) * (((c >> 1) & 1u) ? fr[1] : 1.f - fr[1]) *
+                      (((c >> 2) & 1u) ? fr[2] : 1.f - fr[2]);
+      float2 *e = grad_table + (size_t)l * kNrcTable + nrc_grid_index(gx, gy, gz, side);
+      atomicAdd(&e->x, w * g[2 * l]);
+      atomicAdd(&e->y, w * g[2 * l + 1]);
+    }
+  }
+}
+
+// FP32 master weights -> the two BF16 tile images (forward [out][in],
+// backward [in][out]); one thread per weight
+__global__ void k_nrc_pack(const float *w, unsigned char *w_fwd, unsigned char *w_bwd) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kNrcWeights) {
+    return;
+  }
+  uint32_t l = 0;
+  while (l + 1 < kNrcLayers && e >= nrc_weight_offset(l + 1)) {
+    ++l;
+  }
+  const uint32_t in_l = nrc_in_dim(l), out_l = nrc_out_dim(l);
+  const uint32_t local = e - nrc_weight_offset(l);
+  const uint32_t o = local / in_l, i = local % in_l;
+  const __nv_bfloat16 v = __float2bfloat16(w[e]);
+  unsigned char *f = w_fwd + nrc_weight_offset(l) * 2;
+  unsigned char *b = w_bwd + nrc_weight_offset(l) * 2;
+  *reinterpret_cast<__nv_bfloat16 *>(f + smem_offset(o, i, in_l)) = v;
+  *reinterpret_cast<__nv_bfloat16 *>(b + smem_offset(i, o, out_l)) = v;
+}
+
+// Adam (Kingma and Ba 2015) with bias correction; clears the gradient
+__global__ void k_adam(float *param, float *grad, float *m, float *v, size_t n, float lr,
+                       float beta1, float beta2, float eps, float step) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) {
+    return;
+  }
+  const float g = grad[i];
+  const float mi = beta1 * m[i] + (1.f - beta1) * g;
+  const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / (1.f - powf(beta1, step));
+  const float vh = vi / (1.f - powf(beta2, step));
+  param[i] -= lr * mh / (sqrtf(vh) + eps);
+  grad[i] = 0.f;
+}
+
+} // namespace dev
+
+size_t nrc_infer_smem_bytes() {
+  return kNrcWeightBytes + 128 * kNrcIn * 2 + 2 * 128 * kNrcHid * 2;
+}
+
+size_t nrc_train_smem_bytes() {
+  return 2 * kNrcWeightBytes + 128 * kNrcIn * 2 + 2 * 128 * kNrcHid * 2 + kNrcHid * 128 * 2 +
+         128 * 128 * 2;
+}
+
+size_t nrc_train_scratch_bytes(int grid) {
+  return (size_t)grid * (kNrcIn + 5 * kNrcHid) * 128 * 2;
+}
+
+cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n, float *out,
+                             uint32_t *err, int grid, cudaStream_t s) {
+  const size_t smem = nrc_infer_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(dev::k_nrc_infer,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess || n == 0) {
+    return e;
+  }
+  dev::k_nrc_infer<<<grid, 128, smem, s>>>(c, queries, n, out, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_train(const NrcParams &c, const float *records, uint32_t n,
+                             float inv_batch, float *grad_w, float *d_feat,
+                             unsigned char *scratch, float *loss, uint32_t *err, int grid,
+                             cudaStream_t s) {
+  const size_t smem = nrc_train_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(dev::k_nrc_train,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess || n == 0) {
+    return e;
+  }
+  dev::k_nrc_train<<<grid, 128, smem, s>>>(c, records, n, inv_batch, grad_w, d_feat, scratch,
+                                           loss, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_grid_backward(const NrcParams &c, const float *records, uint32_t n,
+                                     const float *d_feat, float2 *grad_table, cudaStream_t s) {
+  if (n == 0) {
+    return cudaSuccess;
+  }
+  dev::k_nrc_grid_backward<<<(n + 255) / 256, 256, 0, s>>>(c, records, n, d_feat, grad_table);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_pack_weights(const float *w, unsigned char *w_fwd, unsigned char *w_bwd,
+                                    cudaStream_t s) {
+  dev::k_nrc_pack<<<(kNrcWeights + 255) / 256, 256, 0, s>>>(w, w_fwd, w_bwd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float *param, float *grad, float *m, float *v, size_t n, float lr,
+                        float beta1, float beta2, float eps, float step, cudaStream_t s) {
+  if (n == 0) {
+    return cudaSuccess;
+  }
+  dev::k_adam<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(param, grad, m, v, n, lr, beta1,
+                                                           beta2, eps, step);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 // C ABI of the render path (include/path_gb300.h).
 #include "path_gb300.h"
 
+#include "cache_host.h"
 #include "kernels.h"
 #include "renderer.h"
 #include "scene.h"
@@ -297,6 +298,89 @@ path_status path_render(path_renderer *renderer, uint32_t exec_model,
   return guarded([&] {
     return from(renderer->r.render(*sample_spec, *output, scene->s, samples_per, *settings,
                                    seconds));
+  });
+}
+
+struct path_cache {
+  pg::RadianceCache c;
+  pg::DeviceBuffer in, out;
+};
+
+path_status path_cache_create(uint32_t seed, float learning_rate, path_cache **out) {
+  if (!out) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&]() -> path_status {
+    auto *c = new path_cache();
+    path_status st = from(c->c.init(seed, learning_rate));
+    if (st != PATH_OK) {
+      delete c;
+      return st;
+    }
+    *out = c;
+    return PATH_OK;
+  });
+}
+
+void path_cache_destroy(path_cache *cache) { delete cache; }
+
+path_status path_cache_set_bounds(path_cache *cache, const float *lo, const float *hi) {
+  if (!cache || !lo || !hi) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  cache->c.set_bounds(lo, hi);
+  return PATH_OK;
+}
+
+path_status path_cache_query(path_cache *cache, const float *queries, uint32_t n, float *out) {
+  if (!cache || (n > 0 && (!queries || !out))) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&]() -> path_status {
+    cudaStream_t s = cache->c.stream();
+    cudaError_t e;
+    if ((e = cache->in.upload(queries, (size_t)n * 48, s)) != cudaSuccess ||
+        (e = cache->out.ensure((size_t)std::max<uint32_t>(n, 1) * 12)) != cudaSuccess) {
+      return from(pg::cuda_status(e, "cache query"));
+    }
+    path_status st = from(cache->c.infer(cache->in.as<float>(), n, cache->out.as<float>(), s));
+    if (st != PATH_OK) {
+      return st;
+    }
+    if ((e = cudaMemcpyAsync(out, cache->out.get(), (size_t)n * 12, cudaMemcpyDeviceToHost,
+                             s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+      return from(pg::cuda_status(e, "cache query"));
+    }
+    return PATH_OK;
+  });
+}
+
+path_status path_cache_train(path_cache *cache, const float *records, uint32_t n,
+                             uint32_t apply_update, float *loss) {
+  if (!cache || (n > 0 && !records)) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&]() -> path_status {
+    cudaError_t e = cache->in.upload(records, (size_t)n * 64, cache->c.stream());
+    if (e != cudaSuccess) {
+      return from(pg::cuda_status(e, "cache train"));
+    }
+    return from(apply_update ? cache->c.train(cache->in.as<float>(), n, loss)
+                             : cache->c.gradients(cache->in.as<float>(), n, loss));
+  });
+}
+
+path_status path_cache_access(path_cache *cache, float *weights, float *table,
+                              float *grad_weights, float *grad_table, uint32_t set) {
+  if (!cache) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  if (set && (grad_weights || grad_table)) {
+    return fail(PATH_ERR_ARGUMENT, "gradients cannot be set");
+  }
+  return guarded([&] {
+    return from(cache->c.access(weights, table, grad_weights, grad_table, set != 0));
   });
 }
 

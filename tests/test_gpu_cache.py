@@ -1,0 +1,79 @@
+"""Radiance cache network on the tensor cores against its NumPy restatement
+(tests/nrc_reference.py): inference, and the gradients of one training step
+(weights and hash table); and that training reduces the loss."""
+
+import numpy as np
+import pytest
+
+from path_gb300 import api
+
+import nrc_reference as ref
+
+pytestmark = pytest.mark.gpu
+
+LO, HI = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+
+
+def _queries(rng, n):
+    pos = rng.uniform(-1, 1, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    alb = rng.uniform(0, 1, (n, 3))
+    return np.concatenate([pos, d, nrm, alb], 1).astype(np.float32)
+
+
+def _cache(seed=3):
+    c = api.RadianceCache(seed=seed)
+    c.set_bounds(LO, HI)
+    w, t = c.get()
+    # larger table features so the encoding matters
+    rng = np.random.default_rng(seed)
+    t = rng.uniform(-0.5, 0.5, t.shape).astype(np.float32)
+    c.set(table=t)
+    return c, w, t
+
+
+def test_inference_matches_numpy(lib):
+    rng = np.random.default_rng(1)
+    c, w, t = _cache()
+    q = _queries(rng, 1000)
+    got = c.query(q)
+    want, _, _, _ = ref.forward(q, w, t, LO, HI)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    print(f"inference rel err {err:.2e}")
+    assert err < 1e-2
+
+
+def test_training_gradients_match_numpy(lib):
+    rng = np.random.default_rng(2)
+    c, w, t = _cache()
+    q = _queries(rng, 700)
+    target = rng.uniform(0, 2, (700, 3)).astype(np.float32)
+    rec = np.concatenate([q, target, np.zeros((700, 1), np.float32)], 1)
+    loss = c.train(rec, update=False)
+    _, _, gw, gt = c.get(grads=True)
+    loss_ref, gw_ref, gt_ref = ref.gradients(rec, w, t, LO, HI)
+    ew = np.linalg.norm(gw - gw_ref) / np.linalg.norm(gw_ref)
+    et = np.linalg.norm(gt - gt_ref) / np.linalg.norm(gt_ref)
+    print(f"loss {loss:.5f} (numpy {loss_ref:.5f}); weight grad rel err {ew:.2e}, "
+          f"table grad rel err {et:.2e}")
+    assert abs(loss - loss_ref) / loss_ref < 1e-2
+    assert ew < 2e-2
+    assert et < 2e-2
+
+
+def test_training_reduces_the_loss(lib):
+    rng = np.random.default_rng(4)
+    c = api.RadianceCache(seed=5)
+    c.set_bounds(LO, HI)
+    q = _queries(rng, 1 << 14)
+    # a smooth target radiance field
+    p = q[:, :3]
+    target = np.stack([1 + np.sin(3 * p[:, 0]), 1 + np.cos(2 * p[:, 1]),
+                       1 + 0.5 * p[:, 2] * q[:, 9]], 1).astype(np.float32)
+    rec = np.concatenate([q, target, np.zeros((len(q), 1), np.float32)], 1)
+    losses = [c.train(rec) for _ in range(200)]
+    print(f"loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+    assert losses[-1] < 0.1 * losses[0]
