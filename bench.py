@@ -251,6 +251,82 @@ def run_batched(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def run_cache(args, rank, world, local_rank):
+    """Time to 0.02 relative RMSE, plain tracer against the radiance cache,
+    on the large-mesh room at 1024 x 1024 in frames of 4 spp (depth 8).
+    Reference: 4096 spp of the plain tracer accumulated in FP64 (64 frames
+    of 64 spp).  Plain: frames of 4 new samples each, accumulated in FP64
+    until the error is <= 0.02.  Cache: frames whose paths end into the
+    cache after 2 bounces, each followed by 4 Adam steps on 2^16 records
+    from fresh full-length paths, accumulated the same way (the first
+    frames, with an untrained cache, included).  Wall time of render +
+    training calls."""
+    import torch
+    from path_gb300 import api, scenes
+    size = args.size or 1024
+    scene, w, h, _, depth, desc = make_workload("large_mesh", size, 4)
+    settings = scenes.path_settings(8, "wide")
+    settings.kernel_approach = 1
+    f2w = scenes.cornell_camera(w, h)
+    r = api.Renderer()
+    out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    t0 = time.time()
+    ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    ref_frames = 64
+    for f in range(ref_frames):
+        r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w, sample_offset=64 * f), out,
+                 scene, 64, settings)
+        ref += out.double()
+    ref /= ref_frames
+    ref_s = time.time() - t0
+    ref_norm = float(torch.linalg.norm(ref))
+
+    def run(cached, target=0.02):
+        cache = api.RadianceCache(seed=1) if cached else None
+        acc = torch.zeros_like(ref)
+        wall, frames, err = 0.0, 0, None
+        curve = []
+        base = 64 * ref_frames  # samples the reference did not use
+        while frames < args.max_frames:
+            spec = api.SquareImage(w, h, f2w, sample_offset=base + 4 * frames)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            if cached:
+                r.render_cached(cache, spec, out, scene, 4, settings, cache_depth=2,
+                                train_paths=1 << 16, train_steps=4)
+            else:
+                r.render(api.ExecutionModel.GPU, spec, out, scene, 4, settings)
+            torch.cuda.synchronize()
+            wall += time.perf_counter() - t
+            frames += 1
+            acc += out.double()
+            err = float(torch.linalg.norm(acc / frames - ref)) / ref_norm
+            if frames in (1, 2, 4, 8, 16, 32, 64, 128, 256) or err <= target:
+                curve.append((frames, round(wall, 4), round(err, 5)))
+            if err <= target:
+                break
+        return {"frames": frames, "seconds": wall, "rel_rmse": err,
+                "reached": err is not None and err <= target, "curve": curve}
+
+    plain = run(False)
+    cached = run(True)
+    line = {
+        "metric": "seconds to 0.02 relative RMSE", "unit": "s", "higher_is_better": False,
+        "value": cached["seconds"] if cached["reached"] else None,
+        "n_gpus": 1, "dtype": "f32 render, bf16 cache MLP", "data": "synthetic",
+        "config": {"workload": f"{desc} in 4-spp frames; reference 4096 spp FP64",
+                   "cache": "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
+                            "paths end into the cache after 2 bounces, 2^16 records x 4 steps "
+                            "per frame"},
+        "plain": plain, "cached": cached,
+        "ratio_cached_over_plain": (cached["seconds"] / plain["seconds"]
+                                    if plain["reached"] and cached["reached"] else None),
+        "reference_seconds": ref_s,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -258,7 +334,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mesh",
-                    choices=["large_mesh", "cornell", "batched"])
+                    choices=["large_mesh", "cornell", "batched", "cache"])
+    ap.add_argument("--max-frames", type=int, default=400,
+                    help="cache workload: frames before giving up on the error target")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: scene count")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
@@ -267,6 +345,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-megakernel", action="store_true",
                     help="skip the megakernel comparison render")
+    ap.add_argument("--no-reference-error", action="store_true",
+                    help="skip the 4096-spp FP64 reference render and the error against it")
     ap.add_argument("--size", type=int, default=None,
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
@@ -292,6 +372,9 @@ def main():
     build.build()
     if args.workload == "batched":
         run_batched(args, rank, world, local_rank)
+        return
+    if args.workload == "cache":
+        run_cache(args, rank, world, local_rank)
         return
     scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, args.traversal)
@@ -409,6 +492,24 @@ def main():
         "setup_s": setup_s, "bvh_build_s": st0["bvh_build_seconds"],
         "clocks": clocks.summary(),
     }
+    if not args.no_reference_error and rank == 0:
+        # the timed image's error against a 4096-spp render of the same
+        # scene accumulated in FP64 (64 renders of 64 new samples each)
+        ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+        rs = settings.copy()
+        rs.time_kernels = 0
+        n_ref = max(1, 4096 // 64)
+        for f in range(n_ref):
+            r.render(api.ExecutionModel.GPU,
+                     api.SquareImage(w, h, f2w, sample_offset=spp + 64 * f), dev_out, scene,
+                     64, rs)
+            ref += dev_out.double()
+        ref /= n_ref
+        r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, rs)
+        err = float(torch.linalg.norm(dev_out.double() - ref) / torch.linalg.norm(ref))
+        line["error_vs_4096spp_fp64"] = {
+            "rel_rmse": err, "reference": "4096 spp (samples spp..spp+4095), FP64 sum",
+            "image": f"the timed {spp}-spp render"}
     if streaming and args.size is None and args.spp is None and not args.no_megakernel:
         # the same render through the megakernel (identical image), for the
         # wavefront-versus-megakernel comparison of this workload

@@ -158,6 +158,9 @@ typedef struct {
    * pixels are computed exactly as in the whole-image render; output rows
    * outside the band are left untouched.  GB300 addition. */
   uint32_t row_start, row_end;
+  /* first Sobol sample index of every pixel (GB300 addition: progressive
+   * rendering in frames of samples [sample_offset, sample_offset + spp)) */
+  uint32_t sample_offset;
 } path_sample_spec;
 
 typedef enum {
@@ -318,6 +321,19 @@ path_status path_cache_train(path_cache *cache, const float *records, uint32_t n
  * host (set = 0) or weights and table from the host (set = 1); NULL skips */
 path_status path_cache_access(path_cache *cache, float *weights, float *table,
                               float *grad_weights, float *grad_table, uint32_t set);
+
+/* One frame of the render with the radiance cache: a streaming render whose
+ * paths end into the cache at vertex cache_depth (the cache's prediction of
+ * the radiance leaving that vertex, times the path throughput, replaces the
+ * rest of the path), then train_steps Adam steps on train_paths records from
+ * full-length training paths (one random vertex each: its query and the
+ * radiance the rest of its path carried back).  Square images, streaming
+ * approach, 8-wide BVH. */
+path_status path_render_cached(path_renderer *renderer, path_cache *cache,
+                               const path_sample_spec *sample_spec, const path_output *output,
+                               const path_scene *scene, uint32_t samples_per,
+                               const path_settings *settings, uint32_t cache_depth,
+                               uint32_t train_paths, uint32_t train_steps, double *seconds);
 
 /* ---- batched render (GB300 addition; the reference renders one scene per
  * call) ---- */

@@ -169,11 +169,12 @@ class SquareImage:
     """render::SquareImageSpec; ``rows=(start, end)`` renders only that band
     of rows (bit-identical to the same rows of the whole render)."""
 
-    def __init__(self, x_dim, y_dim, film_to_world, rows=None):
+    def __init__(self, x_dim, y_dim, film_to_world, rows=None, sample_offset=0):
         self.x_dim = int(x_dim)
         self.y_dim = int(y_dim)
         self.film_to_world = np.asarray(film_to_world, np.float32).reshape(12)
         self.rows = rows
+        self.sample_offset = int(sample_offset)
 
     def to_c(self):
         s = capi.SampleSpec()
@@ -183,6 +184,7 @@ class SquareImage:
         s.film_to_world[:] = [float(v) for v in self.film_to_world]
         if self.rows is not None:
             s.row_start, s.row_end = int(self.rows[0]), int(self.rows[1])
+        s.sample_offset = self.sample_offset
         return s
 
 
@@ -307,6 +309,18 @@ class Renderer:
             out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(secs)))
         del keep
         return out[:n_mat]
+
+    def render_cached(self, cache, sample_spec, output, scene, samples_per, settings,
+                      cache_depth=2, train_paths=1 << 16, train_steps=4):
+        """One frame with the radiance cache (path_render_cached)."""
+        o = self._output_c(output)
+        spec = sample_spec.to_c()
+        secs = ctypes.c_double()
+        capi.check(capi.load().path_render_cached(
+            self._h, cache.handle, ctypes.byref(spec), ctypes.byref(o), scene.handle,
+            int(samples_per), ctypes.byref(settings.raw), int(cache_depth), int(train_paths),
+            int(train_steps), ctypes.byref(secs)))
+        return secs.value
 
     @staticmethod
     def _output_c(output):

@@ -50,7 +50,7 @@ class SampleSpec(ctypes.Structure):
     _fields_ = [("type", c_u32), ("x_dim", c_u32), ("y_dim", c_u32),
                 ("film_to_world", c_f32 * 12), ("rays", ctypes.POINTER(c_f32)),
                 ("n_rays", c_u32), ("idxs", ctypes.POINTER(c_u32)), ("row_start", c_u32),
-                ("row_end", c_u32)]
+                ("row_end", c_u32), ("sample_offset", c_u32)]
 
 
 class Output(ctypes.Structure):
@@ -134,6 +134,10 @@ SIGNATURES = {
     "path_cache_query": (ctypes.c_int, [_P, _PF, c_u32, _PF]),
     "path_cache_train": (ctypes.c_int, [_P, _PF, c_u32, c_u32, _PF]),
     "path_cache_access": (ctypes.c_int, [_P, _PF, _PF, _PF, _PF, c_u32]),
+    "path_render_cached": (ctypes.c_int, [_P, _P, ctypes.POINTER(SampleSpec),
+                                          ctypes.POINTER(Output), _P, c_u32,
+                                          ctypes.POINTER(PathSettings), c_u32, c_u32, c_u32,
+                                          ctypes.POINTER(ctypes.c_double)]),
     "path_debug_tc_gemm": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint16),
                                           ctypes.POINTER(ctypes.c_uint16), c_u32, c_u32, _PF]),
     "path_render_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), _P, c_u32,

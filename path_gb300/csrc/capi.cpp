@@ -384,6 +384,21 @@ path_status path_cache_access(path_cache *cache, float *weights, float *table,
   });
 }
 
+path_status path_render_cached(path_renderer *renderer, path_cache *cache,
+                               const path_sample_spec *sample_spec, const path_output *output,
+                               const path_scene *scene, uint32_t samples_per,
+                               const path_settings *settings, uint32_t cache_depth,
+                               uint32_t train_paths, uint32_t train_steps, double *seconds) {
+  if (!renderer || !cache || !sample_spec || !output || !scene || !settings) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    return from(renderer->r.render_cached(*sample_spec, *output, scene->s, samples_per,
+                                          *settings, cache->c, cache_depth, train_paths,
+                                          train_steps, seconds));
+  });
+}
+
 path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k, uint32_t n,
                                float *d) {
   if (!a || !b || !d) {

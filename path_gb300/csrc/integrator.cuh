@@ -942,7 +942,7 @@ __device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Came
                                                uint32_t sample_idx, uint32_t x, uint32_t y,
                                                PathState &s) {
   const uint32_t location = x + y * cam.x_dim;
-  s.rng.row = P.sobol + (size_t)sample_idx * P.dim_bound;
+  s.rng.row = P.sobol + (size_t)(sample_idx + P.sample_offset) * P.dim_bound;
   s.rng.bound = P.dim_bound;
   s.rng.dim = fnv_hash(location) % P.init_dim_bound;
   ray r;
@@ -982,10 +982,25 @@ __device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sampl
 // light ray and its hit's emission added (and from which materials), the
 // shaded vertex, and the directions its light sample and continuation took.
 struct StepTrace {
-  bool light_added, emit_added, hit, nee, continuous;
+  bool light_added, emit_added, hit, nee, continuous, cache_query;
   uint32_t light_mat, mat;
-  f3 in, normal, nee_dir, next_dir;
+  f3 in, normal, nee_dir, next_dir, point;
+  rgb albedo;
 };
+
+// the reflectance a radiance-cache query carries for a material
+__device__ __forceinline__ rgb albedo_of(const Mat &m) {
+  switch (m.type) {
+  case kGlossy:
+  case kMirror:
+  case kGGX:
+    return m.specular;
+  case kDielectric:
+    return mkrgb(1.f, 1.f, 1.f);
+  default:
+    return m.diffuse;
+  }
+}
 
 __device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L, PathState &s,
                                        const Hit &lh, const Hit &nh,
@@ -994,6 +1009,7 @@ __device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L,
   const bool cull = P.back_cull != 0;
   if (tr != nullptr) {
     tr->light_added = tr->emit_added = tr->hit = tr->nee = tr->continuous = false;
+    tr->cache_query = false;
   }
   if (s.has_light && lh.ok && pm::fabs(s.light_target - lh.t) <= 1e-6f &&
       (!cull || !lh.back)) {
@@ -1022,6 +1038,16 @@ __device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L,
     tr->mat = mi;
     tr->in = s.d;
     tr->normal = normal;
+    tr->point = point;
+    tr->albedo = albedo_of(mat);
+    if (P.cache_depth != 0 && s.iters == P.cache_depth) {
+      // the path ends into the radiance cache at this vertex
+      tr->cache_query = true;
+      s.o = point;
+      s.has_next = false;
+      s.has_light = false;
+      return false;
+    }
   }
   bool new_has_light = false;
   rgb new_light_mult = zero_rgb();

@@ -50,6 +50,10 @@ struct RenderParams {
   uint32_t start_block;
   // image rows [row_lo, row_hi) are rendered; threads of other rows exit
   uint32_t row_lo, row_hi;
+  // Sobol row of sample s is s + sample_offset
+  uint32_t sample_offset;
+  // radiance cache: paths end into the cache at this vertex (0 = off)
+  uint32_t cache_depth;
 };
 
 enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
@@ -105,6 +109,11 @@ struct WaveParams {
   float4 *pend_nee;      // ... along its light sample
   uint32_t *pend_mat;    // its material, 0xffffffff when none
   double *d_params;      // [materials][7]: reflectance rgb, roughness, emission rgb
+  // radiance cache (P.cache_depth > 0): per sample the query of the vertex
+  // where its path ended into the cache ([12] floats) and the path
+  // throughput there (zero when the path ended before it)
+  float *cache_q;
+  float *cache_beta;
 };
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
@@ -119,6 +128,14 @@ cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_
 // per-pixel sums of the sample buffer into p.out_rgb / p.out_bgra
 cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
                                  uint32_t n_blocks, cudaStream_t s);
+
+// training records for the radiance cache: n full-length paths from random
+// pixels, one random vertex each ([n][16]: query, radiance, pad)
+cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, float *records,
+                             cudaStream_t s);
+// sample_rgb[i] += beta[i] * max(pred[i], 0) for the n samples
+cudaError_t launch_nrc_apply(float *sample_rgb, const float *beta, const float *pred,
+                             size_t n, cudaStream_t s);
 
 // integration megakernel over blocks [start_block, start_block + n_blocks)
 cudaError_t launch_render(const RenderParams &p, uint32_t traversal,

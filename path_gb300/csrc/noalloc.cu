@@ -95,7 +95,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
     return Status::err(PATH_ERR_ARGUMENT,
                        "scene not resident on this renderer: render it once with path_render");
   }
-  if (sobol_bound_ != st.max_sample_size || sobol_count_ != spp || !sobol_table_.get()) {
+  if (sobol_bound_ != st.max_sample_size || sobol_count_ < spp || !sobol_table_.get()) {
     return Status::err(PATH_ERR_ARGUMENT,
                        "Sobol table for this max_sample_size / samples_per not resident: "
                        "render once with path_render");

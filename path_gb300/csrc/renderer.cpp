@@ -1,5 +1,6 @@
 // render::Renderer for the GPU execution model (see renderer.h).
 #include "renderer.h"
+#include "cache_host.h"
 
 #include <curand.h>
 
@@ -290,9 +291,16 @@ Status Renderer::prepare_scene(const FlatScene &flat, uint64_t id, uint64_t vers
 }
 
 Status Renderer::prepare_sobol(uint32_t dim_bound, uint32_t count) {
-  if (sobol_bound_ == dim_bound && sobol_count_ == count && sobol_table_.get()) {
+  // row s of the table is the s-th Sobol point whatever the table's size, so
+  // a table with at least `count` rows serves; grow in powers of two
+  if (sobol_bound_ == dim_bound && sobol_count_ >= count && sobol_table_.get()) {
     return Status::ok();
   }
+  uint32_t rows = 1;
+  while (rows < count) {
+    rows <<= 1;
+  }
+  count = rows;
   curandDirectionVectors32_t *vecs = nullptr;
   unsigned *scr = nullptr;
   if (curandGetDirectionVectors32(&vecs, CURAND_SCRAMBLED_DIRECTION_VECTORS_32_JOEKUO6) !=
@@ -489,7 +497,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
       return sr;
     }
   }
-  Status ss = prepare_sobol(st.max_sample_size, spp);
+  Status ss = prepare_sobol(st.max_sample_size, spec.sample_offset + spp);
   if (!ss.good()) {
     return ss;
   }
@@ -577,6 +585,8 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   const uint32_t n_blocks = (yb1 - yb0) * blocks_per_yblock;
   p.start_block = yb0 * blocks_per_yblock;
   p.row_lo = row_lo;
+  p.sample_offset = spec.sample_offset;
+  p.cache_depth = cache_ != nullptr ? cache_depth_ : 0u;
   p.row_hi = row_hi;
   const size_t pix0 = (size_t)row_lo * x_dim;           // first band pixel
   const size_t n_band = (size_t)(row_hi - row_lo) * x_dim;
@@ -744,6 +754,17 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   w.total_samples = first + total;
   w.sample_rgb = wf_samples_.as<float>();
   w.n_slots = n_slots;
+  if (p.cache_depth != 0 && cache_ != nullptr) {
+    if (total >= (1ull << 32)) {
+      return Status::err(PATH_ERR_UNSUPPORTED, "more than 2^32 samples with the cache");
+    }
+    PG_TRY_CUDA(cache_q_.ensure((size_t)total * 48), "cache queries");
+    PG_TRY_CUDA(cache_beta_.ensure((size_t)total * 12), "cache queries");
+    PG_TRY_CUDA(cudaMemsetAsync(cache_beta_.get(), 0, (size_t)total * 12, stream_),
+                "cache queries");
+    w.cache_q = cache_q_.as<float>();
+    w.cache_beta = cache_beta_.as<float>();
+  }
   const bool grad = adj != nullptr;
   if (grad) {
     // replay: the forward pass's per-sample radiance stays in wf_samples_
@@ -802,6 +823,18 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   }
   if (grad) {
     return Status::ok();
+  }
+  if (w.cache_q != nullptr) {
+    // the radiance cache's prediction at every path's last vertex
+    PG_TRY_CUDA(cache_pred_.ensure((size_t)total * 12), "cache predictions");
+    Status sc = cache_->infer(w.cache_q, (uint32_t)total, cache_pred_.as<float>(), stream_);
+    if (!sc.good()) {
+      return sc;
+    }
+    PG_TRY_CUDA(launch_nrc_apply(w.sample_rgb, w.cache_beta, cache_pred_.as<float>(), total,
+                                 stream_),
+                "cache apply");
+    *launches += 2;
   }
   PG_TRY_CUDA(launch_wavefront_sum(p, w.sample_rgb, n_blocks, stream_), "sample sum");
   *launches += 1;
@@ -959,6 +992,72 @@ Status Renderer::render_adjoint(const path_sample_spec &spec, const Scene &scene
   if (status != 0) {
     return Status::err(PATH_ERR_DEVICE_TIMEOUT,
                        "kernel reported device status " + std::to_string(status));
+  }
+  return Status::ok();
+}
+
+} // namespace pg
+
+namespace pg {
+
+// One frame with the radiance cache: render (paths end into the cache at
+// vertex cache_depth), then train the cache on fresh full-length paths.
+Status Renderer::render_cached(const path_sample_spec &spec, const path_output &output,
+                               const Scene &scene, uint32_t spp, const path_settings &st_in,
+                               RadianceCache &cache, uint32_t cache_depth,
+                               uint32_t train_paths, uint32_t train_steps, double *seconds) {
+  if (spec.type != PATH_SAMPLE_SQUARE_IMAGE) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the cached render takes square images");
+  }
+  if (cache_depth == 0 || cache_depth > 64) {
+    return Status::err(PATH_ERR_ARGUMENT, "cache_depth must be in [1, 64]");
+  }
+  if (st_in.traversal != PATH_TRAVERSAL_WIDE8) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the cached render traces the 8-wide BVH");
+  }
+  path_settings st = st_in;
+  st.kernel_approach = PATH_KERNEL_STREAMING;
+  st.time_kernels = 0;
+  auto t0 = std::chrono::steady_clock::now();
+  cache_ = &cache;
+  cache_depth_ = cache_depth;
+  Status sr = render(spec, output, scene, spp, st, nullptr);
+  cache_ = nullptr;
+  cache_depth_ = 0;
+  if (!sr.good()) {
+    return sr;
+  }
+  const double render_ms = stats_.kernel_ms;
+  // the cache covers the scene's box
+  const box &b = prep_.bvh.nodes.empty() ? box{} : prep_.bvh.nodes[0].aabb;
+  const float lo[3] = {b.lo.x, b.lo.y, b.lo.z}, hi[3] = {b.hi.x, b.hi.y, b.hi.z};
+  cache.set_bounds(lo, hi);
+  if (train_paths > 0 && train_steps > 0) {
+    RenderParams p = last_params_;
+    p.cache_depth = 0;
+    PG_TRY_CUDA(cache_records_.ensure((size_t)train_paths * 64), "cache records");
+    PG_TRY_CUDA(launch_nrc_paths(p, train_paths, frame_counter_++, cache_records_.as<float>(),
+                                 stream_),
+                "cache training paths");
+    PG_TRY_CUDA(cudaStreamSynchronize(stream_), "cache training paths");
+    const uint32_t per = std::max<uint32_t>(train_paths / train_steps, 1);
+    for (uint32_t k = 0; k < train_steps; ++k) {
+      const uint32_t first = k * per;
+      if (first >= train_paths) {
+        break;
+      }
+      const uint32_t cnt = std::min<uint32_t>(per, train_paths - first);
+      Status st_train = cache.train(cache_records_.as<float>() + (size_t)first * 16, cnt, nullptr);
+      if (!st_train.good()) {
+        return st_train;
+      }
+    }
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  stats_.seconds = std::chrono::duration<double>(t1 - t0).count();
+  stats_.kernel_ms = render_ms;
+  if (seconds) {
+    *seconds = stats_.seconds;
   }
   return Status::ok();
 }

@@ -120,6 +120,11 @@ public:
   Status render_adjoint(const path_sample_spec &spec, const Scene &scene, uint32_t spp,
                         const path_settings &settings, const float *d_image,
                         bool d_image_on_device, double *d_params, double *seconds);
+  // one frame with the radiance cache (render, then train it)
+  Status render_cached(const path_sample_spec &spec, const path_output &output,
+                       const Scene &scene, uint32_t spp, const path_settings &settings,
+                       class RadianceCache &cache, uint32_t cache_depth, uint32_t train_paths,
+                       uint32_t train_steps, double *seconds);
   // batched render and its launch-shape autotuner (defined in batch.cpp)
   Status render_batch(const std::vector<BatchItem> &items, const path_settings &settings,
                       const path_batch_tuning *tuning, double *seconds);
@@ -166,6 +171,10 @@ private:
                        uint32_t min_blocks, bool time_trace, uint32_t *launches,
                        const AdjointState *adj = nullptr);
   RenderParams last_params_{};
+  class RadianceCache *cache_ = nullptr; // set during a cached render
+  uint32_t cache_depth_ = 0;
+  uint32_t frame_counter_ = 0;
+  DeviceBuffer cache_q_, cache_beta_, cache_pred_, cache_records_;
   uint32_t last_blocks_ = 0;
   DeviceBuffer adj_image_, adj_dimage_, adj_params_, adj_pend_;
   cudaEvent_t trace_event(size_t i);

@@ -127,7 +127,7 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
     spp = W.scenes[scene].spp;
   }
   const uint32_t smp = (uint32_t)(local % spp);
-  s.rng.row = P.sobol + (size_t)smp * P.dim_bound;
+  s.rng.row = P.sobol + (size_t)(smp + P.sample_offset) * P.dim_bound;
   s.rng.bound = P.dim_bound;
   s.rng.dim = st.z;
   return id;
@@ -419,7 +419,25 @@ __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t p
       Hit lh = s.has_light ? unpack_hit(W.hit_light[slot]) : no_hit();
       Hit nh = s.has_next ? unpack_hit(W.hit_ext[slot]) : no_hit();
       if (!kGrad) {
-        bool cont = path_continues(W.P, s, path_step(W.P, scene_lights(W, scene), s, lh, nh));
+        StepTrace tr;
+        StepTrace *trp = W.cache_q != nullptr ? &tr : nullptr;
+        bool cont =
+            path_continues(W.P, s, path_step(W.P, scene_lights(W, scene), s, lh, nh, trp));
+        if (trp != nullptr && tr.cache_query) {
+          // the path ends into the radiance cache: its query and throughput
+          const size_t k = (size_t)(id - W.first_sample);
+          float *q = W.cache_q + 12 * k;
+          const f3 wo = -tr.in;
+          const float vals[12] = {tr.point.x, tr.point.y, tr.point.z, wo.x, wo.y, wo.z,
+                                  tr.normal.x, tr.normal.y, tr.normal.z, tr.albedo.r,
+                                  tr.albedo.g, tr.albedo.b};
+          for (int j = 0; j < 12; ++j) {
+            q[j] = vals[j];
+          }
+          W.cache_beta[3 * k] = s.multiplier.r;
+          W.cache_beta[3 * k + 1] = s.multiplier.g;
+          W.cache_beta[3 * k + 2] = s.multiplier.b;
+        }
         if (cont) {
           store_path(W, slot, s, id, scene, root);
           live = true;

@@ -77,3 +77,56 @@ def test_training_reduces_the_loss(lib):
     losses = [c.train(rec) for _ in range(200)]
     print(f"loss {losses[0]:.4f} -> {losses[-1]:.4f}")
     assert losses[-1] < 0.1 * losses[0]
+
+
+def _cornell(w, h, depth=6):
+    from path_gb300 import scenes
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(depth, "wide")
+    s.kernel_approach = 1
+    return sc, s, scenes.cornell_camera(w, h)
+
+
+def _render(r, sc, s, f2w, w, h, spp, offset=0):
+    out = np.zeros((h, w, 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w, sample_offset=offset), out, sc,
+             spp, s)
+    return out
+
+
+def test_frames_with_sample_offsets_average_to_one_render(lib):
+    """Frame f renders Sobol samples [4f, 4f + 4): the mean of frames is the
+    render of all their samples (up to the order of the float sums)."""
+    sc, s, f2w = _cornell(32, 32)
+    r = api.Renderer()
+    frames = [_render(r, sc, s, f2w, 32, 32, 4, 4 * f) for f in range(4)]
+    whole = _render(r, sc, s, f2w, 32, 32, 16)
+    np.testing.assert_allclose(np.mean(frames, 0), whole, rtol=2e-5, atol=1e-6)
+
+
+def test_trained_cache_lowers_the_error_of_a_frame(lib):
+    """What the trained network gains: after training frames, a 4-spp frame
+    whose paths end into the cache after 2 bounces is closer to a 1024-spp
+    render than a plain 4-spp frame of the same samples."""
+    w = h = 64
+    sc, s, f2w = _cornell(w, h, depth=8)
+    r = api.Renderer()
+    ref = _render(r, sc, s, f2w, w, h, 1024)
+    cache = api.RadianceCache(seed=7)
+    for f in range(40):
+        img = np.zeros((h, w, 3), np.float32)
+        r.render_cached(cache, api.SquareImage(w, h, f2w, sample_offset=1024 + 4 * f), img, sc,
+                        4, s, cache_depth=2, train_paths=1 << 14, train_steps=4)
+    spec = api.SquareImage(w, h, f2w, sample_offset=4096)
+    cached = np.zeros((h, w, 3), np.float32)
+    r.render_cached(cache, spec, cached, sc, 4, s, cache_depth=2, train_paths=0)
+    plain = np.zeros((h, w, 3), np.float32)
+    r.render(api.ExecutionModel.GPU, spec, plain, sc, 4, s)
+
+    def rel(a):
+        return float(np.linalg.norm(a - ref) / np.linalg.norm(ref))
+
+    e_plain, e_cached = rel(plain), rel(cached)
+    print(f"4-spp frame rel RMSE: plain {e_plain:.4f}, with trained cache {e_cached:.4f}")
+    assert np.isfinite(cached).all()
+    assert e_cached < e_plain
