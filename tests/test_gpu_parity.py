@@ -443,3 +443,40 @@ def test_row_band_equals_the_same_rows_of_the_whole_render(lib, case):
         assert r.stats()["device_status"] == 0
         assert np.array_equal(band[lo:hi], whole[lo:hi])
         assert np.all(band[:lo] == 7) and np.all(band[hi:] == 7)
+
+
+@pytest.mark.parametrize("case", ["empty_scene", "light_only", "one_pixel", "ragged",
+                                  "spp1", "few_dims"])
+def test_edge_cases_match_oracle(lib, oracle, case):
+    """Empty and degenerate inputs: no triangles, nothing but the light, a
+    1 x 1 image, image sizes that divide no block, one sample, and a Sobol
+    dimension bound small enough that every path wraps around it."""
+    s = scenes.path_settings(5, "binary")
+    sc = scenes.cornell_box()
+    w, h, spp = 32, 32, 8
+    if case == "empty_scene":
+        sc = api.Scene()
+        sc.add_material(api.material("Diffuse", diffuse=(0.5, 0.5, 0.5)))
+    elif case == "light_only":
+        sc = api.Scene()
+        m = sc.add_material(api.material("Diffuse", diffuse=(0.5, 0.5, 0.5),
+                                         emission=(4, 4, 4)))
+        _, lt = scenes.room_triangles()
+        sc.add_mesh(np.stack(lt).reshape(-1, 9), np.full(2, m, np.uint32))
+    elif case == "one_pixel":
+        w = h = 1
+        spp = 33
+    elif case == "ragged":
+        w, h, spp = 257, 131, 3
+    elif case == "spp1":
+        spp = 1
+    else:
+        s.max_sample_size = 8
+    f2w = scenes.cornell_camera(w, h)
+    gpu = _render_gpu(sc, s, spp, w, h, f2w)
+    ref = _render_oracle(sc, s, spp, w, h, f2w)
+    assert np.array_equal(bits(gpu), bits(ref))
+    s.kernel_approach = 1
+    s.traversal = 1
+    wave = _render_gpu(sc, s, spp, w, h, f2w)
+    assert rel_rmse(wave, ref) <= RMSE_TOL if np.linalg.norm(ref) > 0 else not wave.any()
