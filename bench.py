@@ -350,6 +350,8 @@ def main():
     ap.add_argument("--size", type=int, default=None,
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
+    ap.add_argument("--gpu-build", action="store_true",
+                    help="build the 8-wide BVH on the GPU (linear BVH) instead of the SBVH")
     ap.add_argument("--trace-min-blocks", type=int, default=0,
                     help="streaming trace kernel variant (resident blocks per SM, 3..6)")
     args = ap.parse_args()
@@ -380,6 +382,7 @@ def main():
     settings = scenes.path_settings(depth, args.traversal)
     settings.kernel_approach = 1 if args.approach == "streaming" else 0
     settings.trace_min_blocks = args.trace_min_blocks
+    settings.gpu_build = 1 if args.gpu_build else 0
     f2w = scenes.cornell_camera(w, h)
     spec = api.SquareImage(w, h, f2w)
     r = api.Renderer()
@@ -475,6 +478,8 @@ def main():
             "width": w, "height": h, "spp": spp,
             "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
             "trace_min_blocks": args.trace_min_blocks or 4,
+            "bvh": "GPU linear BVH collapsed to 8-wide" if args.gpu_build else
+                   "SBVH (host) collapsed to 8-wide",
             "l2": "flushed (512 MB write) before every timed step",
             "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),

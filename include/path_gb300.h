@@ -131,7 +131,10 @@ typedef struct {
                                 default 4); fewer registers per thread above 3 */
   uint32_t time_kernels;     /* 1: time the streaming trace launches with CUDA
                                 events (path_render_stats.trace_ms) */
-  uint32_t reserved[2];
+  uint32_t gpu_build;        /* 1: build the 8-wide BVH on the GPU (linear BVH
+                                over Morton codes, collapsed to 8-wide); the
+                                wide traversal only, no binary SBVH */
+  uint32_t reserved[1];
 } path_settings;
 
 typedef enum {

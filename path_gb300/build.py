@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["render.cu", "sobol.cu", "noalloc.cu", "wavefront.cu", "cache.cu",
-              "nrc_paths.cu"]
+              "nrc_paths.cu", "gpu_build.cu"]
 CPP_SOURCES = ["capi.cpp", "renderer.cpp", "batch.cpp", "cache_host.cpp", "scene.cpp",
                "scene_load.cpp", "sbvh.cpp", "wide.cpp", "settings.cpp"]
 

@@ -110,16 +110,17 @@ namespace dev {
 
 using tc::smem_offset;
 
-// one query row of the MLP: hash features of position, then direction,
-// normal, albedo (9 floats), zero padding to kNrcIn
-__device__ void nrc_encode(const NrcParams &C, const float *q, float *in) {
-  // q: position xyz, direction xyz, normal xyz, albedo rgb (12 floats)
+// hash features of levels [l0, l1) of a query's position (trilinear
+// interpolation of the 8 grid vertices per level) into in[2 (l - l0)] and
+// in[2 (l - l0) + 1]
+__device__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l0, uint32_t l1,
+                                  float *in) {
   float p[3];
   for (int a = 0; a < 3; ++a) {
     p[a] = (q[a] - C.lo[a]) * C.inv_extent[a];
     p[a] = fminf(fmaxf(p[a], 0.f), 1.f);
   }
-  for (uint32_t l = 0; l < kNrcLevels; ++l) {
+  for (uint32_t l = l0; l < l1; ++l) {
     const float res = C.level_res[l];
     const uint32_t side = (uint32_t)res + 1;
     float x[3], fr[3];
@@ -141,9 +142,16 @@ __device__ void nrc_encode(const NrcParams &C, const float *q, float *in) {
       f0 += w * e.x;
       f1 += w * e.y;
     }
-    in[2 * l] = f0;
-    in[2 * l + 1] = f1;
+    in[2 * (l - l0)] = f0;
+    in[2 * (l - l0) + 1] = f1;
   }
+}
+
+// one query row of the MLP (q: position, direction, normal, albedo): hash
+// features of the position, then direction, normal, albedo (9 floats), zero
+// padding to kNrcIn
+__device__ void nrc_encode(const NrcParams &C, const float *q, float *in) {
+  nrc_encode_levels(C, q, 0, kNrcLevels, in);
   for (int k = 0; k < 9; ++k) {
     in[32 + k] = q[3 + k];
   }
@@ -218,9 +226,15 @@ __device__ __forceinline__ void tc_wait(TcSync &s, uint32_t tid, uint32_t *err) 
 }
 
 // Inference: out[i] = MLP(encode(queries[i])) for i < n; persistent CTAs of
-// 128 threads over tiles of 128 queries.
-__global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const float *queries,
-                                                   uint32_t n, float *out, uint32_t *err) {
+// 512 threads over tiles of 128 queries.  The encoding is split four ways
+// (thread t: row t % 128, levels 4 (t / 128) ...), and each layer's
+// epilogue too: warp w reads tensor-memory lanes 32 (w % 4) ... (its lane
+// quarter) and columns 16 (w / 4) ... 16 (w / 4) + 15.
+constexpr uint32_t kInferThreads = 512;
+
+__global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const NrcParams C,
+                                                             const float *queries, uint32_t n,
+                                                             float *out, uint32_t *err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const floa
   unsigned char *x0 = w + kNrcWeightBytes;    // [128][kNrcIn]
   unsigned char *ha = x0 + 128 * kNrcIn * 2;  // [128][64]
   unsigned char *hb = ha + 128 * kNrcHid * 2; // [128][64]
-  copy16(w, C.w_fwd, kNrcWeightBytes, tid, 128);
+  copy16(w, C.w_fwd, kNrcWeightBytes, tid, kInferThreads);
   if (tid < 32) {
     tc::tmem_alloc(tc::smem_addr(&tmem_base), 64);
   }
@@ -239,23 +253,35 @@ __global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const floa
   tc_barrier();
   TcSync sync{tc::smem_addr(&mbar), 0, true};
   const uint32_t tmem = tmem_base;
-  const uint32_t lane_base = (tid / 32) * 32;
+  const uint32_t warp = tid / 32;
+  const uint32_t quarter = warp % 4, cgroup = warp / 4;
+  const uint32_t erow = quarter * 32 + (tid & 31); // epilogue row
+  const uint32_t qrow = tid % 128, lgroup = tid / 128; // encoding row, level group
   for (uint32_t tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
-    const uint32_t row = tid;
-    const uint32_t qi = tile * 128 + row;
-    float in[kNrcIn];
+    const uint32_t qi = tile * 128 + qrow;
+    float in[8];
+    const uint32_t l0 = lgroup * 4;
     if (qi < n) {
-      nrc_encode(C, queries + (size_t)qi * 12, in);
+      nrc_encode_levels(C, queries + (size_t)qi * 12, l0, l0 + 4, in);
     } else {
-      for (uint32_t k = 0; k < kNrcIn; ++k) {
+      for (int k = 0; k < 8; ++k) {
         in[k] = 0.f;
       }
     }
-    for (uint32_t k = 0; k < kNrcIn; ++k) {
-      store_bf16(x0, row, k, kNrcIn, in[k]);
+    for (uint32_t k = 0; k < 8; ++k) {
+      store_bf16(x0, qrow, 2 * l0 + k, kNrcIn, in[k]);
+    }
+    if (lgroup == 0) {
+      for (uint32_t k = 0; k < 9; ++k) {
+        store_bf16(x0, qrow, 32 + k, kNrcIn, qi < n ? queries[(size_t)qi * 12 + 3 + k] : 0.f);
+      }
+      for (uint32_t k = 41; k < kNrcIn; ++k) {
+        store_bf16(x0, qrow, k, kNrcIn, 0.f);
+      }
     }
     tc_barrier();
     const unsigned char *a = x0;
+    const uint32_t oi = tile * 128 + erow;
     for (uint32_t l = 0; l < kNrcLayers; ++l) {
       const uint32_t k_dim = nrc_in_dim(l), n_dim = nrc_out_dim(l);
       tc_layer(sync, tid, tmem, a, w + nrc_weight_offset(l) * 2, k_dim, n_dim, 0);
@@ -264,17 +290,18 @@ __global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const floa
         break;
       }
       unsigned char *dst = (l & 1) ? hb : ha;
-      for (uint32_t c0 = 0; c0 < n_dim; c0 += 16) {
+      const uint32_t c0 = 16 * cgroup;
+      if (c0 < n_dim) {
         float v[16];
-        tc::tmem_ld16(tmem + (lane_base << 16) + c0, v);
+        tc::tmem_ld16(tmem + ((quarter * 32) << 16) + c0, v);
         if (l + 1 < kNrcLayers) {
           for (int j = 0; j < 16; ++j) {
-            store_bf16(dst, row, c0 + j, kNrcHid, fmaxf(v[j], 0.f));
+            store_bf16(dst, erow, c0 + j, kNrcHid, fmaxf(v[j], 0.f));
           }
-        } else if (qi < n) {
-          out[(size_t)qi * 3 + 0] = v[0];
-          out[(size_t)qi * 3 + 1] = v[1];
-          out[(size_t)qi * 3 + 2] = v[2];
+        } else if (oi < n) {
+          out[(size_t)oi * 3 + 0] = v[0];
+          out[(size_t)oi * 3 + 1] = v[1];
+          out[(size_t)oi * 3 + 2] = v[2];
         }
       }
       tc_barrier();
@@ -290,7 +317,6 @@ __global__ void __launch_bounds__(128) k_nrc_infer(const NrcParams C, const floa
     tc::tmem_dealloc(tmem, 64);
   }
 }
-
 
 // Training on tiles of 128 records (query: 12 floats, target: 3 floats,
 // padding: 1).  Forward as in inference, keeping each layer's input
@@ -564,7 +590,7 @@ cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t 
   if (e != cudaSuccess || n == 0) {
     return e;
   }
-  dev::k_nrc_infer<<<grid, 128, smem, s>>>(c, queries, n, out, err);
+  dev::k_nrc_infer<<<grid, dev::kInferThreads, smem, s>>>(c, queries, n, out, err);
   return cudaGetLastError();
 }
 

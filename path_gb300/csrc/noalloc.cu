@@ -222,7 +222,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   stats_.gpu_launches = launches;
   stats_.device_status = dev_status;
   stats_.num_bvh_nodes = (uint32_t)prep_.bvh.nodes.size();
-  stats_.num_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  stats_.num_wide_nodes = prep_.n_wide_nodes;
   if (seconds) {
     *seconds = stats_.seconds;
   }

@@ -1,6 +1,7 @@
 // render::Renderer for the GPU execution model (see renderer.h).
 #include "renderer.h"
 #include "cache_host.h"
+#include "gpu_build.h"
 
 #include <curand.h>
 
@@ -213,6 +214,111 @@ Status Renderer::upload_geometry(const FlatScene &flat,
   return Status::ok();
 }
 
+// box of all vertices (the radiance cache and the GPU builder use it)
+void scene_box(const FlatScene &flat, float *lo, float *hi) {
+  box b = empty_box();
+  for (size_t i = 0; i < flat.v0.size(); ++i) {
+    b = grow(grow(grow(b, flat.v0[i]), flat.v1[i]), flat.v2[i]);
+  }
+  if (flat.v0.empty()) {
+    b.lo = mk(0.f, 0.f, 0.f);
+    b.hi = mk(0.f, 0.f, 0.f);
+  }
+  lo[0] = b.lo.x;
+  lo[1] = b.lo.y;
+  lo[2] = b.lo.z;
+  hi[0] = b.hi.x;
+  hi[1] = b.hi.y;
+  hi[2] = b.hi.z;
+}
+
+// The 8-wide BVH from the GPU builder; the BVH-order triangle and shading
+// arrays are gathered on the host with its permutation, as for the SBVH.
+Status Renderer::prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t version,
+                                   const std::vector<path_material> &mats) {
+  prep_.valid = false;
+  auto t0 = std::chrono::steady_clock::now();
+  const size_t n = flat.v0.size();
+  scene_box(flat, prep_.lo, prep_.hi);
+  std::vector<float> t9(n * 9);
+  for (size_t i = 0; i < n; ++i) {
+    const f3 v[3] = {flat.v0[i], flat.v1[i], flat.v2[i]};
+    for (int k = 0; k < 3; ++k) {
+      t9[9 * i + 3 * k] = v[k].x;
+      t9[9 * i + 3 * k + 1] = v[k].y;
+      t9[9 * i + 3 * k + 2] = v[k].z;
+    }
+  }
+  DeviceBuffer d9;
+  PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, stream_), "gpu build upload");
+  GpuWideBVH g;
+  Status sb = gpu_build_wide(d9.as<float>(), (uint32_t)n, prep_.lo, prep_.hi, stream_, g);
+  if (!sb.good()) {
+    return sb;
+  }
+  prep_.bvh = BinaryBVH{};
+  prep_.bvh.permutation.resize(n);
+  if (n > 0) {
+    PG_TRY_CUDA(cudaMemcpyAsync(prep_.bvh.permutation.data(), g.perm.get(), n * 4,
+                                cudaMemcpyDeviceToHost, stream_),
+                "gpu build permutation");
+  }
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "gpu build");
+  prep_.wide = WideBVH{};
+  prep_.wide.depth = g.depth;
+  prep_.n_wide_nodes = g.n_nodes;
+  wide_nodes_.swap(g.nodes);
+  wide_tris_.swap(g.wide_tris);
+  prep_.orig_to_bvh.assign(n, 0u);
+  for (size_t i = 0; i < n; ++i) {
+    prep_.orig_to_bvh[prep_.bvh.permutation[i]] = (uint32_t)i;
+  }
+  prep_.build_seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  prep_.scene_id = id;
+  prep_.scene_version = version;
+  prep_.gpu_built = true;
+  // BVH-order triangles and shading data; materials and lights
+  PG_TRY_CUDA(st_tris_.ensure(n * 48), "staging");
+  PG_TRY_CUDA(st_data_.ensure(n * 48), "staging");
+  PG_TRY_CUDA(st_mats_.ensure(mats.size() * sizeof(DevMaterial)), "staging");
+  PG_TRY_CUDA(st_lights_.ensure(flat.light_v0.size() * 48), "staging");
+  PG_TRY_CUDA(st_cdf_.ensure(flat.light_cdf.size() * 4), "staging");
+  PG_TRY_CUDA(st_perm_.ensure(n * 4), "staging");
+  for (PinnedBuffer *b : {&st_nodes_, &st_extra_, &st_wnodes_, &st_wtris_}) {
+    PG_TRY_CUDA(b->ensure(0), "staging");
+  }
+  float *tris = st_tris_.as<float>();
+  float *data = st_data_.as<float>();
+  for (size_t i = 0; i < n; ++i) {
+    const uint32_t o = prep_.bvh.permutation[i];
+    put_tri(&tris[12 * i], flat.v0[o], flat.v1[o], flat.v2[o], 0);
+    float d[12] = {flat.n0[o].x, flat.n0[o].y, flat.n0[o].z, flat.n1[o].x,
+                   flat.n1[o].y, flat.n1[o].z, flat.n2[o].x, flat.n2[o].y,
+                   flat.n2[o].z, 0.f, 0.f, 0.f};
+    std::memcpy(&d[11], &flat.material[o], sizeof(uint32_t));
+    std::memcpy(&data[12 * i], d, sizeof(d));
+  }
+  stage_materials(flat, mats);
+  if (n > 0) {
+    std::memcpy(st_perm_.get(), prep_.bvh.permutation.data(), n * 4);
+  }
+  struct Pair {
+    DeviceBuffer *dev;
+    PinnedBuffer *host;
+  };
+  Pair pairs[] = {{&tris_, &st_tris_},         {&tri_data_, &st_data_},
+                  {&materials_, &st_mats_},    {&light_tris_, &st_lights_},
+                  {&light_cdf_, &st_cdf_},     {&perm_, &st_perm_}};
+  for (const Pair &pr : pairs) {
+    PG_TRY_CUDA(pr.dev->upload(pr.host->get(), pr.host->bytes, stream_), "scene upload");
+  }
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "upload sync");
+  prep_.n_tris = (uint32_t)n;
+  prep_.n_lights = (uint32_t)flat.light_v0.size();
+  return Status::ok();
+}
+
 // materials and the light table (which depends on emission) into staging
 void Renderer::stage_materials(const FlatScene &flat, const std::vector<path_material> &mats) {
   DevMaterial *dm = st_mats_.as<DevMaterial>();
@@ -275,9 +381,12 @@ Status Renderer::prepare_scene(const FlatScene &flat, uint64_t id, uint64_t vers
     return Status::ok();
   }
   prep_.valid = false;
+  prep_.gpu_built = false;
   auto t0 = std::chrono::steady_clock::now();
   prep_.bvh = build_sbvh(flat.v0.data(), flat.v1.data(), flat.v2.data(), flat.v0.size(), sbvh);
   prep_.wide = build_wide(prep_.bvh);
+  prep_.n_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  scene_box(flat, prep_.lo, prep_.hi);
   prep_.orig_to_bvh.assign(prep_.bvh.permutation.size(), 0u);
   for (size_t i = 0; i < prep_.bvh.permutation.size(); ++i) {
     prep_.orig_to_bvh[prep_.bvh.permutation[i]] = (uint32_t)i;
@@ -333,7 +442,7 @@ void Renderer::fill_params(RenderParams &p) const {
   p.wide_tris = wide_tris_.as<const float4>();
   p.n_tris = prep_.n_tris;
   p.n_bin_nodes = (uint32_t)prep_.bvh.nodes.size();
-  p.n_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  p.n_wide_nodes = prep_.n_wide_nodes;
   p.materials = materials_.as<const DevMaterial>();
   p.light_tris = light_tris_.as<const float4>();
   p.light_cdf = light_cdf_.as<const float>();
@@ -360,6 +469,10 @@ cudaEvent_t Renderer::trace_event(size_t i) {
 Status Renderer::traversal_fits(const path_settings &st) const {
   if (st.traversal == PATH_TRAVERSAL_WIDE8 && prep_.wide.depth + 1 > kWideStackDepth) {
     return Status::err(PATH_ERR_UNSUPPORTED, "wide BVH deeper than the traversal stack");
+  }
+  if (st.traversal == PATH_TRAVERSAL_BINARY && prep_.gpu_built) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the resident BVH came from the GPU builder, "
+                                             "which makes no binary BVH");
   }
   if (st.traversal == PATH_TRAVERSAL_BINARY) {
     if (prep_.bvh.depth + 2 > 64) {
@@ -458,13 +571,26 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   sb.use_spatial_splits = st.use_spatial_splits != 0;
   sb.traversal_per_intersect_cost = st.traversal_per_intersect_cost;
   sb.target_objects = st.target_objects;
+  const bool gpu_build = st.gpu_build != 0;
+  if (gpu_build && st.traversal != PATH_TRAVERSAL_WIDE8) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "the GPU builder makes the 8-wide BVH only");
+  }
   bool rebuilt = !(prep_.valid && prep_.scene_id == scene.id &&
-                   prep_.scene_version == scene.version &&
+                   prep_.gpu_built == gpu_build && prep_.scene_version == scene.version &&
                    prep_.sbvh.overlap_threshold == sb.overlap_threshold &&
                    prep_.sbvh.use_spatial_splits == sb.use_spatial_splits &&
                    prep_.sbvh.traversal_per_intersect_cost == sb.traversal_per_intersect_cost &&
                    prep_.sbvh.target_objects == sb.target_objects);
-  if (rebuilt) {
+  if (rebuilt && gpu_build) {
+    FlatScene flat = flatten(scene);
+    Status sp = prepare_scene_gpu(flat, scene.id, scene.version, scene.materials);
+    if (!sp.good()) {
+      return sp;
+    }
+    prep_.sbvh = sb;
+    prep_.material_version = scene.material_version;
+    prep_.valid = true;
+  } else if (rebuilt) {
     FlatScene flat = flatten(scene);
     Status sp = prepare_scene(flat, scene.id, scene.version, sb, true);
     if (!sp.good()) {
@@ -684,7 +810,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   stats_.gpu_launches = launches;
   stats_.device_status = status;
   stats_.num_bvh_nodes = (uint32_t)prep_.bvh.nodes.size();
-  stats_.num_wide_nodes = (uint32_t)prep_.wide.nodes.size();
+  stats_.num_wide_nodes = prep_.n_wide_nodes;
   stats_.h2d_bytes = h2d + spec_h2d;
   stats_.d2h_bytes = d2h;
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
@@ -865,15 +991,25 @@ Status Renderer::intersect(const float *tris, uint32_t n_tris, const float *rays
   sb.traversal_per_intersect_cost = st.traversal_per_intersect_cost;
   sb.target_objects = st.target_objects;
   prep_.valid = false;
-  Status sp = prepare_scene(flat, 0, 0, sb, true);
-  if (!sp.good()) {
-    return sp;
-  }
   std::vector<path_material> mats(1);
   std::memset(mats.data(), 0, sizeof(path_material));
-  Status su = upload_geometry(flat, mats);
-  if (!su.good()) {
-    return su;
+  if (st.gpu_build) {
+    if (st.traversal != PATH_TRAVERSAL_WIDE8) {
+      return Status::err(PATH_ERR_UNSUPPORTED, "the GPU builder makes the 8-wide BVH only");
+    }
+    Status sp = prepare_scene_gpu(flat, 0, 0, mats);
+    if (!sp.good()) {
+      return sp;
+    }
+  } else {
+    Status sp = prepare_scene(flat, 0, 0, sb, true);
+    if (!sp.good()) {
+      return sp;
+    }
+    Status su = upload_geometry(flat, mats);
+    if (!su.good()) {
+      return su;
+    }
   }
   Status sf = traversal_fits(st);
   if (!sf.good()) {
@@ -1029,9 +1165,7 @@ Status Renderer::render_cached(const path_sample_spec &spec, const path_output &
   }
   const double render_ms = stats_.kernel_ms;
   // the cache covers the scene's box
-  const box &b = prep_.bvh.nodes.empty() ? box{} : prep_.bvh.nodes[0].aabb;
-  const float lo[3] = {b.lo.x, b.lo.y, b.lo.z}, hi[3] = {b.hi.x, b.hi.y, b.hi.z};
-  cache.set_bounds(lo, hi);
+  cache.set_bounds(prep_.lo, prep_.hi);
   if (train_paths > 0 && train_steps > 0) {
     RenderParams p = last_params_;
     p.cache_depth = 0;

@@ -15,6 +15,7 @@
 
 #include <array>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace pg {
@@ -28,6 +29,10 @@ public:
   cudaError_t ensure(size_t bytes);
   cudaError_t upload(const void *src, size_t bytes, cudaStream_t s);
   void release();
+  void swap(DeviceBuffer &o) {
+    std::swap(ptr_, o.ptr_);
+    std::swap(size_, o.size_);
+  }
   void *get() const { return ptr_; }
   template <typename T> T *as() const { return static_cast<T *>(ptr_); }
   size_t size() const { return size_; }
@@ -73,6 +78,9 @@ struct PreparedScene {
   BinaryBVH bvh;
   WideBVH wide;
   std::vector<uint32_t> orig_to_bvh; // inverse of bvh.permutation
+  bool gpu_built = false;            // wide BVH from the GPU builder (no binary BVH)
+  uint32_t n_wide_nodes = 0;
+  float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}; // scene box
   uint32_t n_tris = 0, n_lights = 0;
   double build_seconds = 0.0;
 };
@@ -84,6 +92,9 @@ DevMaterial to_dev(const path_material &m);
 void put_tri(float *dst, f3 v0, f3 v1, f3 v2, uint32_t extra_bits);
 // settings every render accepts (enum ranges, supported RNG, bounds)
 Status check_settings(const path_settings &s);
+
+// box of all vertices of a flattened scene
+void scene_box(const FlatScene &flat, float *lo, float *hi);
 
 // one image of a batched render (path_batch_item)
 struct BatchItem {
@@ -144,6 +155,8 @@ private:
   Status copy_staged(uint64_t *bytes);
   void stage_materials(const FlatScene &flat, const std::vector<path_material> &mats);
   Status refresh_materials(const Scene &scene, uint64_t *bytes);
+  Status prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t version,
+                           const std::vector<path_material> &mats);
   Status prepare_sobol(uint32_t dim_bound, uint32_t count);
   void fill_params(RenderParams &p) const;
   Status traversal_fits(const path_settings &st) const;

@@ -480,3 +480,45 @@ def test_edge_cases_match_oracle(lib, oracle, case):
     s.traversal = 1
     wave = _render_gpu(sc, s, spp, w, h, f2w)
     assert rel_rmse(wave, ref) <= RMSE_TOL if np.linalg.norm(ref) > 0 else not wave.any()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 37, 5000])
+def test_gpu_built_wide_bvh_finds_the_order_independent_closest_hit(lib, oracle, n):
+    """The GPU builder (linear BVH collapsed to 8-wide): the same closest hit
+    as a brute-force search, ties by smallest BVH-order index."""
+    rng = np.random.default_rng(n)
+    tris = rng.uniform(-1, 1, (n, 9)).astype(np.float32)
+    rays = _random_rays(rng, -1, 1, 3000)
+    s = api.Settings()
+    s.traversal = 1
+    s.gpu_build = 1
+    got, gt = api.Renderer().intersect(tris, rays, s)
+    want, wt = ol.loop_all(tris, rays)
+    hit = want >= 0
+    assert np.array_equal(hit, got >= 0)
+    assert np.array_equal(bits(wt[hit]), bits(gt[hit]))
+    tie = np.abs(wt - gt) <= 1e-6
+    assert np.all((want == got) | (hit & tie))
+
+
+@pytest.mark.parametrize("case", ["cornell", "large_mesh"])
+def test_gpu_built_bvh_renders_the_same_image(lib, case):
+    """Images through the GPU-built BVH equal those through the host SBVH
+    (both through the order-independent 8-wide traversal)."""
+    if case == "cornell":
+        sc, w, h, depth, spp = scenes.cornell_box(), 64, 64, 5, 16
+    else:
+        sc, w, h, depth, spp = scenes.large_mesh_room(6, 40, 40), 64, 64, 8, 4
+    s = scenes.path_settings(depth, "wide")
+    s.kernel_approach = 1
+    f2w = scenes.cornell_camera(w, h)
+    host_built = _render_gpu(sc, s, spp, w, h, f2w)
+    s.gpu_build = 1
+    r = api.Renderer()
+    out = np.zeros((h, w, 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), out, sc, spp, s)
+    st = r.stats()
+    assert st["device_status"] == 0
+    print(f"{case}: gpu build {1e3 * st['bvh_build_seconds']:.1f} ms, "
+          f"{st['num_wide_nodes']} wide nodes, rel RMSE {rel_rmse(out, host_built):.2e}")
+    assert rel_rmse(out, host_built) <= RMSE_TOL
