@@ -287,13 +287,25 @@ def run_cache(args, rank, world, local_rank):
         wall, frames, err = 0.0, 0, None
         curve = []
         base = 64 * ref_frames  # samples the reference did not use
+        if cached and args.pretrain_frames > 0:
+            # training-only frames (their images are not kept; time counted)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for f in range(args.pretrain_frames):
+                spec = api.SquareImage(w, h, f2w, sample_offset=base + 4 * (args.max_frames + f))
+                r.render_cached(cache, spec, out, scene, 4, settings,
+                                cache_depth=args.cache_depth, train_paths=args.train_paths,
+                                train_steps=args.train_steps)
+            torch.cuda.synchronize()
+            wall += time.perf_counter() - t
         while frames < args.max_frames:
             spec = api.SquareImage(w, h, f2w, sample_offset=base + 4 * frames)
             torch.cuda.synchronize()
             t = time.perf_counter()
             if cached:
-                r.render_cached(cache, spec, out, scene, 4, settings, cache_depth=2,
-                                train_paths=1 << 16, train_steps=4)
+                r.render_cached(cache, spec, out, scene, 4, settings,
+                                cache_depth=args.cache_depth, train_paths=args.train_paths,
+                                train_steps=args.train_steps)
             else:
                 r.render(api.ExecutionModel.GPU, spec, out, scene, 4, settings)
             torch.cuda.synchronize()
@@ -316,8 +328,9 @@ def run_cache(args, rank, world, local_rank):
         "n_gpus": 1, "dtype": "f32 render, bf16 cache MLP", "data": "synthetic",
         "config": {"workload": f"{desc} in 4-spp frames; reference 4096 spp FP64",
                    "cache": "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
-                            "paths end into the cache after 2 bounces, 2^16 records x 4 steps "
-                            "per frame"},
+                            f"paths end into the cache at vertex {args.cache_depth}, "
+                            f"{args.train_paths} records x {args.train_steps} steps per frame, "
+                            f"{args.pretrain_frames} training-only frames first"},
         "plain": plain, "cached": cached,
         "ratio_cached_over_plain": (cached["seconds"] / plain["seconds"]
                                     if plain["reached"] and cached["reached"] else None),
@@ -337,6 +350,14 @@ def main():
                     choices=["large_mesh", "cornell", "batched", "cache"])
     ap.add_argument("--max-frames", type=int, default=400,
                     help="cache workload: frames before giving up on the error target")
+    ap.add_argument("--cache-depth", type=int, default=2,
+                    help="cache workload: the vertex where paths end into the cache")
+    ap.add_argument("--train-paths", type=int, default=1 << 16,
+                    help="cache workload: training records per frame")
+    ap.add_argument("--train-steps", type=int, default=4,
+                    help="cache workload: Adam steps per frame")
+    ap.add_argument("--pretrain-frames", type=int, default=0,
+                    help="cache workload: training-only frames before the first image")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: scene count")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
@@ -350,6 +371,8 @@ def main():
     ap.add_argument("--size", type=int, default=None,
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
+    ap.add_argument("--slots-log2", type=int, default=0,
+                    help="streaming: paths in flight = 2^this (0 = default 21)")
     ap.add_argument("--gpu-build", action="store_true",
                     help="build the 8-wide BVH on the GPU (linear BVH) instead of the SBVH")
     ap.add_argument("--trace-min-blocks", type=int, default=0,
@@ -383,6 +406,7 @@ def main():
     settings.kernel_approach = 1 if args.approach == "streaming" else 0
     settings.trace_min_blocks = args.trace_min_blocks
     settings.gpu_build = 1 if args.gpu_build else 0
+    settings.wavefront_slots_log2 = args.slots_log2
     f2w = scenes.cornell_camera(w, h)
     spec = api.SquareImage(w, h, f2w)
     r = api.Renderer()
@@ -478,6 +502,7 @@ def main():
             "width": w, "height": h, "spp": spp,
             "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
             "trace_min_blocks": args.trace_min_blocks or 4,
+            "slots_log2": args.slots_log2 or 21,
             "bvh": "GPU linear BVH collapsed to 8-wide" if args.gpu_build else
                    "SBVH (host) collapsed to 8-wide",
             "l2": "flushed (512 MB write) before every timed step",

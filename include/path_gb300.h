@@ -134,7 +134,8 @@ typedef struct {
   uint32_t gpu_build;        /* 1: build the 8-wide BVH on the GPU (linear BVH
                                 over Morton codes, collapsed to 8-wide); the
                                 wide traversal only, no binary SBVH */
-  uint32_t reserved[1];
+  uint32_t wavefront_slots_log2; /* streaming: paths in flight = 2^this
+                                    (10..24, 0 = default 21) */
 } path_settings;
 
 typedef enum {

@@ -43,7 +43,7 @@ class PathSettings(ctypes.Structure):
                 ("back_cull_emission", c_u32), ("traversal", c_u32),
                 ("persistent_ctas_per_sm", c_u32), ("count_work", c_u32),
                 ("upload_scene_every_render", c_u32), ("trace_min_blocks", c_u32),
-                ("time_kernels", c_u32), ("gpu_build", c_u32), ("reserved", c_u32 * 1)]
+                ("time_kernels", c_u32), ("gpu_build", c_u32), ("wavefront_slots_log2", c_u32)]
 
 
 class SampleSpec(ctypes.Structure):

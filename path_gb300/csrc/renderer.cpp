@@ -505,6 +505,9 @@ Status check_settings(const path_settings &s) {
   if (s.target_objects == 0 || s.target_objects > 10) {
     return Status::err(PATH_ERR_ARGUMENT, "target_objects must be in [1, 10]");
   }
+  if (s.wavefront_slots_log2 != 0 && (s.wavefront_slots_log2 < 10 || s.wavefront_slots_log2 > 24)) {
+    return Status::err(PATH_ERR_ARGUMENT, "wavefront_slots_log2 must be 0 or in [10, 24]");
+  }
   return Status::ok();
 }
 
@@ -724,6 +727,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
+    slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 21u;
     Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks,
                               st.time_kernels != 0, &launches);
     if (!sw.good()) {
@@ -839,6 +843,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
 Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool counting,
                                uint32_t min_blocks, bool time_trace, uint32_t *launches,
                                const AdjointState *adj) {
+  const uint32_t slots_log2 = slots_log2_;
   trace_timed_ = 0;
   trace_launches_ = 0;
   if (num_sms_ == 0) {
@@ -850,7 +855,7 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   const unsigned long long first = (unsigned long long)p.row_lo * p.x_dim * p.spp;
   const unsigned long long total =
       (unsigned long long)(p.row_hi - p.row_lo) * p.x_dim * p.spp;
-  const uint32_t n_slots = (uint32_t)std::min<unsigned long long>(total, 1ull << 21);
+  const uint32_t n_slots = (uint32_t)std::min<unsigned long long>(total, 1ull << slots_log2);
   auto a256 = [](size_t n) { return (n + 255) & ~size_t(255); };
   const size_t f4 = a256((size_t)n_slots * 16), u2 = a256((size_t)n_slots * 8),
                u1 = a256((size_t)n_slots * 4);

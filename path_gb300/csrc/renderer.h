@@ -184,6 +184,7 @@ private:
                        uint32_t min_blocks, bool time_trace, uint32_t *launches,
                        const AdjointState *adj = nullptr);
   RenderParams last_params_{};
+  uint32_t slots_log2_ = 21; // paths in flight of the streaming render, log2
   class RadianceCache *cache_ = nullptr; // set during a cached render
   uint32_t cache_depth_ = 0;
   uint32_t frame_counter_ = 0;
