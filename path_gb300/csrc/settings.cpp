@@ -385,7 +385,9 @@ bool settings_from_yaml_text(const std::string &text, path_settings &s,
     if (!read_u32(get(g, "persistent_ctas_per_sm"), s.persistent_ctas_per_sm, err) ||
         !read_u32(get(g, "trace_min_blocks"), s.trace_min_blocks, err) ||
         !read_bool(get(g, "count_work"), s.count_work, err) ||
-        !read_bool(get(g, "time_kernels"), s.time_kernels, err)) {
+        !read_bool(get(g, "time_kernels"), s.time_kernels, err) ||
+        !read_bool(get(g, "gpu_build"), s.gpu_build, err) ||
+        !read_u32(get(g, "wavefront_slots_log2"), s.wavefront_slots_log2, err)) {
       return false;
     }
   }

@@ -72,6 +72,11 @@ settings:
     value: {sequence_settings: {}, max_sample_size: 128}
   rendering_equation_settings:
     back_cull_emission: false
+  gb300:
+    traversal: Wide8
+    trace_min_blocks: 5
+    gpu_build: true
+    wavefront_slots_log2: 22
 """
     p = tmp_path / "cfg.yaml"
     p.write_text(text)
@@ -85,6 +90,8 @@ settings:
     assert s.binary_search_threshold == 100
     assert s.term_prob == capi.TERM["NIters"] and s.term_prob_iters == 4
     assert s.max_sample_size == 128 and s.back_cull_emission == 0
+    assert s.traversal == 1 and s.trace_min_blocks == 5 and s.gpu_build == 1
+    assert s.wavefront_slots_log2 == 22
     bad = tmp_path / "bad.yaml"
     bad.write_text("settings:\n  term_prob:\n    type: Nope\n")
     with pytest.raises(capi.PathError) as e:
