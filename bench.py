@@ -196,6 +196,7 @@ def run_batched(args, rank, world, local_rank):
     batch = scenes.batch_scenes(args.scenes, seed=0)
     gen_s = time.time() - t0
     settings = scenes.path_settings(6, "wide")
+    settings.gpu_build = 1 if args.gpu_build else 0
     outs = [np.zeros((h, w, 3), np.float32) for _, w, h, _ in batch]
     items = [(sc, api.SquareImage(w, h, scenes.cornell_camera(w, h)), o, spp)
              for (sc, w, h, spp), o in zip(batch, outs)]
@@ -237,6 +238,7 @@ def run_batched(args, rank, world, local_rank):
         "config": {"workload": f"batched: {len(batch)} seeded scenes, {tris} triangles, "
                                f"{samples} samples, depth 6",
                    "tuning": tuning, "l2": "flushed (512 MB write) before every timed step",
+                   "bvh": "GPU linear BVH" if args.gpu_build else "SBVH (host)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * samples * args.steps / e2e_total / 1e6, "unit": METRIC,
                 "h2d_bytes_per_step": 0,

@@ -355,7 +355,7 @@ typedef struct {
  * (bit for bit); they only change speed.  Zero fields take the defaults in
  * brackets. */
 typedef struct {
-  uint32_t slots_log2;          /* paths in flight = 2^slots_log2 [21] */
+  uint32_t slots_log2;          /* paths in flight = 2^slots_log2 [23] */
   uint32_t trace_min_blocks;    /* trace kernel variant, 3..6 [4] */
   uint32_t shade_ctas_per_sm;   /* shade grid = SMs x this [4] */
   uint32_t iterations_per_graph; /* trace/shade iterations per CUDA-graph

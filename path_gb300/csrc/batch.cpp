@@ -16,6 +16,7 @@
 // whatever the launch shape, which is what lets the autotuner pick shapes
 // by time alone.
 #include "renderer.h"
+#include "gpu_build.h"
 
 #include <omp.h>
 
@@ -29,7 +30,7 @@ namespace pg {
 
 namespace {
 
-constexpr uint32_t kDefaultSlotsLog2 = 21;
+constexpr uint32_t kDefaultSlotsLog2 = 23;
 constexpr uint32_t kDefaultTraceMinBlocks = 4;
 constexpr uint32_t kDefaultShadeCtas = 4;
 constexpr uint32_t kDefaultItersPerGraph = 4;
@@ -117,13 +118,15 @@ Status Renderer::check_batch(const std::vector<BatchItem> &items,
   return Status::ok();
 }
 
-Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb) {
+Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb,
+                               bool gpu_build) {
   std::vector<std::array<uint64_t, 3>> key;
   key.reserve(items.size());
   for (const BatchItem &it : items) {
     key.push_back({it.scene->id, it.scene->version, it.scene->material_version});
   }
-  if (batch_.valid && batch_.key == key && same_sbvh(batch_.sbvh, sb)) {
+  if (batch_.valid && batch_.key == key && same_sbvh(batch_.sbvh, sb) &&
+      batch_.gpu_build == gpu_build) {
     return Status::ok();
   }
   batch_.valid = false;
@@ -152,10 +155,62 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
     try {
       FlatScene &f = flats[(size_t)i];
       f = flatten(*items[(size_t)i].scene);
-      bvhs[(size_t)i] = build_sbvh(f.v0.data(), f.v1.data(), f.v2.data(), f.v0.size(), sb);
-      wides[(size_t)i] = build_wide(bvhs[(size_t)i]);
+      if (!gpu_build) {
+        bvhs[(size_t)i] = build_sbvh(f.v0.data(), f.v1.data(), f.v2.data(), f.v0.size(), sb);
+        wides[(size_t)i] = build_wide(bvhs[(size_t)i]);
+      }
     } catch (const std::exception &e) {
       errors[(size_t)i] = e.what();
+    }
+  }
+  if (gpu_build) {
+    // one GPU build per distinct scene; its wide nodes, leaf references and
+    // permutation come back for the arena assembly below
+    for (size_t i = 0; i < n; ++i) {
+      if (first_of[i] != i || !errors[i].empty()) {
+        continue;
+      }
+      const FlatScene &f = flats[i];
+      const size_t nt = f.v0.size();
+      std::vector<float> t9(nt * 9);
+      for (size_t k = 0; k < nt; ++k) {
+        const f3 v[3] = {f.v0[k], f.v1[k], f.v2[k]};
+        for (int c = 0; c < 3; ++c) {
+          t9[9 * k + 3 * c] = v[c].x;
+          t9[9 * k + 3 * c + 1] = v[c].y;
+          t9[9 * k + 3 * c + 2] = v[c].z;
+        }
+      }
+      float lo[3], hi[3];
+      scene_box(f, lo, hi);
+      DeviceBuffer d9;
+      PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, stream_), "gpu build upload");
+      GpuWideBVH g;
+      Status sg = gpu_build_wide(d9.as<float>(), (uint32_t)nt, lo, hi, stream_, g);
+      if (!sg.good()) {
+        return sg;
+      }
+      WideBVH &w = wides[i];
+      w.nodes.resize(g.n_nodes);
+      w.depth = g.depth;
+      std::vector<float> wt(nt * 12);
+      bvhs[i].permutation.resize(nt);
+      if (nt > 0) {
+        PG_TRY_CUDA(cudaMemcpyAsync(w.nodes.data(), g.nodes.get(), g.n_nodes * sizeof(WideNode),
+                                    cudaMemcpyDeviceToHost, stream_),
+                    "gpu build download");
+        PG_TRY_CUDA(cudaMemcpyAsync(wt.data(), g.wide_tris.get(), nt * 48,
+                                    cudaMemcpyDeviceToHost, stream_),
+                    "gpu build download");
+        PG_TRY_CUDA(cudaMemcpyAsync(bvhs[i].permutation.data(), g.perm.get(), nt * 4,
+                                    cudaMemcpyDeviceToHost, stream_),
+                    "gpu build download");
+      }
+      PG_TRY_CUDA(cudaStreamSynchronize(stream_), "gpu build download");
+      w.tri_index.resize(nt);
+      for (size_t k = 0; k < nt; ++k) {
+        std::memcpy(&w.tri_index[k], &wt[12 * k + 9], 4);
+      }
     }
   }
   for (size_t i = 0; i < n; ++i) {
@@ -262,6 +317,7 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
   batch_.total_tris = tris;
   batch_.key = key;
   batch_.sbvh = sb;
+  batch_.gpu_build = gpu_build;
   batch_.build_seconds =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   batch_.valid = true;
@@ -593,7 +649,7 @@ Status Renderer::render_batch(const std::vector<BatchItem> &items, const path_se
     return s0;
   }
   auto t0 = std::chrono::steady_clock::now();
-  Status sp = prepare_batch(items, sbvh_of(st));
+  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build != 0);
   if (!sp.good()) {
     return sp;
   }
@@ -625,7 +681,7 @@ Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_
   if (!s0.good()) {
     return s0;
   }
-  Status sp = prepare_batch(items, sbvh_of(st));
+  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build != 0);
   if (!sp.good()) {
     return sp;
   }
@@ -637,7 +693,7 @@ Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_
   path_settings quiet = st;
   quiet.count_work = 0;
   // candidates: paths in flight x trace occupancy x shade grid
-  const uint32_t slots[] = {20, 21, 22};
+  const uint32_t slots[] = {21, 22, 23, 24};
   const uint32_t mins[] = {3, 4, 5};
   const uint32_t shades[] = {2, 4, 8};
   path_batch_tuning best = resolved(nullptr);

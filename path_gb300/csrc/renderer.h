@@ -109,6 +109,7 @@ struct PreparedBatch {
   bool valid = false;
   std::vector<std::array<uint64_t, 3>> key; // (scene id, version, material version)
   SBVHSettings sbvh;
+  bool gpu_build = false;
   std::vector<uint32_t> root, light_off, n_lights, n_tris;
   uint32_t n_wide_nodes = 0;
   uint64_t total_tris = 0;
@@ -198,7 +199,8 @@ private:
   path_render_stats stats_{};
   // batched render
   Status check_batch(const std::vector<BatchItem> &items, const path_settings &st) const;
-  Status prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb);
+  Status prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb,
+                       bool gpu_build);
   Status run_batch(const std::vector<BatchItem> &items, const path_settings &st,
                    const path_batch_tuning &tu, uint64_t sample_limit, bool with_images,
                    float *kernel_ms, uint32_t *launches);
