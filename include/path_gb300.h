@@ -135,7 +135,7 @@ typedef struct {
                                 over Morton codes, collapsed to 8-wide); the
                                 wide traversal only, no binary SBVH */
   uint32_t wavefront_slots_log2; /* streaming: paths in flight = 2^this
-                                    (10..24, 0 = default 21) */
+                                    (10..24, 0 = default 24) */
 } path_settings;
 
 typedef enum {

@@ -18,6 +18,7 @@
 #include <iterator>
 #include <limits>
 #include <optional>
+#include <random>
 #include <unordered_map>
 #include <unordered_set>
 #include <vector>
@@ -909,11 +910,22 @@ bool sobol_table(unsigned dimension_bound, unsigned count, SobolTable &out) {
   return true;
 }
 
+// Sobel (table) or Uniform: include/rng/uniform/uniform.h:18-76 on the CPU
+// execution model, std::mt19937 seeded with sample + location x samples_per
+// and std::uniform_real_distribution<float>(0, 1).  (The reference's GPU
+// execution model draws cuRAND XORWOW for Uniform, so its two models give
+// different images; they agree in expectation.)
 struct RngState {
   const SobolTable *table;
   unsigned sample;
   unsigned dim;
+  bool uniform = false;
+  std::mt19937 gen;
+  std::uniform_real_distribution<float> dist{0.f, 1.f};
   float next() {
+    if (uniform) {
+      return dist(gen);
+    }
     float out = table->vals[(size_t)sample * table->dimension_bound + dim];
     ++dim;
     dim %= table->dimension_bound;
@@ -921,9 +933,17 @@ struct RngState {
   }
 };
 
-RngState get_generator(const SobolTable &t, unsigned sample_idx,
-                       unsigned location) {
-  return {&t, sample_idx, fnv_hash(location) % t.initial_dimension_bound};
+void get_generator(const SobolTable &t, unsigned sample_idx, unsigned location,
+                   RngState &out) {
+  out.table = &t;
+  out.sample = sample_idx;
+  out.dim = fnv_hash(location) % t.initial_dimension_bound;
+}
+
+void get_uniform_generator(unsigned sample_idx, unsigned location, unsigned samples_per,
+                           RngState &out) {
+  out.uniform = true;
+  out.gen.seed(sample_idx + location * samples_per);
 }
 
 // ---------------------------------------------------------------------------
@@ -1370,6 +1390,7 @@ struct RenderCtx {
   const float *rays = nullptr; // InitialRays / InitialIdxAndDir: one ray per location
   const unsigned *idxs = nullptr; // InitialIdxAndDir: BVH-order hit triangle per location
   unsigned n_steps = 0;           // OutputPerStep: steps per path, 0 = off
+  unsigned spp = 0;               // samples per location (Uniform RNG seed)
 };
 
 // rendering_equation.h:27-129 + rendering_equation_iteration.h:9-153 for one
@@ -1382,7 +1403,12 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
   const FlatScene &sc = *c.scene;
   const oracle_settings &st = *c.st;
   unsigned location = x + y * c.x_dim;
-  RngState rng = get_generator(*c.sobol, sample_idx, location);
+  RngState rng;
+  if (st.rng == 1) {
+    get_uniform_generator(sample_idx, location, c.spp, rng);
+  } else {
+    get_generator(*c.sobol, sample_idx, location, rng);
+  }
   Ray ray;
   if (c.rays != nullptr) {
     // initial_ray_sample.h:47-48: the caller's ray, no RNG draw
@@ -1768,7 +1794,7 @@ bool render_image(const oracle_scene &scene, const oracle_settings &st,
     }
   }
   RenderCtx ctx{&sc, &bvh, &st, &sobol, read_affine(f2w ? f2w : identity), x_dim, y_dim,
-                ex.rays, ex.idxs ? bvh_idxs.data() : nullptr, ex.n_steps};
+                ex.rays, ex.idxs ? bvh_idxs.data() : nullptr, ex.n_steps, spp};
   const unsigned n_out = ex.n_steps ? ex.n_steps : 1;
   const size_t n_pix = (size_t)x_dim * y_dim;
   auto t0 = std::chrono::steady_clock::now();

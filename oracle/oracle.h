@@ -98,6 +98,7 @@ typedef struct {
   uint32_t back_cull_emission;
   uint32_t reduce_order; /* 0: CPU lane order, 1: GPU shuffle-tree order */
   uint32_t n_threads;    /* OpenMP threads, 0 = default */
+  uint32_t rng;          /* 0 Sobel, 1 Uniform (std::mt19937) */
 } oracle_settings;
 
 typedef struct {

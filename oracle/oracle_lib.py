@@ -56,7 +56,8 @@ class OracleSettings(ctypes.Structure):
                 ("light_sampler", c_u32), ("dir_sampler", c_u32), ("term_prob", c_u32),
                 ("term_prob_prob", c_f32), ("term_prob_iters", c_u32), ("term_prob_exp", c_f32),
                 ("term_prob_min_prob", c_f32), ("max_sample_size", c_u32),
-                ("back_cull_emission", c_u32), ("reduce_order", c_u32), ("n_threads", c_u32)]
+                ("back_cull_emission", c_u32), ("reduce_order", c_u32), ("n_threads", c_u32),
+                ("rng", c_u32)]
 
 
 class WorkDivision(ctypes.Structure):
@@ -282,7 +283,7 @@ def settings_from(s, reduce_order=1, n_threads=0):
                           r.traversal_per_intersect_cost, r.target_objects, r.light_sampler,
                           r.dir_sampler, r.term_prob, r.term_prob_prob, r.term_prob_iters,
                           r.term_prob_exp, r.term_prob_min_prob, r.max_sample_size,
-                          r.back_cull_emission, reduce_order, n_threads)
+                          r.back_cull_emission, reduce_order, n_threads, r.rng)
 
 
 class SceneArrays:

@@ -378,9 +378,11 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
     }
   }
   const unsigned long long limit = std::min<unsigned long long>(total, sample_limit);
-  Status ss = prepare_sobol(st.max_sample_size, max_spp);
-  if (!ss.good()) {
-    return ss;
+  if (st.rng == PATH_RNG_SOBEL) {
+    Status ss = prepare_sobol(st.max_sample_size, max_spp);
+    if (!ss.good()) {
+      return ss;
+    }
   }
   PG_TRY_CUDA(b_scenes_.upload(scenes.data(), n * sizeof(BatchScene), stream_), "scene table");
   // wavefront state for the whole batch
@@ -430,6 +432,7 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   p.term_min_prob = st.term_prob_min_prob;
   p.back_cull = st.back_cull_emission;
   p.target_objects = st.target_objects;
+  p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   p.status = status_.as<uint32_t>();
   p.counters = counters_.as<unsigned long long>();
 
@@ -455,6 +458,10 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   w.total_samples = limit;
   w.sample_rgb = wf_samples_.as<float>();
   w.n_slots = n_slots;
+  if (p.rng_uniform) {
+    PG_TRY_CUDA(wf_rng_.ensure((size_t)n_slots * kRngStateWords * 4), "rng states");
+    w.rng_state = wf_rng_.as<uint32_t>();
+  }
   w.scenes = b_scenes_.as<const BatchScene>();
   w.n_scenes = (uint32_t)n;
 

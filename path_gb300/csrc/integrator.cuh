@@ -17,6 +17,8 @@
 #include "geom.h"
 #include "kernels.h"
 
+#include <curand_kernel.h>
+
 namespace pg {
 namespace dev {
 // internal linkage: every translation unit that includes this header gets
@@ -411,8 +413,48 @@ __device__ __forceinline__ float light_bound(float target) {
 }
 
 // ---------------------------------------------------------------------------
-// RNG: table-driven Sobol (include/rng/rng_from_sequence_gen.h:26-107)
-struct Rng {
+// RNG.  Sobel: table-driven Sobol (include/rng/rng_from_sequence_gen.h:26-107).
+// Uniform (include/rng/uniform/uniform.h:18-76, GPU execution model): a
+// cuRAND XORWOW state per path, seeded with curand_init(seed, 0, 0) and
+// drawn with curand_uniform, 1.0 mapped to 0.0
+// (include/lib/cuda/curand_utils.h:58-66).  The state lives in memory (a
+// slot of the streaming buffers or the thread's stack) as 32-bit words
+// `stride` apart, so a path can stop in one kernel and go on in the next.
+constexpr uint32_t kXorwowWords = sizeof(curandStateXORWOW) / 4;
+static_assert(kXorwowWords == kRngStateWords, "Uniform RNG state size");
+
+__device__ __noinline__ void uniform_seed(uint32_t seed, uint32_t *w, uint32_t stride) {
+  curandStateXORWOW st;
+  curand_init(seed, 0, 0, &st);
+  const uint32_t *q = reinterpret_cast<const uint32_t *>(&st);
+#pragma unroll
+  for (uint32_t k = 0; k < kXorwowWords; ++k) {
+    w[k * stride] = q[k];
+  }
+}
+
+__device__ __forceinline__ float uniform_next(uint32_t *w, uint32_t stride) {
+  curandStateXORWOW st;
+  uint32_t *q = reinterpret_cast<uint32_t *>(&st);
+#pragma unroll
+  for (uint32_t k = 0; k < kXorwowWords; ++k) {
+    q[k] = w[k * stride];
+  }
+  const float out = curand_uniform(&st);
+#pragma unroll
+  for (uint32_t k = 0; k < kXorwowWords; ++k) {
+    w[k * stride] = q[k];
+  }
+  return out == 1.0f ? 0.0f : out;
+}
+
+// RngT<false>: Sobel, row = the sample's table row, dim = next dimension,
+// bound = the dimension bound.  RngT<true>: Uniform, the state words `stride`
+// apart from w.  The mode is a type so that the Sobel kernels carry no trace
+// of the Uniform draw.
+template <bool kUniform> struct RngT;
+
+template <> struct RngT<false> {
   const float *row;
   uint32_t dim;
   uint32_t bound;
@@ -422,6 +464,12 @@ struct Rng {
     dim = dim == bound ? 0u : dim;
     return v;
   }
+};
+
+template <> struct RngT<true> {
+  uint32_t *w;
+  uint32_t stride;
+  __device__ __forceinline__ float next() { return uniform_next(w, stride); }
 };
 
 __device__ __forceinline__ uint32_t fnv_hash(uint32_t in) {
@@ -646,7 +694,8 @@ struct Sample {
   rgb mult;
 };
 
-__device__ __forceinline__ Sample diffuse_sample(rgb albedo, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ __forceinline__ Sample diffuse_sample(rgb albedo, f3 in, f3 n, R &rng) {
   float v0 = rng.next();
   float v1 = rng.next();
   float phi = (float)(kTwoPi * (double)v0);
@@ -658,7 +707,8 @@ __device__ __forceinline__ Sample diffuse_sample(rgb albedo, f3 in, f3 n, Rng &r
   return s;
 }
 
-__device__ Sample glossy_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ Sample glossy_sample(const Mat &m, f3 in, f3 n, R &rng) {
   float v0 = rng.next();
   float v1 = rng.next();
   f3 refl = reflect(in, n);
@@ -680,7 +730,8 @@ __device__ __forceinline__ void onb(f3 n, f3 &b1, f3 &b2) {
   b2 = mk(b, sign + n.y * n.y * a, -n.y);
 }
 
-__device__ Sample ggx_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ Sample ggx_sample(const Mat &m, f3 in, f3 n, R &rng) {
   float u0 = rng.next();
   float u1 = rng.next();
   f3 wo = -in;
@@ -716,7 +767,8 @@ __device__ Sample ggx_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
   return s;
 }
 
-__device__ Sample continuous_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ Sample continuous_sample(const Mat &m, f3 in, f3 n, R &rng) {
   switch (m.type) {
   case kDiffuse:
     return diffuse_sample(m.diffuse, in, n, rng);
@@ -743,7 +795,8 @@ __device__ Sample continuous_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
   }
 }
 
-__device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, R &rng) {
   Sample s;
   s.mult = m.specular;
   switch (m.type) {
@@ -774,7 +827,8 @@ __device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
   }
 }
 
-__device__ Sample uniform_dir_sample(const Mat &m, f3 in, f3 n, Rng &rng) {
+template <class R>
+__device__ Sample uniform_dir_sample(const Mat &m, f3 in, f3 n, R &rng) {
   float v0 = rng.next();
   float v1 = rng.next();
   bool whole = !is_brdf(m);
@@ -812,7 +866,8 @@ __device__ __forceinline__ LightSet lights_of(const RenderParams &P) {
   return l;
 }
 
-__device__ bool sample_light(const LightSet &L, f3 pos, const Mat &m, f3 normal, Rng &rng,
+template <class R>
+__device__ bool sample_light(const LightSet &L, f3 pos, const Mat &m, f3 normal, R &rng,
                              LightSample &out) {
   if (L.n == 0) {
     return false;
@@ -882,9 +937,10 @@ __device__ __forceinline__ float term_prob(const RenderParams &P, uint32_t iters
 
 // camera ray (initial_ray_sample.h:16-56)
 // film_to_world and image size of one camera
+// the image a sample belongs to: camera, size and samples per location
 struct Camera {
   const float *f2w;
-  uint32_t x_dim, y_dim;
+  uint32_t x_dim, y_dim, spp;
 };
 
 __device__ __forceinline__ Camera camera_of(const RenderParams &P) {
@@ -892,6 +948,7 @@ __device__ __forceinline__ Camera camera_of(const RenderParams &P) {
   c.f2w = P.f2w;
   c.x_dim = P.x_dim;
   c.y_dim = P.y_dim;
+  c.spp = P.spp;
   return c;
 }
 
@@ -927,24 +984,37 @@ __device__ __forceinline__ f3 shading_normal(const RenderParams &P, uint32_t idx
 // RenderingEquationState (rendering_equation_state.h:14-52) with at most
 // one light sample per vertex.  o is the current vertex, the origin of both
 // the next extension ray (direction d) and the light ray (direction ld).
-struct PathState {
+template <bool kUniform> struct PathStateT {
   f3 o, d, ld;
   float light_target;
   rgb multiplier, light_mult, total;
   uint32_t iters;
   bool count_emission, has_next, has_light;
-  Rng rng;
+  RngT<kUniform> rng;
 };
+using PathState = PathStateT<false>;
 
 // camera ray of a sample (initial_ray_sample.h:36-56): 2 RNG draws for a
-// square image, the caller's ray for an InitialRays spec
+// square image, the caller's ray for an InitialRays spec.  A Uniform path's
+// generator is seeded with sample + location x spp (uniform.h:63-66; the
+// frame offset of a progressive render adds offset x locations) and keeps
+// its state at rng_words (words rng_stride apart).
+template <bool kUniform>
 __device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Camera &cam,
                                                uint32_t sample_idx, uint32_t x, uint32_t y,
-                                               PathState &s) {
+                                               PathStateT<kUniform> &s, uint32_t *rng_words,
+                                               uint32_t rng_stride) {
   const uint32_t location = x + y * cam.x_dim;
-  s.rng.row = P.sobol + (size_t)(sample_idx + P.sample_offset) * P.dim_bound;
-  s.rng.bound = P.dim_bound;
-  s.rng.dim = fnv_hash(location) % P.init_dim_bound;
+  if constexpr (kUniform) {
+    uniform_seed(sample_idx + location * cam.spp + P.sample_offset * (cam.x_dim * cam.y_dim),
+                 rng_words, rng_stride);
+    s.rng.w = rng_words;
+    s.rng.stride = rng_stride;
+  } else {
+    s.rng.row = P.sobol + (size_t)(sample_idx + P.sample_offset) * P.dim_bound;
+    s.rng.bound = P.dim_bound;
+    s.rng.dim = fnv_hash(location) % P.init_dim_bound;
+  }
   ray r;
   if (P.initial_rays != nullptr) {
     // InitialRays: the caller's ray for this location, no RNG draw
@@ -969,9 +1039,12 @@ __device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Came
   s.has_light = false;
 }
 
+// rng_words: where a Uniform path keeps its XORWOW state (unused for Sobel)
+template <bool kUniform>
 __device__ __forceinline__ void path_begin(const RenderParams &P, uint32_t sample_idx,
-                                           uint32_t x, uint32_t y, PathState &s) {
-  path_begin_cam(P, camera_of(P), sample_idx, x, y, s);
+                                           uint32_t x, uint32_t y, PathStateT<kUniform> &s,
+                                           uint32_t *rng_words, uint32_t rng_stride) {
+  path_begin_cam(P, camera_of(P), sample_idx, x, y, s, rng_words, rng_stride);
 }
 
 // One rendering_equation_iteration (rendering_equation_iteration.h:9-153)
@@ -1002,7 +1075,9 @@ __device__ __forceinline__ rgb albedo_of(const Mat &m) {
   }
 }
 
-__device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L, PathState &s,
+template <bool kUniform>
+__device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L,
+                                       PathStateT<kUniform> &s,
                                        const Hit &lh, const Hit &nh,
                                        StepTrace *tr = nullptr) {
   const bool performs_samples = P.light_sampler == 0;
@@ -1109,8 +1184,8 @@ __device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L,
 }
 
 // the safety bound on path vertices (no counterpart in the reference)
-__device__ __forceinline__ bool path_continues(const RenderParams &P, PathState &s,
-                                               bool cont) {
+template <class S>
+__device__ __forceinline__ bool path_continues(const RenderParams &P, S &s, bool cont) {
   if (cont && s.iters >= kMaxPathVertices) {
     set_status(P.status, kStatusPathTooLong);
     return false;
@@ -1121,8 +1196,8 @@ __device__ __forceinline__ bool path_continues(const RenderParams &P, PathState 
 // closest hits of a path's pending light and extension rays.  The first
 // step of an InitialIdxAndDir sample takes the caller's hit instead of
 // tracing (initial_ray_sample.h:58-74: distance 1, front side).
-template <uint32_t kTrav, bool kCount>
-__device__ __forceinline__ void step_hits(const RenderParams &P, const PathState &s,
+template <uint32_t kTrav, bool kCount, class S>
+__device__ __forceinline__ void step_hits(const RenderParams &P, const S &s,
                                           bool first, uint32_t x, Counts &cnt, Hit &lh,
                                           Hit &nh) {
   lh = no_hit();
@@ -1147,11 +1222,12 @@ __device__ __forceinline__ void step_hits(const RenderParams &P, const PathState
 }
 
 // one camera sample of rendering_equation, traced in a loop
-template <uint32_t kTrav, bool kCount>
+template <uint32_t kTrav, bool kCount, bool kUniform>
 __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
                                 uint32_t x, uint32_t y, Counts &cnt) {
-  PathState s;
-  path_begin(P, sample_idx, x, y, s);
+  PathStateT<kUniform> s;
+  uint32_t xw[kUniform ? kXorwowWords : 1]; // the Uniform generator's state
+  path_begin(P, sample_idx, x, y, s, xw, 1);
   bool first = true;
   while (true) {
     Hit lh, nh;
@@ -1165,11 +1241,12 @@ __device__ rgb integrate_sample(const RenderParams &P, uint32_t sample_idx,
 
 // OutputPerStep (rendering_equation.h:61-124): the radiance gathered in
 // step k is added to steps[k]; a path stops after P.n_steps steps
-template <uint32_t kTrav>
+template <uint32_t kTrav, bool kUniform>
 __device__ void integrate_sample_steps(const RenderParams &P, uint32_t sample_idx,
                                        uint32_t x, uint32_t y, rgb *steps) {
-  PathState s;
-  path_begin(P, sample_idx, x, y, s);
+  PathStateT<kUniform> s;
+  uint32_t xw[kUniform ? kXorwowWords : 1];
+  path_begin(P, sample_idx, x, y, s, xw, 1);
   Counts cnt = {0, 0, 0};
   for (uint32_t k = 0; k < P.n_steps; ++k) {
     Hit lh, nh;

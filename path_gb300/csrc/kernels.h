@@ -54,9 +54,14 @@ struct RenderParams {
   uint32_t sample_offset;
   // radiance cache: paths end into the cache at this vertex (0 = off)
   uint32_t cache_depth;
+  // Uniform RNG (cuRAND XORWOW per path) instead of the Sobol table
+  uint32_t rng_uniform;
 };
 
 enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
+
+// 32-bit words of one Uniform-RNG path state (a curandStateXORWOW)
+constexpr uint32_t kRngStateWords = 12;
 
 // queue heads of the wavefront render
 struct WaveQueues {
@@ -114,6 +119,8 @@ struct WaveParams {
   // throughput there (zero when the path ended before it)
   float *cache_q;
   float *cache_beta;
+  // Uniform RNG: the XORWOW state words of slot i at rng_state[k * n_slots + i]
+  uint32_t *rng_state;
 };
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);

@@ -81,7 +81,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
       (output.type != PATH_OUTPUT_BGRA && output.type != PATH_OUTPUT_FLOAT_RGB)) {
     return Status::err(PATH_ERR_ARGUMENT, "the output must be device memory (on_device = 1)");
   }
-  if (st.rng != PATH_RNG_SOBEL || st.traversal > PATH_TRAVERSAL_WIDE8 ||
+  if (st.rng > PATH_RNG_UNIFORM || st.traversal > PATH_TRAVERSAL_WIDE8 ||
       st.target_objects == 0 || st.target_objects > 10) {
     return Status::err(PATH_ERR_ARGUMENT, "unsupported settings");
   }
@@ -95,7 +95,8 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
     return Status::err(PATH_ERR_ARGUMENT,
                        "scene not resident on this renderer: render it once with path_render");
   }
-  if (sobol_bound_ != st.max_sample_size || sobol_count_ < spp || !sobol_table_.get()) {
+  if (st.rng == PATH_RNG_SOBEL &&
+      (sobol_bound_ != st.max_sample_size || sobol_count_ < spp || !sobol_table_.get())) {
     return Status::err(PATH_ERR_ARGUMENT,
                        "Sobol table for this max_sample_size / samples_per not resident: "
                        "render once with path_render");
@@ -147,6 +148,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   p.term_min_prob = st.term_prob_min_prob;
   p.back_cull = st.back_cull_emission;
   p.target_objects = st.target_objects;
+  p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   std::memcpy(p.f2w, spec.film_to_world, sizeof(p.f2w));
   p.x_dim = spec.x_dim;
   p.y_dim = spec.y_dim;

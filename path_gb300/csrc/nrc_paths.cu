@@ -24,6 +24,7 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   return x;
 }
 
+template <bool kUniform>
 __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_t n,
                                                    uint32_t frame, float *records) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -35,8 +36,9 @@ __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_
   const uint32_t pixel = h0 % n_pix;
   const uint32_t x = pixel % P.x_dim, y = pixel / P.x_dim;
   const uint32_t smp = mix32(h0) % P.spp;
-  PathState s;
-  path_begin(P, smp, x, y, s);
+  PathStateT<kUniform> s;
+  uint32_t xw[kUniform ? kXorwowWords : 1];
+  path_begin(P, smp, x, y, s, xw, 1);
   float q[kMaxRecordVertices][12];
   rgb gathered[kMaxRecordVertices], beta[kMaxRecordVertices];
   uint32_t nv = 0;
@@ -110,7 +112,11 @@ cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, 
   if (n == 0) {
     return cudaSuccess;
   }
-  dev::k_nrc_paths<<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, records);
+  if (p.rng_uniform) {
+    dev::k_nrc_paths<true><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, records);
+  } else {
+    dev::k_nrc_paths<false><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, records);
+  }
   return cudaGetLastError();
 }
 

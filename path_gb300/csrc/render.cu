@@ -10,7 +10,7 @@ namespace dev {
 // thread's samples summed serially in FP32 (rendering_equation.h:51-124),
 // then the sample_block_size lanes of a pixel summed by the shuffle tree and
 // written by the first lane (mega_kernel/run_impl.h:165-204).
-template <uint32_t kTrav, bool kCount>
+template <uint32_t kTrav, bool kCount, bool kUniform>
 __global__ void __launch_bounds__(256) k_render(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(256) k_render(const RenderParams P) {
   rgb total = zero_rgb();
   if (!tw.exit) {
     for (uint32_t s = tw.start; s < tw.end; ++s) {
-      total = total + integrate_sample<kTrav, kCount>(P, s, tw.x, tw.y, cnt);
+      total = total + integrate_sample<kTrav, kCount, kUniform>(P, s, tw.x, tw.y, cnt);
     }
   }
   const uint32_t sbs = P.wd.sample_block_size;
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_render(const RenderParams P) {
 
 // the mega kernel with OutputPerStep output (mega_kernel/run_impl.h:
 // 160-185): per-thread step sums, one sub-block reduction per step
-template <uint32_t kTrav>
+template <uint32_t kTrav, bool kUniform>
 __global__ void __launch_bounds__(256) k_render_steps(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) k_render_steps(const RenderParams P) {
   }
   if (!tw.exit) {
     for (uint32_t s = tw.start; s < tw.end; ++s) {
-      integrate_sample_steps<kTrav>(P, s, tw.x, tw.y, steps);
+      integrate_sample_steps<kTrav, kUniform>(P, s, tw.x, tw.y, steps);
     }
   }
   const uint32_t sbs = P.wd.sample_block_size;
@@ -138,20 +138,40 @@ __global__ void k_pmath(uint32_t fn, const float *x, const float *y, float *out,
 
 } // namespace dev
 
+namespace {
+template <uint32_t kTrav, bool kCount>
+void render_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s) {
+  if (p.rng_uniform) {
+    dev::k_render<kTrav, kCount, true><<<grid, block, 0, s>>>(p);
+  } else {
+    dev::k_render<kTrav, kCount, false><<<grid, block, 0, s>>>(p);
+  }
+}
+
+template <uint32_t kTrav>
+void render_steps_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s) {
+  if (p.rng_uniform) {
+    dev::k_render_steps<kTrav, true><<<grid, block, 0, s>>>(p);
+  } else {
+    dev::k_render_steps<kTrav, false><<<grid, block, 0, s>>>(p);
+  }
+}
+} // namespace
+
 cudaError_t launch_render(const RenderParams &p, uint32_t traversal,
                           uint32_t n_blocks, bool counting, cudaStream_t s) {
   const dim3 grid(n_blocks), block(p.wd.block_size);
   if (traversal == kTravWide) {
     if (counting) {
-      dev::k_render<kTravWide, true><<<grid, block, 0, s>>>(p);
+      render_variant<kTravWide, true>(p, grid, block, s);
     } else {
-      dev::k_render<kTravWide, false><<<grid, block, 0, s>>>(p);
+      render_variant<kTravWide, false>(p, grid, block, s);
     }
   } else {
     if (counting) {
-      dev::k_render<kTravBinary, true><<<grid, block, 0, s>>>(p);
+      render_variant<kTravBinary, true>(p, grid, block, s);
     } else {
-      dev::k_render<kTravBinary, false><<<grid, block, 0, s>>>(p);
+      render_variant<kTravBinary, false>(p, grid, block, s);
     }
   }
   return cudaGetLastError();
@@ -161,9 +181,9 @@ cudaError_t launch_render_steps(const RenderParams &p, uint32_t traversal,
                                 uint32_t n_blocks, cudaStream_t s) {
   const dim3 grid(n_blocks), block(p.wd.block_size);
   if (traversal == kTravWide) {
-    dev::k_render_steps<kTravWide><<<grid, block, 0, s>>>(p);
+    render_steps_variant<kTravWide>(p, grid, block, s);
   } else {
-    dev::k_render_steps<kTravBinary><<<grid, block, 0, s>>>(p);
+    render_steps_variant<kTravBinary>(p, grid, block, s);
   }
   return cudaGetLastError();
 }

@@ -490,10 +490,8 @@ Status check_settings(const path_settings &s) {
   if (s.kernel_approach != PATH_KERNEL_MEGA && s.kernel_approach != PATH_KERNEL_STREAMING) {
     return Status::err(PATH_ERR_ARGUMENT, "unknown kernel_approach");
   }
-  if (s.rng != PATH_RNG_SOBEL) {
-    return Status::err(PATH_ERR_UNSUPPORTED,
-                       "only the Sobel RNG is built (Uniform draws cuRAND XORWOW / "
-                       "mt19937 streams that differ between the reference's CPU and GPU)");
+  if (s.rng != PATH_RNG_SOBEL && s.rng != PATH_RNG_UNIFORM) {
+    return Status::err(PATH_ERR_ARGUMENT, "unknown rng value");
   }
   if (s.light_sampler > PATH_LIGHT_NONE || s.dir_sampler > PATH_DIR_UNIFORM ||
       s.term_prob > PATH_TERM_NORMALIZE || s.traversal > PATH_TRAVERSAL_WIDE8) {
@@ -626,9 +624,11 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
       return sr;
     }
   }
-  Status ss = prepare_sobol(st.max_sample_size, spec.sample_offset + spp);
-  if (!ss.good()) {
-    return ss;
+  if (st.rng == PATH_RNG_SOBEL) {
+    Status ss = prepare_sobol(st.max_sample_size, spec.sample_offset + spp);
+    if (!ss.good()) {
+      return ss;
+    }
   }
   WorkDiv wd;
   if (!make_workdiv(st.render_work_division, spp, x_dim, y_dim, wd)) {
@@ -716,6 +716,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   p.row_lo = row_lo;
   p.sample_offset = spec.sample_offset;
   p.cache_depth = cache_ != nullptr ? cache_depth_ : 0u;
+  p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   p.row_hi = row_hi;
   const size_t pix0 = (size_t)row_lo * x_dim;           // first band pixel
   const size_t n_band = (size_t)(row_hi - row_lo) * x_dim;
@@ -727,7 +728,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
-    slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 21u;
+    slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 24u;
     Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks,
                               st.time_kernels != 0, &launches);
     if (!sw.good()) {
@@ -907,6 +908,10 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
     w.pend_mat = reinterpret_cast<uint32_t *>(pb + 2 * a256((size_t)n_slots * 16));
     w.d_params = adj->d_params;
     PG_TRY_CUDA(cudaMemsetAsync(w.pend_mat, 0xff, (size_t)n_slots * 4, stream_), "adjoint init");
+  }
+  if (p.rng_uniform) {
+    PG_TRY_CUDA(wf_rng_.ensure((size_t)n_slots * kRngStateWords * 4), "rng states");
+    w.rng_state = wf_rng_.as<uint32_t>();
   }
   // queue heads: n_slots live slots, one extension ray each
   uint32_t *h = wf_host_.as<uint32_t>();

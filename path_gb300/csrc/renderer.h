@@ -193,7 +193,7 @@ private:
   uint32_t last_blocks_ = 0;
   DeviceBuffer adj_image_, adj_dimage_, adj_params_, adj_pend_;
   cudaEvent_t trace_event(size_t i);
-  DeviceBuffer wf_slots_, wf_queues_, wf_samples_;
+  DeviceBuffer wf_slots_, wf_queues_, wf_samples_, wf_rng_;
   PinnedBuffer wf_host_;
   int num_sms_ = 0;
   path_render_stats stats_{};

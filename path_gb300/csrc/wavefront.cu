@@ -19,6 +19,8 @@
 // the shuffle tree), so the image is bit-identical to the megakernel's.
 #include "integrator.cuh"
 
+#include <type_traits>
+
 namespace pg {
 namespace dev {
 
@@ -70,8 +72,9 @@ __device__ __forceinline__ uint32_t scene_of(const WaveParams &W, unsigned long 
 // Slot state: o (xyz, light target), d and ld (xyz, scene root node bits in
 // w, read by the trace kernel), multipliers, radiance so far, and
 // (id low word, id bits 32-39 | scene << 8, RNG dimension, iters | flags << 24).
+template <class S>
 __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
-                                           const PathState &s, unsigned long long id,
+                                           const S &s, unsigned long long id,
                                            uint32_t scene, uint32_t root) {
   W.o[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.light_target);
   W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, __uint_as_float(root));
@@ -81,8 +84,12 @@ __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
   W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
   uint32_t flags = (s.has_next ? kFlagNext : 0u) | (s.has_light ? kFlagLight : 0u) |
                    (s.count_emission ? kFlagEmission : 0u);
+  uint32_t dim = 0; // a Uniform path's generator state is in W.rng_state
+  if constexpr (std::is_same_v<S, PathState>) {
+    dim = s.rng.dim;
+  }
   W.state[slot] = make_uint4((uint32_t)id, ((uint32_t)(id >> 32) & 0xffu) | (scene << 8),
-                             s.rng.dim, s.iters | (flags << 24));
+                             dim, s.iters | (flags << 24));
 }
 
 // the lights of a slot's scene
@@ -98,9 +105,10 @@ __device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t s
   return l;
 }
 
+template <bool kUniform>
 __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
-                                                        PathState &s, uint32_t &scene,
-                                                        uint32_t &root) {
+                                                        PathStateT<kUniform> &s,
+                                                        uint32_t &scene, uint32_t &root) {
   const RenderParams &P = W.P;
   float4 o = W.o[slot], d = W.d[slot], ld = W.ld[slot];
   float4 m = W.mult[slot], lm = W.lmult[slot], t = W.total[slot];
@@ -126,20 +134,26 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
     local = id - W.scenes[scene].first_sample;
     spp = W.scenes[scene].spp;
   }
-  const uint32_t smp = (uint32_t)(local % spp);
-  s.rng.row = P.sobol + (size_t)(smp + P.sample_offset) * P.dim_bound;
-  s.rng.bound = P.dim_bound;
-  s.rng.dim = st.z;
+  if constexpr (kUniform) {
+    s.rng.w = W.rng_state + slot;
+    s.rng.stride = W.n_slots;
+  } else {
+    const uint32_t smp = (uint32_t)(local % spp);
+    s.rng.row = P.sobol + (size_t)(smp + P.sample_offset) * P.dim_bound;
+    s.rng.bound = P.dim_bound;
+    s.rng.dim = st.z;
+  }
   return id;
 }
 
+template <bool kUniform>
 __device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
                                              unsigned long long id) {
   uint32_t x, y, smp, scene = 0, root = 0;
-  PathState s;
+  PathStateT<kUniform> s;
   if (W.scenes == nullptr) {
     sample_coords(id, W.P.spp, W.P.x_dim, x, y, smp);
-    path_begin(W.P, smp, x, y, s);
+    path_begin(W.P, smp, x, y, s, W.rng_state + slot, W.n_slots);
   } else {
     scene = scene_of(W, id);
     const BatchScene &b = W.scenes[scene];
@@ -148,7 +162,8 @@ __device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
     cam.f2w = b.f2w;
     cam.x_dim = b.x_dim;
     cam.y_dim = b.y_dim;
-    path_begin_cam(W.P, cam, smp, x, y, s);
+    cam.spp = b.spp;
+    path_begin_cam(W.P, cam, smp, x, y, s, W.rng_state + slot, W.n_slots);
     root = b.root;
   }
   store_path(W, slot, s, id, scene, root);
@@ -260,7 +275,11 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
   if (i >= n0) {
     return;
   }
-  begin_sample(W, i, W.first_sample + i);
+  if (W.P.rng_uniform) {
+    begin_sample<true>(W, i, W.first_sample + i);
+  } else {
+    begin_sample<false>(W, i, W.first_sample + i);
+  }
   W.active[0][i] = i;
   W.rays[i] = i << 1;
 }
@@ -389,7 +408,7 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // d log f / d(parameter) of that vertex is its parameter gradient; the
 // light sample adds its own term, and emission terms are linear.  Sampling
 // densities and the light table are held fixed (detached estimator).
-template <bool kGrad>
+template <bool kGrad, bool kUniform>
 __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t parity) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->active[parity];
@@ -413,7 +432,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t p
     float gv_light[3] = {0.f, 0.f, 0.f}, gv_emit[3] = {0.f, 0.f, 0.f};
     if (valid) {
       slot = in[i];
-      PathState s;
+      PathStateT<kUniform> s;
       uint32_t scene, root;
       unsigned long long id = load_path(W, slot, s, scene, root);
       Hit lh = s.has_light ? unpack_hit(W.hit_light[slot]) : no_hit();
@@ -537,7 +556,7 @@ __global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t p
       if (finished) {
         unsigned long long id = first + (unsigned long long)__popc(mask & ((1u << lane) - 1u));
         if (id < W.total_samples) {
-          begin_sample(W, slot, id);
+          begin_sample<kUniform>(W, slot, id);
           if (kGrad) {
             W.pend_mat[slot] = kNoMaterial;
           }
@@ -634,10 +653,17 @@ cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
 cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_t shade_grid,
                                    cudaStream_t s, bool grad) {
   dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
+  const bool u = w.P.rng_uniform != 0;
   if (grad) {
-    dev::k_wf_shade<true><<<shade_grid, 256, 0, s>>>(w, parity);
+    if (u) {
+      dev::k_wf_shade<true, true><<<shade_grid, 256, 0, s>>>(w, parity);
+    } else {
+      dev::k_wf_shade<true, false><<<shade_grid, 256, 0, s>>>(w, parity);
+    }
+  } else if (u) {
+    dev::k_wf_shade<false, true><<<shade_grid, 256, 0, s>>>(w, parity);
   } else {
-    dev::k_wf_shade<false><<<shade_grid, 256, 0, s>>>(w, parity);
+    dev::k_wf_shade<false, false><<<shade_grid, 256, 0, s>>>(w, parity);
   }
   return cudaGetLastError();
 }

@@ -52,11 +52,13 @@ def _small_batch(seed, n):
     return items
 
 
-@pytest.mark.parametrize("tuning", [None, {"slots_log2": 10, "trace_min_blocks": 3,
-                                           "shade_ctas_per_sm": 2,
-                                           "iterations_per_graph": 2}])
-def test_batch_images_equal_single_renders(lib, tuning):
+@pytest.mark.parametrize("tuning,rng", [(None, 0),
+                                        ({"slots_log2": 10, "trace_min_blocks": 3,
+                                          "shade_ctas_per_sm": 2, "iterations_per_graph": 2}, 0),
+                                        ({"slots_log2": 10}, 1)])
+def test_batch_images_equal_single_renders(lib, tuning, rng):
     s = scenes.path_settings(6, "wide")
+    s.rng = rng
     items = _small_batch(3, 7)
     outs, refs, batch = [], [], []
     for k, (sc, w, h, spp) in enumerate(items):

@@ -275,6 +275,20 @@ def test_streaming_equals_megakernel_full_cornell(lib):
     assert np.array_equal(bits(mega), bits(wave))
 
 
+@pytest.mark.parametrize("slots_log2", [10, 13])
+def test_streaming_refill_equals_megakernel(lib, slots_log2):
+    """Fewer paths in flight than samples: slots are refilled with new
+    samples as paths end, and the image stays the megakernel's bit for bit."""
+    sc = scenes.large_mesh_room(5, 40, 40)
+    s = scenes.path_settings(8, "wide")
+    f2w = scenes.cornell_camera(96, 96)
+    mega = _render_gpu(sc, s, 8, 96, 96, f2w)
+    s.kernel_approach = 1
+    s.wavefront_slots_log2 = slots_log2
+    wave = _render_gpu(sc, s, 8, 96, 96, f2w)
+    assert np.array_equal(bits(mega), bits(wave))
+
+
 def _camera_rays(rng, n, f2w):
     """Rays through random film points of the Cornell camera."""
     m = np.asarray(f2w, np.float64).reshape(3, 4)

@@ -1,0 +1,84 @@
+"""Uniform RNG (include/rng/uniform/uniform.h:18-76): one cuRAND XORWOW
+generator per path, seeded with sample + location x spp.
+
+The reference's two execution models draw different streams for Uniform
+(XORWOW on the GPU, std::mt19937 on the CPU), so the GPU image is held to
+the oracle in expectation: relative RMSE (||a - b||_2 / ||b||_2 over all
+pixel channels) against a 4096-spp Sobol render of the oracle at most 0.04,
+and against the oracle's own Uniform render at most 0.06 (measured: 0.018
+for the oracle's Uniform render at 1024 spp).  Within the GPU path the
+stream is exact: the megakernel, the streaming approach (slots refilled or
+not) and the batched render give the same image bit for bit."""
+
+import numpy as np
+import pytest
+
+from path_gb300 import api, scenes
+from oracle import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _gpu(scene, s, spp, w, h, spec=None):
+    out = np.zeros((h, w, 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, spec or api.SquareImage(w, h, scenes.cornell_camera(w, h)),
+             out, scene, spp, s)
+    assert r.stats()["device_status"] == 0
+    return out
+
+
+@pytest.mark.parametrize("traversal,slots_log2", [("wide", 0), ("wide", 10), ("binary", 0)])
+def test_uniform_megakernel_equals_streaming(lib, traversal, slots_log2):
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, traversal)
+    s.rng = 1
+    mega = _gpu(sc, s, 16, 64, 64)
+    s.kernel_approach = 1
+    s.wavefront_slots_log2 = slots_log2
+    wave = _gpu(sc, s, 16, 64, 64)
+    assert np.array_equal(bits(mega), bits(wave))
+
+
+def test_uniform_converges_to_the_oracle(lib, oracle):
+    sc = scenes.cornell_box()
+    w = h = 24
+    f2w = scenes.cornell_camera(w, h)
+    arr = ol.SceneArrays(sc.export())
+    s = scenes.path_settings(5, "wide")
+    ref, _ = ol.render(arr, ol.settings_from(s, reduce_order=1), 4096, w, h, f2w)
+    s.rng = 1
+    s.kernel_approach = 1
+    gpu = _gpu(sc, s, 1024, w, h)
+    cpu, _ = ol.render(arr, ol.settings_from(s, reduce_order=1), 1024, w, h, f2w)
+    e_ref, e_cpu = rel_rmse(gpu, ref), rel_rmse(gpu, cpu)
+    print(f"uniform: vs 4096-spp Sobol {e_ref:.4f}, vs oracle Uniform {e_cpu:.4f}")
+    assert e_ref <= 0.04
+    assert e_cpu <= 0.06
+    assert not np.array_equal(bits(gpu), bits(cpu))  # different generators
+
+
+def test_uniform_frames_draw_new_samples(lib):
+    """A progressive frame (sample_offset) seeds new generators: frames differ
+    from each other, and their mean is closer to the converged image."""
+    sc = scenes.cornell_box()
+    w = h = 32
+    f2w = scenes.cornell_camera(w, h)
+    s = scenes.path_settings(5, "wide")
+    s.rng = 1
+    s.kernel_approach = 1
+    ref = _gpu(sc, s, 1024, w, h)
+    frames = [_gpu(sc, s, 4, w, h, api.SquareImage(w, h, f2w, sample_offset=4 * k))
+              for k in range(16)]
+    assert not np.array_equal(bits(frames[0]), bits(frames[1]))
+    assert rel_rmse(np.mean(frames, 0), ref) < 0.6 * rel_rmse(frames[0], ref)

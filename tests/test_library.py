@@ -176,10 +176,10 @@ def test_render_rejects_bad_requests_before_touching_the_gpu(lib):
     with pytest.raises(capi.PathError) as e:
         r.render(api.ExecutionModel.CPU, spec, out, sc, 4, s)
     assert e.value.status == 5
-    s.rng = 1
+    s.rng = 2
     with pytest.raises(capi.PathError) as e:
         r.render(api.ExecutionModel.GPU, spec, out, sc, 4, s)
-    assert e.value.status == 5
+    assert e.value.status == 1
     s = api.Settings()
     s.target_objects = 11
     with pytest.raises(capi.PathError) as e:

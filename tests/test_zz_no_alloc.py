@@ -45,7 +45,7 @@ def _sample_block_settings():
     return s
 
 
-@pytest.mark.parametrize("case", ["direct", "sample_blocks", "bgra"])
+@pytest.mark.parametrize("case", ["direct", "sample_blocks", "bgra", "uniform_rng"])
 def test_noalloc_matches_path_render_twice(lib, case):
     torch = pytest.importorskip("torch")
     scene = scenes.cornell_box()
@@ -53,6 +53,8 @@ def test_noalloc_matches_path_render_twice(lib, case):
     spp = 128 if case == "sample_blocks" else 16
     settings = _sample_block_settings() if case == "sample_blocks" else \
         scenes.path_settings(5, "binary")
+    if case == "uniform_rng":
+        settings.rng = 1
     spec = api.SquareImage(w, h, scenes.cornell_camera(w, h))
     r = api.Renderer()
     if case == "bgra":
