@@ -85,6 +85,11 @@ typedef enum {
   PATH_TERM_MULTIPLIER_FUNC = 2,
   PATH_TERM_NORMALIZE = 3
 } path_term_prob;
+/* Sobel: the scrambled Sobol table (rng_from_sequence_gen.h).  Uniform: one
+ * cuRAND XORWOW generator per sample, seeded with sample + location x spp and
+ * drawn with curand_uniform, 1.0 mapped to 0.0 (include/rng/uniform/
+ * uniform.h:18-76, the reference's GPU execution model; its CPU model draws
+ * std::mt19937 instead, so the two agree only in expectation). */
 typedef enum { PATH_RNG_SOBEL = 0, PATH_RNG_UNIFORM = 1 } path_rng;
 typedef enum {
   PATH_TRAVERSAL_BINARY = 0, /* the reference's binary SBVH and traversal order */
