@@ -172,6 +172,36 @@ __device__ __forceinline__ float byte8_float(uint32_t lo, uint32_t hi, int i) {
   return byte_float(i < 4 ? lo : hi, i & 3);
 }
 
+// two-lane FP32 (one instruction on sm_100 and later; each lane rounds like
+// the scalar operation)
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
+      "add.rn.f32x2 %0, ra, rb;\n\t}"
+      : "=l"(d)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
+}
+
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
+      "mov.b64 rc, {%5, %6};\n\tfma.rn.f32x2 %0, ra, rb, rc;\n\t}"
+      : "=l"(d)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
+}
+
+// bytes i of (n, f) as the pair of plane distances q * a + (bn, bf)
+__device__ __forceinline__ float2 plane_pair(uint32_t nl, uint32_t nh, uint32_t fl, uint32_t fh,
+                                             int i, float2 aa, float2 bb) {
+  const uint32_t wn = i < 4 ? nl : nh, wf = i < 4 ? fl : fh;
+  const float2 m = make_float2(__uint_as_float(__byte_perm(wn, 0x4B000000u, 0x7650u | (uint32_t)(i & 3))),
+                               __uint_as_float(__byte_perm(wf, 0x4B000000u, 0x7650u | (uint32_t)(i & 3))));
+  const float2 q = add2_rn(m, make_float2(-8388608.0f, -8388608.0f));
+  return fma2_rn(q, aa, bb);
+}
+
 constexpr int kWideStack = (int)kWideStackDepth;
 
 // three-operand minimum / maximum (one instruction on sm_100 and later)
@@ -307,26 +337,36 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
   const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
   const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
   const float tcull = w.best.t;
-  uint32_t hits = 0, tm = 0;
+  // slot i's box test into bit i (empty slots never pass: lo > hi)
+  uint32_t hm = 0;
+  const float2 aax = make_float2(ax, ax), aay = make_float2(ay, ay), aaz = make_float2(az, az);
+  const float2 bbx = make_float2(bnx, bfx), bby = make_float2(bny, bfy),
+               bbz = make_float2(bnz, bfz);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const float tnx = __fmaf_rn(byte8_float(nxl, nxh, i), ax, bnx);
-    const float tfx = __fmaf_rn(byte8_float(fxl, fxh, i), ax, bfx);
-    const float tny = __fmaf_rn(byte8_float(nyl, nyh, i), ay, bny);
-    const float tfy = __fmaf_rn(byte8_float(fyl, fyh, i), ay, bfy);
-    const float tnz = __fmaf_rn(byte8_float(nzl, nzh, i), az, bnz);
-    const float tfz = __fmaf_rn(byte8_float(fzl, fzh, i), az, bfz);
+    // (near, far) plane distance per axis
+    const float2 tx = plane_pair(nxl, nxh, fxl, fxh, i, aax, bbx);
+    const float2 ty = plane_pair(nyl, nyh, fyl, fyh, i, aay, bby);
+    const float2 tz = plane_pair(nzl, nzh, fzl, fzh, i, aaz, bbz);
     // tmin <= tmax && tmax >= 0 && tmin <= tcull, as one comparison (tcull >= 0)
-    const float tmin = fmax3(tnx, tny, fmaxf(tnz, 0.f));
-    const float tmax = fmin3(tfx, tfy, fminf(tfz, tcull));
-    const bool hit = tmin <= tmax;
-    const uint32_t meta = byte_of(n1.z, n1.w, i);
-    if ((imask >> i) & 1u) {
-      hits |= (hit ? 1u : 0u) << (i ^ (int)w.oct);
-    } else if (hit) {
-      // leaf slot: meta = count << 5 | first triangle offset
-      tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-    }
+    const float tmin = fmax3(tx.x, ty.x, fmaxf(tz.x, 0.f));
+    const float tmax = fmin3(tx.y, ty.y, fminf(tz.y, tcull));
+    hm |= (tmin <= tmax ? 1u : 0u) << i;
+  }
+  // internal children: slot i -> bit i ^ oct (ray order), by three swaps
+  uint32_t hits = hm & imask;
+  const uint32_t h1 = ((hits & 0x55u) << 1) | ((hits >> 1) & 0x55u);
+  hits = (w.oct & 1u) ? h1 : hits;
+  const uint32_t h2 = ((hits & 0x33u) << 2) | ((hits >> 2) & 0x33u);
+  hits = (w.oct & 2u) ? h2 : hits;
+  const uint32_t h4 = ((hits & 0x0fu) << 4) | (hits >> 4);
+  hits = (w.oct & 4u) ? h4 : hits;
+  // leaf children: meta = count << 5 | first triangle offset
+  uint32_t tm = 0;
+  for (uint32_t lh = hm & ~imask & 0xffu; lh != 0; lh &= lh - 1u) {
+    const uint32_t i = __ffs(lh) - 1;
+    const uint32_t meta = ((i < 4 ? n1.z : n1.w) >> (8 * (i & 3u))) & 0xffu;
+    tm |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
   }
   tri_base = n1.y;
   tmask = tm;
