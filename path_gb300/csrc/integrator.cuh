@@ -1116,7 +1116,7 @@ __device__ __forceinline__ rgb albedo_of(const Mat &m) {
 }
 
 template <bool kUniform>
-__device__ __noinline__ bool path_step(const RenderParams &P, const LightSet &L,
+__device__ __forceinline__ bool path_step(const RenderParams &P, const LightSet &L,
                                        PathStateT<kUniform> &s,
                                        const Hit &lh, const Hit &nh,
                                        StepTrace *tr = nullptr) {

@@ -408,8 +408,11 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // d log f / d(parameter) of that vertex is its parameter gradient; the
 // light sample adds its own term, and emission terms are linear.  Sampling
 // densities and the light table are held fixed (detached estimator).
+// path_step is inlined and the kernel held to 64 registers (4 CTAs of 256
+// per SM): the latency of the slot loads is hidden by more resident warps,
+// which measured faster than fewer warps without register spills.
 template <bool kGrad, bool kUniform>
-__global__ void __launch_bounds__(256) k_wf_shade(const WaveParams W, uint32_t parity) {
+__global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_t parity) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->active[parity];
   const uint32_t *in = W.active[parity];
