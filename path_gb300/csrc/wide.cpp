@@ -9,28 +9,9 @@ namespace pg {
 
 namespace {
 
-struct Child {
-  uint32_t bin; // binary node index
-  bool leaf;
-  uint32_t ntri;
-  float area;
-};
-
-uint32_t leaf_count(const BinaryNode &n) {
-  return (n.w1 & ~kNodeTag) - n.w0;
-}
-
 bool is_split(const BinaryNode &n) { return (n.w0 & kNodeTag) != 0; }
 
-Child make_child(const BinaryBVH &b, uint32_t i) {
-  const BinaryNode &n = b.nodes[i];
-  Child c;
-  c.bin = i;
-  c.leaf = !is_split(n);
-  c.ntri = c.leaf ? leaf_count(n) : 0;
-  c.area = area(n.aabb);
-  return c;
-}
+uint32_t leaf_count(const BinaryNode &n) { return (n.w1 & ~kNodeTag) - n.w0; }
 
 // Origin and scale of one axis of a wide node: the origin is a multiple of
 // the power-of-two scale, so every decoded plane p + q * 2^e (q < 256) is an
@@ -137,92 +118,177 @@ box wide_child_box(const WideNode &n, int slot) {
   return b;
 }
 
+namespace {
+
+// SAH weights of the collapse: a wide-node visit (eight box tests) against
+// one triangle test, per unit of surface area
+constexpr float kCostNode = 1.0f;
+constexpr float kCostTri = 0.3f;
+// triangles per leaf slot in the collapse: eight slots of at most four stay
+// within the 32 triangles a node addresses
+constexpr uint32_t kSlotTris = 4;
+
+// how the best forest of <= i slots represents a binary subtree
+enum How : uint8_t {
+  kFewer = 0, // the forest of <= i - 1 slots
+  kWide = 1,  // one wide node of its own
+  kLeaf = 2,  // leaf slots (binary leaves only)
+  kOpen = 3,  // kOpen + k: the left child's forest of <= k slots and the
+              // right child's of <= i - k
+};
+
+struct Collapse {
+  const BinaryBVH &bvh;
+  std::vector<std::array<float, 9>> cost; // [node][i], i = 1..8 slots
+  std::vector<std::array<uint8_t, 9>> how;
+  std::vector<uint8_t> wide_k;            // left share of a wide node's 8 slots
+
+  explicit Collapse(const BinaryBVH &b) : bvh(b) {}
+
+  uint32_t left(uint32_t n) const { return bvh.nodes[n].w0 & ~kNodeTag; }
+  uint32_t right(uint32_t n) const { return bvh.nodes[n].w1 & ~kNodeTag; }
+
+  // Ylitie, Karras and Laine (HPG 2017), section 3.1: the cost of a subtree
+  // as a forest of at most i slots of its parent wide node, minimised over
+  // leaf slots, wide nodes and distributions of the slots between the two
+  // children, bottom-up.
+  void solve() {
+    const size_t n = bvh.nodes.size();
+    cost.assign(n, {});
+    how.assign(n, {});
+    wide_k.assign(n, 0);
+    // post-order without recursion: a node after both of its children
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    std::vector<uint32_t> stack = {0};
+    while (!stack.empty()) {
+      const uint32_t v = stack.back();
+      stack.pop_back();
+      order.push_back(v);
+      if (is_split(bvh.nodes[v])) {
+        stack.push_back(left(v));
+        stack.push_back(right(v));
+      }
+    }
+    for (size_t o = order.size(); o-- > 0;) {
+      const uint32_t v = order[o];
+      const BinaryNode &b = bvh.nodes[v];
+      const float a = area(b.aabb);
+      std::array<float, 9> &c = cost[v];
+      std::array<uint8_t, 9> &h = how[v];
+      c[0] = INFINITY;
+      if (!is_split(b)) {
+        const uint32_t t = leaf_count(b);
+        const uint32_t slots = std::max(1u, (t + kSlotTris - 1) / kSlotTris);
+        const float tris = a * kCostTri * (float)t;
+        for (uint32_t i = 1; i <= 8; ++i) {
+          if (i >= slots) {
+            c[i] = tris;
+            h[i] = kLeaf;
+          } else {
+            c[i] = a * kCostNode + tris;
+            h[i] = kWide;
+          }
+        }
+        continue;
+      }
+      const std::array<float, 9> &cl = cost[left(v)], &cr = cost[right(v)];
+      float best = INFINITY;
+      uint8_t bk = 1;
+      for (uint32_t k = 1; k < 8; ++k) {
+        const float x = cl[k] + cr[8 - k];
+        if (x < best) {
+          best = x;
+          bk = (uint8_t)k;
+        }
+      }
+      wide_k[v] = bk;
+      c[1] = a * kCostNode + best;
+      h[1] = kWide;
+      for (uint32_t i = 2; i <= 8; ++i) {
+        c[i] = c[i - 1];
+        h[i] = kFewer;
+        for (uint32_t k = 1; k < i; ++k) {
+          const float x = cl[k] + cr[i - k];
+          if (x < c[i]) {
+            c[i] = x;
+            h[i] = (uint8_t)(kOpen + k);
+          }
+        }
+      }
+    }
+  }
+
+  // the slots of the best forest of <= i slots for subtree v
+  void forest(uint32_t v, uint32_t i, std::vector<Slot> &out) const {
+    while (how[v][i] == kFewer) {
+      --i;
+    }
+    const uint8_t h = how[v][i];
+    if (h == kWide) {
+      out.push_back({v, false, 0, 0});
+    } else if (h == kLeaf) {
+      const uint32_t t = leaf_count(bvh.nodes[v]);
+      if (t == 0) {
+        out.push_back({v, true, 0, 0});
+      }
+      for (uint32_t f = 0; f < t; f += kSlotTris) {
+        out.push_back({v, true, f, std::min(kSlotTris, t - f)});
+      }
+    } else {
+      const uint32_t k = h - kOpen;
+      forest(left(v), k, out);
+      forest(right(v), i - k, out);
+    }
+  }
+};
+
+} // namespace
+
 WideBVH build_wide(const BinaryBVH &bvh) {
   WideBVH out;
   if (bvh.nodes.empty()) {
     return out;
   }
+  Collapse col(bvh);
+  col.solve();
+  // a wide node stands for binary node `bin`; for a binary leaf, for its
+  // triangles from `first` on (a leaf of more than a node's 32 triangles
+  // continues in a child node with the same box)
   struct Job {
     uint32_t wide;
     uint32_t bin;
+    uint32_t first;
     uint32_t depth;
   };
   out.nodes.resize(1);
   std::vector<Job> stack;
-  stack.push_back({0, 0, 0});
+  stack.push_back({0, 0, 0, 0});
   while (!stack.empty()) {
     Job job = stack.back();
     stack.pop_back();
     out.depth = std::max(out.depth, job.depth);
-    std::vector<Child> kids;
+    std::vector<Slot> slots;
     const BinaryNode &root = bvh.nodes[job.bin];
     if (is_split(root)) {
-      kids.push_back(make_child(bvh, root.w0 & ~kNodeTag));
-      kids.push_back(make_child(bvh, root.w1 & ~kNodeTag));
+      const uint32_t k = col.wide_k[job.bin];
+      col.forest(col.left(job.bin), k, slots);
+      col.forest(col.right(job.bin), 8 - k, slots);
     } else {
-      kids.push_back(make_child(bvh, job.bin));
-    }
-    // greedy collapse: open the largest internal child while it fits
-    while (kids.size() < 8) {
-      int pick = -1;
-      for (size_t i = 0; i < kids.size(); ++i) {
-        if (kids[i].leaf) {
-          continue;
-        }
-        const BinaryNode &n = bvh.nodes[kids[i].bin];
-        Child l = make_child(bvh, n.w0 & ~kNodeTag);
-        Child r = make_child(bvh, n.w1 & ~kNodeTag);
-        uint32_t tris = l.ntri + r.ntri;
-        for (size_t k = 0; k < kids.size(); ++k) {
-          tris += kids[k].ntri;
-        }
-        if (tris > kMaxNodeTris) {
-          continue;
-        }
-        if (pick < 0 || kids[i].area > kids[(size_t)pick].area) {
-          pick = (int)i;
-        }
+      const uint32_t t = leaf_count(root);
+      uint32_t f = job.first, used = 0;
+      if (t == 0) {
+        slots.push_back({job.bin, true, 0, 0});
       }
-      if (pick < 0) {
-        break;
+      while (f < t && slots.size() < 7 && used + std::min(kMaxLeafTris, t - f) <= kMaxNodeTris) {
+        const uint32_t c = std::min(kMaxLeafTris, t - f);
+        slots.push_back({job.bin, true, f, c});
+        f += c;
+        used += c;
       }
-      const BinaryNode &n = bvh.nodes[kids[(size_t)pick].bin];
-      Child l = make_child(bvh, n.w0 & ~kNodeTag);
-      Child r = make_child(bvh, n.w1 & ~kNodeTag);
-      kids[(size_t)pick] = l;
-      kids.insert(kids.begin() + pick + 1, r);
-    }
-    // leaves larger than a slot can hold are split across slots with the
-    // same box; leaves that no longer fit get a node of their own
-    std::vector<Slot> slots;
-    for (const Child &c : kids) {
-      if (!c.leaf) {
-        slots.push_back({c.bin, false, 0, 0});
-        continue;
+      if (f < t) {
+        slots.push_back({job.bin, false, f, 0}); // the rest of the leaf
       }
-      for (uint32_t f = 0; f < c.ntri; f += kMaxLeafTris) {
-        slots.push_back({c.bin, true, f, std::min(kMaxLeafTris, c.ntri - f)});
-      }
-      if (c.ntri == 0) {
-        slots.push_back({c.bin, true, 0, 0});
-      }
-    }
-    if (slots.size() > 8) {
-      // demote whole leaves into nodes of their own until the slots fit
-      std::vector<Slot> merged;
-      size_t excess = slots.size() - 8;
-      for (size_t i = 0; i < slots.size(); ++i) {
-        const Slot &s = slots[i];
-        if (excess > 0 && s.leaf && s.first == 0 && leaf_count(bvh.nodes[s.bin]) > kMaxLeafTris) {
-          uint32_t used = (leaf_count(bvh.nodes[s.bin]) + kMaxLeafTris - 1) / kMaxLeafTris;
-          merged.push_back({s.bin, false, 0, 0});
-          i += used - 1;
-          excess -= std::min<size_t>(excess, used - 1);
-          continue;
-        }
-        merged.push_back(s);
-      }
-      slots.swap(merged);
     }
     WideNode wn;
     std::memset(&wn, 0, sizeof(wn));
@@ -266,7 +332,7 @@ WideBVH build_wide(const BinaryBVH &bvh) {
       if (!s.leaf) {
         wn.imask |= (uint8_t)(1u << i);
         wn.meta[i] = (uint8_t)rank;
-        children.push_back({child_base + rank, s.bin, job.depth + 1});
+        children.push_back({child_base + rank, s.bin, s.first, job.depth + 1});
         ++rank;
       } else {
         const BinaryNode &ln = bvh.nodes[s.bin];

@@ -1,14 +1,18 @@
 // Compressed 8-wide BVH built from the binary SBVH.
 //
-// Each wide node takes the children of a binary node and repeatedly opens the
-// internal child with the largest surface area until it has eight children
-// (or no internal child can be opened without exceeding 32 leaf triangles);
-// this is the greedy collapse used for wide BVHs in Ylitie, Karras and Laine,
-// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs"
-// (HPG 2017), whose 80-byte quantised node this layout follows.  Leaves keep
-// the binary leaves' triangles (duplicates from spatial splits included), so
-// the closest hit found through the wide BVH is the one the binary BVH finds,
-// up to the order in which equal-distance candidates are met.
+// The binary tree is collapsed by the surface-area cost optimisation of
+// Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs
+// Through Compressed Wide BVHs" (HPG 2017, section 3.1): bottom-up, the
+// cheapest way to represent every binary subtree as a forest of at most i
+// slots (i = 1..8) of its parent -- leaf slots of at most four triangles,
+// a wide node of its own, or a split of the slots between its two children
+// -- then top-down, every wide node takes the best forest of eight slots of
+// its binary node's children.  The 80-byte quantised node follows the same
+// paper.  Leaves keep the binary leaves' triangles (duplicates from spatial
+// splits included), so the closest hit found through the wide BVH is the one
+// the binary BVH finds, up to the order in which equal-distance candidates
+// are met; a binary leaf of more than a node's 32 triangles continues in a
+// child node with the same box.
 #pragma once
 
 #include "devtypes.h"

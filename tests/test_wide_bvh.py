@@ -106,10 +106,33 @@ def test_wide_bvh_covers_every_triangle_and_children_contain_their_subtrees():
     subtree_box(0)
 
 
-@pytest.mark.parametrize("case", ["random", "sphere", "grid_ties"])
+def _big_leaf_scene(rng):
+    """90 copies of one triangle (the SBVH cannot split them: one binary leaf
+    of 90, more than the 32 triangles a wide node addresses) among random
+    triangles."""
+    one = np.array([[-0.5, -0.5, 0.2, 0.5, -0.5, 0.2, 0.0, 0.5, 0.2]], np.float32)
+    return np.concatenate([rng.uniform(-1, 1, (60, 9)).astype(np.float32),
+                           np.repeat(one, 90, 0)])
+
+
+def test_wide_bvh_splits_a_leaf_larger_than_a_node():
+    tris = _big_leaf_scene(np.random.default_rng(5))
+    w = api.wide_build(tris, api.Settings())
+    assert sorted(w["leaf_refs"].tolist()) == list(range(len(tris)))
+    for node in w["nodes"]:
+        used = sum(int(m) >> 5 for s, m in enumerate(node["meta"])
+                   if not (int(node["imask"]) >> s) & 1)
+        assert used <= 32
+
+
+@pytest.mark.parametrize("case", ["random", "sphere", "grid_ties", "big_leaf"])
 def test_wide_traversal_mirror_finds_the_order_independent_closest_hit(case):
     rng = np.random.default_rng(3)
-    if case == "random":
+    if case == "big_leaf":
+        tris = _big_leaf_scene(rng)
+        o = np.concatenate([rng.uniform(-0.3, 0.3, (100, 2)), np.ones((100, 1))], 1)
+        d = rng.normal(size=(100, 3)) * [0.1, 0.1, 0.0] + [0.0, 0.0, -1.0]
+    elif case == "random":
         tris = rng.uniform(-1, 1, (300, 9)).astype(np.float32)
         o = rng.uniform(-1, 1, (200, 3))
         d = rng.normal(size=(200, 3))
