@@ -410,8 +410,10 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // densities and the light table are held fixed (detached estimator).
 // path_step is inlined and the kernel held to 64 registers (4 CTAs of 256
 // per SM): the latency of the slot loads is hidden by more resident warps,
-// which measured faster than fewer warps without register spills.
-template <bool kGrad, bool kUniform>
+// which measured faster than fewer warps without register spills.  kCache
+// (paths end into the radiance cache) is a template parameter so that the
+// plain kernel carries none of the cache-query code.
+template <bool kGrad, bool kUniform, bool kCache>
 __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_t parity) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->active[parity];
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
       Hit nh = s.has_next ? unpack_hit(W.hit_ext[slot]) : no_hit();
       if (!kGrad) {
         StepTrace tr;
-        StepTrace *trp = W.cache_q != nullptr ? &tr : nullptr;
+        StepTrace *trp = kCache ? &tr : nullptr;
         bool cont =
             path_continues(W.P, s, path_step(W.P, scene_lights(W, scene), s, lh, nh, trp));
         if (trp != nullptr && tr.cache_query) {
@@ -657,16 +659,23 @@ cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_
                                    cudaStream_t s, bool grad) {
   dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
   const bool u = w.P.rng_uniform != 0;
+  const bool cache = w.cache_q != nullptr;
   if (grad) {
     if (u) {
-      dev::k_wf_shade<true, true><<<shade_grid, 256, 0, s>>>(w, parity);
+      dev::k_wf_shade<true, true, false><<<shade_grid, 256, 0, s>>>(w, parity);
     } else {
-      dev::k_wf_shade<true, false><<<shade_grid, 256, 0, s>>>(w, parity);
+      dev::k_wf_shade<true, false, false><<<shade_grid, 256, 0, s>>>(w, parity);
+    }
+  } else if (cache) {
+    if (u) {
+      dev::k_wf_shade<false, true, true><<<shade_grid, 256, 0, s>>>(w, parity);
+    } else {
+      dev::k_wf_shade<false, false, true><<<shade_grid, 256, 0, s>>>(w, parity);
     }
   } else if (u) {
-    dev::k_wf_shade<false, true><<<shade_grid, 256, 0, s>>>(w, parity);
+    dev::k_wf_shade<false, true, false><<<shade_grid, 256, 0, s>>>(w, parity);
   } else {
-    dev::k_wf_shade<false, false><<<shade_grid, 256, 0, s>>>(w, parity);
+    dev::k_wf_shade<false, false, false><<<shade_grid, 256, 0, s>>>(w, parity);
   }
   return cudaGetLastError();
 }
