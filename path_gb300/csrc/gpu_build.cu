@@ -12,10 +12,13 @@
 // Stages: Morton code of each centroid (10 bits per axis) -> radix sort of
 // (code, triangle) pairs -> internal nodes of the radix tree (longest common
 // prefix, ties broken by position) with parent links -> boxes bottom-up (the
-// second child to arrive at a node merges) -> collapse: every wide node
-// opens the largest-area internal node among its children until it has
-// eight, places them in octant slots (as the host builder does), quantises
-// their boxes (the same exact-plane frame), and queues its internal children.
+// second child to arrive at a node merges), together with the surface-area
+// cost optimisation of the collapse (the host builder's: per binary node the
+// cheapest forest of at most 1..8 slots, from its children's) -> collapse:
+// every wide node takes the best forest of eight slots of its binary node's
+// children, places them in octant slots (as the host builder does),
+// quantises their boxes (the same exact-plane frame), and queues its
+// internal children.
 #include "geom.h"
 #include "gpu_build.h"
 
@@ -122,10 +125,25 @@ __device__ __forceinline__ box load_box_cg(const box *b) {
   return o;
 }
 
-// boxes [internal n-1 | leaves n], bottom-up; flags start at zero
+// collapse costs (as the host builder: a wide-node visit 1, a triangle test
+// 0.3, per unit area); every leaf of the linear BVH is one triangle
+constexpr float kCostNode = 1.0f;
+constexpr float kCostTri = 0.3f;
+// how the best forest of <= i slots represents a binary subtree
+constexpr uint8_t kFewer = 0, kWide = 1, kOpen = 3; // kOpen + k: k slots left
+
+// the cost of child c's best forest of <= i slots (i = 1..8)
+__device__ __forceinline__ float child_cost(uint32_t c, const box &cb, const float *cost,
+                                            int i) {
+  return (c & kLeafBit) ? area(cb) * kCostTri : __ldcg(cost + 8 * (size_t)c + (i - 1));
+}
+
+// boxes [internal n-1 | leaves n] and the collapse costs of internal nodes
+// ([n-1][8] cost and decision of the forests of 1..8 slots, the left share
+// of a wide node's 8 slots), bottom-up; flags start at zero
 __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const uint32_t *left,
                         const uint32_t *right, const uint32_t *parent, box *boxes,
-                        uint32_t *flags) {
+                        uint32_t *flags, float *cost, uint8_t *how, uint8_t *wide_k) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) {
     return;
@@ -145,7 +163,38 @@ __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const
     // the sibling's box was written by another thread: read past L1
     const box bl = load_box_cg(boxes + ((l & kLeafBit) ? (n - 1) + (l & ~kLeafBit) : l));
     const box br = load_box_cg(boxes + ((r & kLeafBit) ? (n - 1) + (r & ~kLeafBit) : r));
-    boxes[node] = merge(bl, br);
+    const box bn = merge(bl, br);
+    boxes[node] = bn;
+    float cl[9], cr[9];
+    for (int i = 1; i <= 8; ++i) {
+      cl[i] = child_cost(l, bl, cost, i);
+      cr[i] = child_cost(r, br, cost, i);
+    }
+    float best = INFINITY;
+    uint8_t bk = 1;
+    for (int k = 1; k < 8; ++k) {
+      const float x = cl[k] + cr[8 - k];
+      if (x < best) {
+        best = x;
+        bk = (uint8_t)k;
+      }
+    }
+    wide_k[node] = bk;
+    float c = area(bn) * kCostNode + best;
+    cost[8 * (size_t)node] = c;
+    how[8 * (size_t)node] = kWide;
+    for (int i = 2; i <= 8; ++i) {
+      uint8_t h = kFewer;
+      for (int k = 1; k < i; ++k) {
+        const float x = cl[k] + cr[i - k];
+        if (x < c) {
+          c = x;
+          h = (uint8_t)(kOpen + k);
+        }
+      }
+      cost[8 * (size_t)node + (i - 1)] = c;
+      how[8 * (size_t)node + (i - 1)] = h;
+    }
     if (node == 0) {
       return;
     }
@@ -183,9 +232,9 @@ struct Entry {
 };
 
 __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, const uint32_t *left,
-                           const uint32_t *right, const box *boxes, const Entry *in,
-                           uint32_t n_in, Entry *out, uint32_t *counters, WideNode *nodes,
-                           float *wide_tris) {
+                           const uint32_t *right, const box *boxes, const uint8_t *how,
+                           const uint8_t *wide_k, const Entry *in, uint32_t n_in, Entry *out,
+                           uint32_t *counters, WideNode *nodes, float *wide_tris) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n_in) {
     return;
@@ -199,28 +248,36 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
   if (e.bin & kLeafBit) {
     kids[nk++] = e.bin;
   } else {
-    kids[nk++] = left[e.bin];
-    kids[nk++] = right[e.bin];
-  }
-  // open the largest internal child while there is room
-  while (nk < 8) {
-    int pick = -1;
-    float best = -1.f;
-    for (uint32_t i = 0; i < nk; ++i) {
-      if (!(kids[i] & kLeafBit)) {
-        const float a = area(box_of(kids[i]));
-        if (a > best) {
-          best = a;
-          pick = (int)i;
-        }
+    // the best forest of eight slots: (subtree, slots) pairs still to decode
+    uint32_t st_node[8], st_slots[8];
+    uint32_t sp = 0;
+    const uint32_t k = wide_k[e.bin];
+    st_node[sp] = right[e.bin];
+    st_slots[sp++] = 8 - k;
+    st_node[sp] = left[e.bin];
+    st_slots[sp++] = k;
+    while (sp > 0 && nk < 8) {
+      --sp;
+      const uint32_t v = st_node[sp];
+      uint32_t i = st_slots[sp];
+      if (v & kLeafBit) {
+        kids[nk++] = v; // a triangle
+        continue;
+      }
+      while (i > 1 && how[8 * (size_t)v + (i - 1)] == kFewer) {
+        --i;
+      }
+      const uint8_t h = how[8 * (size_t)v + (i - 1)];
+      if (i == 1 || h == kWide) {
+        kids[nk++] = v; // a wide node of its own
+      } else {
+        const uint32_t kk = h - kOpen; // 1 <= kk < i: both children get a slot
+        st_node[sp] = right[v];
+        st_slots[sp++] = i - kk;
+        st_node[sp] = left[v];
+        st_slots[sp++] = kk;
       }
     }
-    if (pick < 0) {
-      break;
-    }
-    const uint32_t b = kids[pick];
-    kids[pick] = left[b];
-    kids[nk++] = right[b];
   }
   box all = empty_box();
   for (uint32_t i = 0; i < nk; ++i) {
@@ -348,7 +405,8 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
     }                                                                          \
   } while (0)
   const size_t nn = n;
-  DeviceBuffer keys, vals, keys2, tmp, left, right, parent, boxes, flags, qa, qb, counters;
+  DeviceBuffer keys, vals, keys2, tmp, left, right, parent, boxes, flags, qa, qb, counters, cost,
+      how, wide_k;
   PG_GB_TRY(keys.ensure(nn * 4), "gpu build");
   PG_GB_TRY(vals.ensure(nn * 4), "gpu build");
   PG_GB_TRY(keys2.ensure(nn * 4), "gpu build");
@@ -376,6 +434,9 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   PG_GB_TRY(boxes.ensure((n_int + nn) * sizeof(box)), "gpu build");
   PG_GB_TRY(flags.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
   PG_GB_TRY(cudaMemsetAsync(flags.get(), 0, std::max<size_t>(n_int, 1) * 4, s), "gpu build");
+  PG_GB_TRY(cost.ensure(std::max<size_t>(n_int, 1) * 32), "gpu build");
+  PG_GB_TRY(how.ensure(std::max<size_t>(n_int, 1) * 8), "gpu build");
+  PG_GB_TRY(wide_k.ensure(std::max<size_t>(n_int, 1)), "gpu build");
   if (n_int > 0) {
     dev::k_radix_tree<<<(uint32_t)((n_int + bs - 1) / bs), bs, 0, s>>>(
         keys2.as<uint32_t>(), n, left.as<uint32_t>(), right.as<uint32_t>(),
@@ -384,7 +445,8 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   }
   dev::k_boxes<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(),
                                  right.as<uint32_t>(), parent.as<uint32_t>(), boxes.as<box>(),
-                                 flags.as<uint32_t>());
+                                 flags.as<uint32_t>(), cost.as<float>(), how.as<uint8_t>(),
+                                 wide_k.as<uint8_t>());
   PG_GB_TRY(cudaGetLastError(), "boxes");
   // collapse: a wide node has at most 8 children and at least 2 binary
   // nodes below it, so n wide nodes and n queue entries always suffice
@@ -406,7 +468,8 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
     PG_GB_TRY(cudaMemsetAsync(counters.as<uint32_t>() + 2, 0, 4, s), "gpu build");
     dev::k_collapse<<<(n_in + 127) / 128, 128, 0, s>>>(
         t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(), right.as<uint32_t>(),
-        boxes.as<box>(), cur->as<dev::Entry>(), n_in, nxt->as<dev::Entry>(),
+        boxes.as<box>(), how.as<uint8_t>(), wide_k.as<uint8_t>(), cur->as<dev::Entry>(), n_in,
+        nxt->as<dev::Entry>(),
         counters.as<uint32_t>(), out.nodes.as<WideNode>(), out.wide_tris.as<float>());
     PG_GB_TRY(cudaGetLastError(), "collapse");
     uint32_t h[4];

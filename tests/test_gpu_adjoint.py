@@ -35,11 +35,12 @@ DEPTH = 4
 STEP = 1e-3
 
 
-def _setup(dir_sampler=0, spp=SPP):
+def _setup(dir_sampler=0, spp=SPP, rng=0):
     sc, mats = scenes.patch_cornell(seed=1)
     s = scenes.path_settings(DEPTH, "wide")
     s.kernel_approach = 1
     s.dir_sampler = dir_sampler
+    s.rng = rng
     spec = api.SquareImage(W, H, scenes.cornell_camera(W, H))
     rend = diff.Renderable(sc, mats, spec, spp, s)
     p0 = diff.params_of(mats)
@@ -79,13 +80,16 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("sampler", ["bsdf", "uniform"])
+@pytest.mark.parametrize("sampler", ["bsdf", "uniform", "bsdf_uniform_rng"])
 def test_adjoint_matches_central_differences_on_the_gpu(lib, sampler):
-    rend, mats, p0, target = _setup(dir_sampler=0 if sampler == "bsdf" else 1)
+    """bsdf_uniform_rng: the replay re-seeds each path's XORWOW generator, so
+    the Uniform RNG gives common random numbers too."""
+    rend, mats, p0, target = _setup(dir_sampler=1 if sampler == "uniform" else 0,
+                                    rng=1 if sampler == "bsdf_uniform_rng" else 0)
     img = rend.render(p0)
     g_adj = rend.adjoint(p0, (2.0 * (img.astype(np.float64) - target)).astype(np.float32))
     pairs = _active(mats)
-    if sampler == "bsdf":
+    if sampler != "uniform":
         pairs = [pq for pq in pairs if pq[1] != 3]
     g_fd = _fd(rend.render, p0, target, pairs)
     a = np.array([g_adj[i, j] for i, j in pairs])
