@@ -113,14 +113,19 @@ using tc::smem_offset;
 // hash features of levels [l0, l1) of a query's position (trilinear
 // interpolation of the 8 grid vertices per level) into in[2 (l - l0)] and
 // in[2 (l - l0) + 1]
-__device__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l0, uint32_t l1,
-                                  float *in) {
+// levels [l0, l0 + kN), unrolled so that all 8 kN corner loads can be in
+// flight together (the encoding waits on these table reads)
+template <uint32_t kN>
+__device__ __forceinline__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l0,
+                                                  float *in) {
   float p[3];
   for (int a = 0; a < 3; ++a) {
     p[a] = (q[a] - C.lo[a]) * C.inv_extent[a];
     p[a] = fminf(fmaxf(p[a], 0.f), 1.f);
   }
-  for (uint32_t l = l0; l < l1; ++l) {
+#pragma unroll
+  for (uint32_t j = 0; j < kN; ++j) {
+    const uint32_t l = l0 + j;
     const float res = C.level_res[l];
     const uint32_t side = (uint32_t)res + 1;
     float x[3], fr[3];
@@ -132,6 +137,7 @@ __device__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l
       fr[a] = x[a] - fl;
     }
     float f0 = 0.f, f1 = 0.f;
+#pragma unroll
     for (uint32_t c = 0; c < 8; ++c) {
       const uint32_t gx = c0[0] + (c & 1u), gy = c0[1] + ((c >> 1) & 1u),
                      gz = c0[2] + ((c >> 2) & 1u);
@@ -142,8 +148,8 @@ __device__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l
       f0 += w * e.x;
       f1 += w * e.y;
     }
-    in[2 * (l - l0)] = f0;
-    in[2 * (l - l0) + 1] = f1;
+    in[2 * j] = f0;
+    in[2 * j + 1] = f1;
   }
 }
 
@@ -151,7 +157,10 @@ __device__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l
 // features of the position, then direction, normal, albedo (9 floats), zero
 // padding to kNrcIn
 __device__ void nrc_encode(const NrcParams &C, const float *q, float *in) {
-  nrc_encode_levels(C, q, 0, kNrcLevels, in);
+#pragma unroll
+  for (uint32_t g = 0; g < kNrcLevels; g += 4) {
+    nrc_encode_levels<4>(C, q, g, in + 2 * g);
+  }
   for (int k = 0; k < 9; ++k) {
     in[32 + k] = q[3 + k];
   }
@@ -232,7 +241,7 @@ __device__ __forceinline__ void tc_wait(TcSync &s, uint32_t tid, uint32_t *err) 
 // quarter) and columns 16 (w / 4) ... 16 (w / 4) + 15.
 constexpr uint32_t kInferThreads = 512;
 
-__global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const NrcParams C,
+__global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const __grid_constant__ NrcParams C,
                                                              const float *queries, uint32_t n,
                                                              float *out, uint32_t *err) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const NrcParams C,
     float in[8];
     const uint32_t l0 = lgroup * 4;
     if (qi < n) {
-      nrc_encode_levels(C, queries + (size_t)qi * 12, l0, l0 + 4, in);
+      nrc_encode_levels<4>(C, queries + (size_t)qi * 12, l0, in);
     } else {
       for (int k = 0; k < 8; ++k) {
         in[k] = 0.f;
@@ -327,7 +336,7 @@ __global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const NrcParams C,
 // dX_l = dY_l . W_l, ReLU-masked into dY_{l-1}.  dLoss/d(hash features) of
 // every record goes to d_feat [n][32]; the CTA's dW is added to grad_w at
 // the end.  inv_batch scales the loss (1 / records of the step).
-__global__ void __launch_bounds__(128) k_nrc_train(const NrcParams C, const float *records,
+__global__ void __launch_bounds__(128) k_nrc_train(const __grid_constant__ NrcParams C, const float *records,
                                                    uint32_t n, float inv_batch, float *grad_w,
                                                    float *d_feat, unsigned char *scratch,
                                                    float *loss_out, uint32_t *err) {
@@ -493,7 +502,7 @@ __global__ void __launch_bounds__(128) k_nrc_train(const NrcParams C, const floa
 
 // dLoss/d(hash table): each record's feature gradient spread over the
 // eight grid vertices of every level with the trilinear weights
-__global__ void k_nrc_grid_backward(const NrcParams C, const float *records, uint32_t n,
+__global__ void k_nrc_grid_backward(const __grid_constant__ NrcParams C, const float *records, uint32_t n,
                                     const float *d_feat, float2 *grad_table) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) {
