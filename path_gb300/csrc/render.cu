@@ -40,6 +40,126 @@ __global__ void __launch_bounds__(256, 4) k_render(const RenderParams P) {
   }
 }
 
+// The megakernel on the 8-wide BVH with warp-cooperative traversal.  Every
+// thread keeps its WorkDivision samples and sums their radiance serially in
+// sample order, exactly as k_render does, so the image is the same bit for
+// bit; but the paths of a warp advance together one BVH node per lane and
+// step (idle lanes start their next sample), leaf triangles are tested by
+// the whole warp, and the lanes whose rays are done shade together once
+// kShadeLanes of them are ready (or no lane is tracing).  Per lane the two
+// rays of a vertex are traced in turn: the pending light ray, then the
+// extension ray.  On the large-mesh room, 28 ready lanes measured best (8:
+// 101, 16: 121, 24: 135, 28: 140, 32: 134 Msamples/s; the per-thread
+// kernel 68).
+constexpr uint32_t kShadeLanes = 28;
+
+template <bool kCount, bool kUniform>
+__global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
+  const uint32_t block = blockIdx.x + P.start_block;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t lane = tid & 31;
+  const ThreadWork tw = band_work(P, block, tid);
+  Counts cnt = {0, 0, 0};
+  rgb total = zero_rgb();
+  uint32_t smp = tw.start;
+  const uint32_t end = tw.exit ? tw.start : tw.end;
+  const LightSet L = lights_of(P);
+  PathStateT<kUniform> s;
+  uint32_t xw[kUniform ? kXorwowWords : 1];
+  WideWalk w;
+  w.done = true;
+  uint32_t st_base[kWideStack];
+  uint32_t st_bits[kWideStack];
+  Hit lh = no_hit(), nh = no_hit();
+  // 0: start the next sample, 1: tracing the light ray, 2: tracing the
+  // extension ray, 3: ready to shade, 4: all samples done
+  uint32_t phase = 0;
+  // the rays of the vertex just shaded (or of the camera sample)
+  auto begin_rays = [&]() {
+    lh = no_hit();
+    nh = no_hit();
+    ray r;
+    r.o = s.o;
+    if (s.has_light) {
+      r.d = s.ld;
+      wide_begin(P, w, r, light_bound(s.light_target), s.light_target);
+      phase = 1;
+    } else {
+      r.d = s.d;
+      wide_begin(P, w, r, PG_INF, -PG_INF);
+      phase = 2;
+    }
+    if (kCount) {
+      ++cnt.rays;
+    }
+  };
+  while (true) {
+    if (phase == 0) {
+      if (smp < end) {
+        path_begin(P, smp, tw.x, tw.y, s, xw, 1);
+        begin_rays();
+      } else {
+        phase = 4;
+      }
+    }
+    if (__ballot_sync(kFull, phase != 4) == 0) {
+      break;
+    }
+    const bool tracing = phase == 1 || phase == 2;
+    uint32_t tri_base = 0, tmask = 0;
+    if (tracing && !w.done) {
+      wide_node<kCount>(P, w, st_base, st_bits, cnt, tri_base, tmask);
+    }
+    warp_triangles<kCount>(P, w, tri_base, tmask, lane, cnt);
+    if (tracing && w.done) {
+      if (phase == 1) {
+        lh = w.best;
+        if (s.has_next) {
+          ray r;
+          r.o = s.o;
+          r.d = s.d;
+          wide_begin(P, w, r, PG_INF, -PG_INF);
+          phase = 2;
+          if (kCount) {
+            ++cnt.rays;
+          }
+        } else {
+          phase = 3;
+        }
+      } else {
+        nh = w.best;
+        phase = 3;
+      }
+    }
+    const uint32_t ready = __ballot_sync(kFull, phase == 3);
+    const uint32_t busy = __ballot_sync(kFull, phase == 1 || phase == 2);
+    if (ready != 0 && (__popc(ready) >= kShadeLanes || busy == 0) && phase == 3) {
+      if (path_continues(P, s, path_step(P, L, s, lh, nh))) {
+        begin_rays();
+      } else {
+        total = total + s.total;
+        ++smp;
+        phase = 0;
+      }
+    }
+  }
+  const uint32_t sbs = P.wd.sample_block_size;
+  total = sub_block_reduce(total, tid, sbs);
+  if (!tw.exit && tid % sbs == 0) {
+    const uint32_t nsb = P.wd.num_sample_blocks;
+    const size_t idx = (block % nsb) + (size_t)nsb * (tw.x + (size_t)tw.y * P.x_dim);
+    if (nsb == 1) {
+      total = total / (float)P.spp;
+    }
+    write_pixel(P.out_rgb, P.out_bgra, P.output_bgra && nsb == 1, idx, total);
+  }
+  if (kCount) {
+    atomicAdd(P.counters + 0, (unsigned long long)cnt.rays);
+    atomicAdd(P.counters + 1, (unsigned long long)cnt.nodes);
+    atomicAdd(P.counters + 2, (unsigned long long)cnt.tris);
+  }
+}
+
 // the mega kernel with OutputPerStep output (mega_kernel/run_impl.h:
 // 160-185): per-thread step sums, one sub-block reduction per step
 template <uint32_t kTrav, bool kUniform>
@@ -142,8 +262,17 @@ __global__ void k_pmath(uint32_t fn, const float *x, const float *y, float *out,
 namespace {
 template <uint32_t kTrav, bool kCount>
 void render_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s) {
+  // the 8-wide traversal runs warp-cooperatively (InitialIdxAndDir, whose
+  // first hit is given, keeps the per-thread kernel)
+  const bool coop = kTrav == kTravWide && p.initial_idx == nullptr;
   if (p.rng_uniform) {
-    dev::k_render<kTrav, kCount, true><<<grid, block, 0, s>>>(p);
+    if (coop) {
+      dev::k_render_coop<kCount, true><<<grid, block, 0, s>>>(p);
+    } else {
+      dev::k_render<kTrav, kCount, true><<<grid, block, 0, s>>>(p);
+    }
+  } else if (coop) {
+    dev::k_render_coop<kCount, false><<<grid, block, 0, s>>>(p);
   } else {
     dev::k_render<kTrav, kCount, false><<<grid, block, 0, s>>>(p);
   }
