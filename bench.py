@@ -23,7 +23,8 @@ step is one full render.
   workload, all host threads.
 
 ``--impl reference`` times that CPU restatement alone (the reference itself
-cannot be built on this image).  N > 1 runs independent
+cannot be built here: it needs clang as its CUDA compiler and libraries that
+are not installed).  N > 1 runs independent
 replicas, one per GPU (the render has no data-path exchange).
 """
 

@@ -126,9 +126,12 @@ def test_cornell_full_size(lib, oracle, traversal):
     assert 0.15 < float(gpu.mean()) < 0.6
 
 
-def test_cornell_bgra(lib, oracle):
+@pytest.mark.parametrize("traversal", ["binary", "wide"])
+def test_cornell_bgra(lib, oracle, traversal):
+    """BGRA output (tone map v / (v + 1), x 255 truncated) of the per-thread
+    (binary) and warp-cooperative (8-wide) megakernels."""
     sc = scenes.cornell_box()
-    s = scenes.path_settings(5, "binary")
+    s = scenes.path_settings(5, traversal)
     f2w = scenes.cornell_camera(48, 40)
     gpu = _render_gpu(sc, s, 8, 48, 40, f2w, bgra=True)
     arr = ol.SceneArrays(sc.export())
