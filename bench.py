@@ -267,7 +267,10 @@ def run_cache(args, rank, world, local_rank):
     until the error is <= 0.02.  Cache: frames whose paths end into the
     cache after 2 bounces, each followed by 4 Adam steps on 2^16 records
     from fresh full-length paths, accumulated the same way (the first
-    frames, with an untrained cache, included).  Wall time of render +
+    frames, with an untrained cache, included).  Then a tuned cache (paths
+    end at vertex 3, 2^14 records x 2 steps per frame) and, as its control,
+    the same truncation with the cache left untrained (what ending the paths
+    early does without the network).  Wall time of render +
     training calls."""
     import torch
     from path_gb300 import api, scenes
@@ -336,15 +339,18 @@ def run_cache(args, rank, world, local_rank):
         return out_d
 
     plain = run(False)
-    # the configuration on the command line (defaults: the specified one), then
-    # a tuned one: paths end one bounce later, 4x the records and 4x the Adam
-    # steps per frame, two training-only frames first
+    # the configuration on the command line (defaults: the specified one),
+    # then a tuned one (picked by a search on this scene over the depth, the
+    # records and the steps per frame) and its untrained control
     spec_cfg = {"cache_depth": args.cache_depth, "train_paths": args.train_paths,
                 "train_steps": args.train_steps, "pretrain_frames": args.pretrain_frames}
     runs = {"cached": run(True, spec_cfg)}
+    controls = {}
     if not args.no_tuned_cache:
-        runs["cached_tuned"] = run(True, {"cache_depth": 3, "train_paths": 1 << 18,
-                                          "train_steps": 16, "pretrain_frames": 2})
+        tuned = {"cache_depth": 3, "train_paths": 1 << 14, "train_steps": 2,
+                 "pretrain_frames": 0}
+        runs["cached_tuned"] = run(True, tuned)
+        controls["cached_tuned_untrained"] = run(True, dict(tuned, train_steps=0))
     reached = [k for k in runs if runs[k]["reached"]]
     best = min(reached, key=lambda k: runs[k]["seconds"]) if reached else None
     line = {
@@ -354,7 +360,7 @@ def run_cache(args, rank, world, local_rank):
         "config": {"workload": f"{desc} in 4-spp frames; reference 4096 spp FP64",
                    "value_from": best,
                    "cache": runs[best]["cache"] if best else runs["cached"]["cache"]},
-        "plain": plain, **runs,
+        "plain": plain, **runs, **controls,
         "ratio_cached_over_plain": (runs[best]["seconds"] / plain["seconds"]
                                     if plain["reached"] and best else None),
         "reference_seconds": ref_s,
