@@ -97,7 +97,18 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
     if (phase == 0) {
       if (smp < end) {
         path_begin(P, smp, tw.x, tw.y, s, xw, 1);
-        begin_rays();
+        if (P.initial_idx != nullptr) {
+          // InitialIdxAndDir: the first hit is the caller's, at distance 1
+          // from the front (initial_ray_sample.h:58-74)
+          lh = no_hit();
+          nh.t = 1.f;
+          nh.idx = P.initial_idx[tw.x];
+          nh.ok = true;
+          nh.back = false;
+          phase = 3;
+        } else {
+          begin_rays();
+        }
       } else {
         phase = 4;
       }
@@ -262,17 +273,15 @@ __global__ void k_pmath(uint32_t fn, const float *x, const float *y, float *out,
 namespace {
 template <uint32_t kTrav, bool kCount>
 void render_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s) {
-  // the 8-wide traversal runs warp-cooperatively (InitialIdxAndDir, whose
-  // first hit is given, keeps the per-thread kernel)
-  const bool coop = kTrav == kTravWide && p.initial_idx == nullptr;
-  if (p.rng_uniform) {
-    if (coop) {
+  if constexpr (kTrav == kTravWide) {
+    // the 8-wide traversal runs warp-cooperatively
+    if (p.rng_uniform) {
       dev::k_render_coop<kCount, true><<<grid, block, 0, s>>>(p);
     } else {
-      dev::k_render<kTrav, kCount, true><<<grid, block, 0, s>>>(p);
+      dev::k_render_coop<kCount, false><<<grid, block, 0, s>>>(p);
     }
-  } else if (coop) {
-    dev::k_render_coop<kCount, false><<<grid, block, 0, s>>>(p);
+  } else if (p.rng_uniform) {
+    dev::k_render<kTrav, kCount, true><<<grid, block, 0, s>>>(p);
   } else {
     dev::k_render<kTrav, kCount, false><<<grid, block, 0, s>>>(p);
   }
