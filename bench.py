@@ -393,7 +393,8 @@ def main():
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
                     help="wavefront (streaming) or megakernel integration")
-    ap.add_argument("--cpu-rows", type=int, default=16)
+    ap.add_argument("--cpu-rows", type=int, default=128,
+                    help="image rows (centred) in the CPU baseline sample: about 7 s on 16 cores")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-megakernel", action="store_true",
                     help="skip the megakernel comparison render")
