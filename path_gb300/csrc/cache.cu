@@ -241,9 +241,12 @@ __device__ __forceinline__ void tc_wait(TcSync &s, uint32_t tid, uint32_t *err) 
 // quarter) and columns 16 (w / 4) ... 16 (w / 4) + 15.
 constexpr uint32_t kInferThreads = 512;
 
+// live (optional): per query 3 floats, all zero for a query no path uses
+// (its encoding is skipped and its output is not meaningful)
 __global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const __grid_constant__ NrcParams C,
                                                              const float *queries, uint32_t n,
-                                                             float *out, uint32_t *err) {
+                                                             const float *live, float *out,
+                                                             uint32_t *err) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
@@ -270,7 +273,10 @@ __global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const __grid_consta
     const uint32_t qi = tile * 128 + qrow;
     float in[8];
     const uint32_t l0 = lgroup * 4;
-    if (qi < n) {
+    const bool used = qi < n && (live == nullptr || live[3 * (size_t)qi] != 0.f ||
+                                 live[3 * (size_t)qi + 1] != 0.f ||
+                                 live[3 * (size_t)qi + 2] != 0.f);
+    if (used) {
       nrc_encode_levels<4>(C, queries + (size_t)qi * 12, l0, in);
     } else {
       for (int k = 0; k < 8; ++k) {
@@ -282,7 +288,7 @@ __global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const __grid_consta
     }
     if (lgroup == 0) {
       for (uint32_t k = 0; k < 9; ++k) {
-        store_bf16(x0, qrow, 32 + k, kNrcIn, qi < n ? queries[(size_t)qi * 12 + 3 + k] : 0.f);
+        store_bf16(x0, qrow, 32 + k, kNrcIn, used ? queries[(size_t)qi * 12 + 3 + k] : 0.f);
       }
       for (uint32_t k = 41; k < kNrcIn; ++k) {
         store_bf16(x0, qrow, k, kNrcIn, 0.f);
@@ -591,15 +597,16 @@ size_t nrc_train_scratch_bytes(int grid) {
   return (size_t)grid * (kNrcIn + 5 * kNrcHid) * 128 * 2;
 }
 
-cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n, float *out,
-                             uint32_t *err, int grid, cudaStream_t s) {
+cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n,
+                             const float *live, float *out, uint32_t *err, int grid,
+                             cudaStream_t s) {
   const size_t smem = nrc_infer_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(dev::k_nrc_infer,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess || n == 0) {
     return e;
   }
-  dev::k_nrc_infer<<<grid, dev::kInferThreads, smem, s>>>(c, queries, n, out, err);
+  dev::k_nrc_infer<<<grid, dev::kInferThreads, smem, s>>>(c, queries, n, live, out, err);
   return cudaGetLastError();
 }
 

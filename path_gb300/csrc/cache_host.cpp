@@ -120,9 +120,11 @@ Status RadianceCache::check_err(const char *what) {
   return Status::ok();
 }
 
-Status RadianceCache::infer(const float *queries, uint32_t n, float *out, cudaStream_t s) {
+Status RadianceCache::infer(const float *queries, uint32_t n, float *out, cudaStream_t s,
+                            const float *live) {
   PG_TRY_CUDA(cudaMemsetAsync(err_.get(), 0, 4, s), "cache query");
-  PG_TRY_CUDA(launch_nrc_infer(params(), queries, n, out, err_.as<uint32_t>(), kInferGrid, s),
+  PG_TRY_CUDA(launch_nrc_infer(params(), queries, n, live, out, err_.as<uint32_t>(), kInferGrid,
+                               s),
               "cache query");
   return Status::ok();
 }

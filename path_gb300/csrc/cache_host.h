@@ -17,8 +17,10 @@ public:
   // scene box mapped to the unit cube of the hash grid
   void set_bounds(const float *lo, const float *hi);
   NrcParams params() const;
-  // out [n][3] = network(queries [n][12]) on stream s (device pointers)
-  Status infer(const float *queries, uint32_t n, float *out, cudaStream_t s);
+  // out [n][3] = network(queries [n][12]) on stream s (device pointers);
+  // with live ([n][3]), queries whose three live values are zero are skipped
+  Status infer(const float *queries, uint32_t n, float *out, cudaStream_t s,
+               const float *live = nullptr);
   // gradients of the mean relative L2 loss over records [n][16] (query,
   // target rgb, pad) into the gradient buffers, without an update
   Status gradients(const float *records, uint32_t n, float *loss);

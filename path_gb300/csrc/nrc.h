@@ -59,8 +59,10 @@ struct NrcParams {
   const unsigned char *w_bwd; // BF16 [in][out] K-major tiles
 };
 
-cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n, float *out,
-                             uint32_t *err, int grid, cudaStream_t s);
+// live: optional [n][3], a query whose three values are zero is skipped
+cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n,
+                             const float *live, float *out, uint32_t *err, int grid,
+                             cudaStream_t s);
 cudaError_t launch_nrc_train(const NrcParams &c, const float *records, uint32_t n,
                              float inv_batch, float *grad_w, float *d_feat,
                              unsigned char *scratch, float *loss, uint32_t *err, int grid,

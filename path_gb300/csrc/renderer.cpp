@@ -102,6 +102,11 @@ Renderer::~Renderer() {
       cudaEventDestroy(e);
     }
     cudaStreamDestroy(stream_);
+    if (side_stream_ != nullptr) {
+      cudaStreamSynchronize(side_stream_);
+      cudaEventDestroy(side_done_);
+      cudaStreamDestroy(side_stream_);
+    }
   }
 }
 
@@ -727,6 +732,22 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   auto t0 = std::chrono::steady_clock::now();
   uint32_t launches = 0;
   PG_TRY_CUDA(cudaEventRecord(ev_start_, stream_), "event");
+  if (cache_ != nullptr && cache_train_paths_ > 0) {
+    // the cache's training paths are independent of the frame: trace them on
+    // a side stream while the frame renders (the scene is uploaded already)
+    if (side_stream_ == nullptr) {
+      PG_TRY_CUDA(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
+      PG_TRY_CUDA(cudaEventCreateWithFlags(&side_done_, cudaEventDisableTiming), "event");
+    }
+    RenderParams tp = p;
+    tp.cache_depth = 0;
+    PG_TRY_CUDA(cache_records_.ensure((size_t)cache_train_paths_ * 64), "cache records");
+    PG_TRY_CUDA(launch_nrc_paths(tp, cache_train_paths_, frame_counter_++,
+                                 cache_records_.as<float>(), side_stream_),
+                "cache training paths");
+    PG_TRY_CUDA(cudaEventRecord(side_done_, side_stream_), "event");
+    ++launches;
+  }
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
     slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 24u;
     Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks,
@@ -963,7 +984,9 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   if (w.cache_q != nullptr) {
     // the radiance cache's prediction at every path's last vertex
     PG_TRY_CUDA(cache_pred_.ensure((size_t)total * 12), "cache predictions");
-    Status sc = cache_->infer(w.cache_q, (uint32_t)total, cache_pred_.as<float>(), stream_);
+    // paths that ended before the cache vertex (zero throughput) skip it
+    Status sc = cache_->infer(w.cache_q, (uint32_t)total, cache_pred_.as<float>(), stream_,
+                              w.cache_beta);
     if (!sc.good()) {
       return sc;
     }
@@ -1167,9 +1190,17 @@ Status Renderer::render_cached(const path_sample_spec &spec, const path_output &
   auto t0 = std::chrono::steady_clock::now();
   cache_ = &cache;
   cache_depth_ = cache_depth;
+  cache_train_paths_ = train_steps > 0 ? train_paths : 0u;
   Status sr = render(spec, output, scene, spp, st, nullptr);
+  const bool side = cache_train_paths_ > 0;
   cache_ = nullptr;
   cache_depth_ = 0;
+  cache_train_paths_ = 0;
+  if (side && side_done_ != nullptr) {
+    // the training paths' records (traced beside the frame)
+    PG_TRY_CUDA(cudaEventSynchronize(side_done_), "cache training paths");
+    PG_TRY_CUDA(cudaGetLastError(), "cache training paths");
+  }
   if (!sr.good()) {
     return sr;
   }
@@ -1177,13 +1208,6 @@ Status Renderer::render_cached(const path_sample_spec &spec, const path_output &
   // the cache covers the scene's box
   cache.set_bounds(prep_.lo, prep_.hi);
   if (train_paths > 0 && train_steps > 0) {
-    RenderParams p = last_params_;
-    p.cache_depth = 0;
-    PG_TRY_CUDA(cache_records_.ensure((size_t)train_paths * 64), "cache records");
-    PG_TRY_CUDA(launch_nrc_paths(p, train_paths, frame_counter_++, cache_records_.as<float>(),
-                                 stream_),
-                "cache training paths");
-    PG_TRY_CUDA(cudaStreamSynchronize(stream_), "cache training paths");
     const uint32_t per = std::max<uint32_t>(train_paths / train_steps, 1);
     for (uint32_t k = 0; k < train_steps; ++k) {
       const uint32_t first = k * per;

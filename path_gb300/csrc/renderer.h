@@ -189,6 +189,11 @@ private:
   class RadianceCache *cache_ = nullptr; // set during a cached render
   uint32_t cache_depth_ = 0;
   uint32_t frame_counter_ = 0;
+  // cached render: training paths traced on a side stream while the frame
+  // renders (cache_train_paths_ > 0 asks render() to launch them)
+  uint32_t cache_train_paths_ = 0;
+  cudaStream_t side_stream_ = nullptr;
+  cudaEvent_t side_done_ = nullptr;
   DeviceBuffer cache_q_, cache_beta_, cache_pred_, cache_records_;
   uint32_t last_blocks_ = 0;
   DeviceBuffer adj_image_, adj_dimage_, adj_params_, adj_pend_;
