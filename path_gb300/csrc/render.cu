@@ -50,10 +50,12 @@ __global__ void __launch_bounds__(256, 4) k_render(const RenderParams P) {
 // rays of a vertex are traced in turn: the pending light ray, then the
 // extension ray.  On the large-mesh room, 28 ready lanes measured best (8:
 // 101, 16: 121, 24: 135, 28: 140, 32: 134 Msamples/s; the per-thread
-// kernel 68).
+// kernel 68).  With kSteps (OutputPerStep, rendering_equation.h:61-124) the
+// radiance of path step k goes to the thread's step sum k and a path stops
+// after P.n_steps steps, as in k_render_steps.
 constexpr uint32_t kShadeLanes = 28;
 
-template <bool kCount, bool kUniform>
+template <bool kCount, bool kUniform, bool kSteps = false>
 __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
@@ -71,6 +73,13 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
   uint32_t st_base[kWideStack];
   uint32_t st_bits[kWideStack];
   Hit lh = no_hit(), nh = no_hit();
+  rgb steps[kSteps ? kMaxOutputSteps : 1];
+  uint32_t step = 0; // OutputPerStep: the current path's step
+  if constexpr (kSteps) {
+    for (uint32_t k = 0; k < P.n_steps; ++k) {
+      steps[k] = zero_rgb();
+    }
+  }
   // 0: start the next sample, 1: tracing the light ray, 2: tracing the
   // extension ray, 3: ready to shade, 4: all samples done
   uint32_t phase = 0;
@@ -145,7 +154,19 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
     const uint32_t ready = __ballot_sync(kFull, phase == 3);
     const uint32_t busy = __ballot_sync(kFull, phase == 1 || phase == 2);
     if (ready != 0 && (__popc(ready) >= kShadeLanes || busy == 0) && phase == 3) {
-      if (path_continues(P, s, path_step(P, L, s, lh, nh))) {
+      if constexpr (kSteps) {
+        const bool cont = path_step(P, L, s, lh, nh);
+        steps[step] = steps[step] + s.total;
+        s.total = zero_rgb();
+        ++step;
+        if (cont && step < P.n_steps) {
+          begin_rays();
+        } else {
+          step = 0;
+          ++smp;
+          phase = 0;
+        }
+      } else if (path_continues(P, s, path_step(P, L, s, lh, nh))) {
         begin_rays();
       } else {
         total = total + s.total;
@@ -155,6 +176,22 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
     }
   }
   const uint32_t sbs = P.wd.sample_block_size;
+  if constexpr (kSteps) {
+    // one sub-block reduction per step (mega_kernel/run_impl.h:160-185)
+    const uint32_t nsb = P.wd.num_sample_blocks;
+    const size_t idx = (block % nsb) + (size_t)nsb * (tw.x + (size_t)tw.y * P.x_dim);
+    for (uint32_t k = 0; k < P.n_steps; ++k) {
+      rgb sum = sub_block_reduce(steps[k], tid, sbs);
+      if (!tw.exit && tid % sbs == 0) {
+        if (nsb == 1) {
+          sum = sum / (float)P.spp;
+        }
+        write_pixel(P.out_rgb + k * P.step_stride, nullptr, false, idx, sum);
+      }
+      __syncthreads(); // the next step reuses the reduction's shared memory
+    }
+    return;
+  }
   total = sub_block_reduce(total, tid, sbs);
   if (!tw.exit && tid % sbs == 0) {
     const uint32_t nsb = P.wd.num_sample_blocks;
@@ -289,7 +326,13 @@ void render_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s
 
 template <uint32_t kTrav>
 void render_steps_variant(const RenderParams &p, dim3 grid, dim3 block, cudaStream_t s) {
-  if (p.rng_uniform) {
+  if constexpr (kTrav == kTravWide) {
+    if (p.rng_uniform) {
+      dev::k_render_coop<false, true, true><<<grid, block, 0, s>>>(p);
+    } else {
+      dev::k_render_coop<false, false, true><<<grid, block, 0, s>>>(p);
+    }
+  } else if (p.rng_uniform) {
     dev::k_render_steps<kTrav, true><<<grid, block, 0, s>>>(p);
   } else {
     dev::k_render_steps<kTrav, false><<<grid, block, 0, s>>>(p);
