@@ -404,7 +404,7 @@ def main():
                     help="image width = height (profiling cases; default: the workload's)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
     ap.add_argument("--slots-log2", type=int, default=0,
-                    help="streaming: paths in flight = 2^this (0 = default 24)")
+                    help="streaming: paths in flight = 2^this (0 = default 26)")
     ap.add_argument("--gpu-build", action="store_true",
                     help="build the 8-wide BVH on the GPU (linear BVH) instead of the SBVH")
     ap.add_argument("--trace-min-blocks", type=int, default=0,
@@ -523,7 +523,7 @@ def main():
         kern_ms = mean_ms
         kernel_name = "k_render"
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
-    shape = (f"slots_log2={args.slots_log2 or 24} trace_min_blocks={args.trace_min_blocks or 4} "
+    shape = (f"slots_log2={args.slots_log2 or 26} trace_min_blocks={args.trace_min_blocks or 4} "
              f"bvh={'gpu' if args.gpu_build else 'sbvh'}")
     traffic = _profiled_traffic(kernel_name, args, shape) if args.size is None and \
         args.spp is None else None
@@ -536,7 +536,7 @@ def main():
             "width": w, "height": h, "spp": spp,
             "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
             "trace_min_blocks": args.trace_min_blocks or 4,
-            "slots_log2": args.slots_log2 or 24,
+            "slots_log2": args.slots_log2 or 26,
             "bvh": "GPU linear BVH collapsed to 8-wide" if args.gpu_build else
                    "SBVH (host) collapsed to 8-wide",
             "l2": "flushed (512 MB write) before every timed step",

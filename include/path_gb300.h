@@ -140,7 +140,7 @@ typedef struct {
                                 over Morton codes, collapsed to 8-wide); the
                                 wide traversal only, no binary SBVH */
   uint32_t wavefront_slots_log2; /* streaming: paths in flight = 2^this
-                                    (10..24, 0 = default 24) */
+                                    (10..26, 0 = default 26) */
 } path_settings;
 
 typedef enum {
@@ -360,7 +360,7 @@ typedef struct {
  * (bit for bit); they only change speed.  Zero fields take the defaults in
  * brackets. */
 typedef struct {
-  uint32_t slots_log2;          /* paths in flight = 2^slots_log2 [23] */
+  uint32_t slots_log2;          /* paths in flight = 2^slots_log2, 10..26 [26] */
   uint32_t trace_min_blocks;    /* trace kernel variant, 3..6 [4] */
   uint32_t shade_ctas_per_sm;   /* shade grid = SMs x this [4] */
   uint32_t iterations_per_graph; /* trace/shade iterations per CUDA-graph

@@ -30,7 +30,7 @@ namespace pg {
 
 namespace {
 
-constexpr uint32_t kDefaultSlotsLog2 = 23;
+constexpr uint32_t kDefaultSlotsLog2 = 26;
 constexpr uint32_t kDefaultTraceMinBlocks = 4;
 constexpr uint32_t kDefaultShadeCtas = 4;
 constexpr uint32_t kDefaultItersPerGraph = 4;
@@ -338,7 +338,7 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
                 "sm count");
   }
   if (tu.trace_min_blocks < 3 || tu.trace_min_blocks > 6 || tu.slots_log2 < 10 ||
-      tu.slots_log2 > 24 || tu.shade_ctas_per_sm > 64 || tu.iterations_per_graph > 64) {
+      tu.slots_log2 > 26 || tu.shade_ctas_per_sm > 64 || tu.iterations_per_graph > 64) {
     return Status::err(PATH_ERR_ARGUMENT, "batch tuning out of range");
   }
   uint32_t max_spp = 0;
@@ -700,7 +700,7 @@ Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_
   path_settings quiet = st;
   quiet.count_work = 0;
   // candidates: paths in flight x trace occupancy x shade grid
-  const uint32_t slots[] = {21, 22, 23, 24};
+  const uint32_t slots[] = {23, 24, 25, 26};
   const uint32_t mins[] = {3, 4, 5};
   const uint32_t shades[] = {2, 4, 8};
   path_batch_tuning best = resolved(nullptr);

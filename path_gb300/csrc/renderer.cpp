@@ -508,8 +508,8 @@ Status check_settings(const path_settings &s) {
   if (s.target_objects == 0 || s.target_objects > 10) {
     return Status::err(PATH_ERR_ARGUMENT, "target_objects must be in [1, 10]");
   }
-  if (s.wavefront_slots_log2 != 0 && (s.wavefront_slots_log2 < 10 || s.wavefront_slots_log2 > 24)) {
-    return Status::err(PATH_ERR_ARGUMENT, "wavefront_slots_log2 must be 0 or in [10, 24]");
+  if (s.wavefront_slots_log2 != 0 && (s.wavefront_slots_log2 < 10 || s.wavefront_slots_log2 > 26)) {
+    return Status::err(PATH_ERR_ARGUMENT, "wavefront_slots_log2 must be 0 or in [10, 26]");
   }
   return Status::ok();
 }
@@ -749,7 +749,9 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     ++launches;
   }
   if (st.kernel_approach == PATH_KERNEL_STREAMING) {
-    slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 24u;
+    // paths in flight: up to 2^26 (144 bytes each, 9.7 GB at the most), so
+    // that a render of up to 67 M samples has all of them in flight at once
+    slots_log2_ = st.wavefront_slots_log2 ? st.wavefront_slots_log2 : 26u;
     Status sw = run_wavefront(p, n_blocks, st.count_work != 0, st.trace_min_blocks,
                               st.time_kernels != 0, &launches);
     if (!sw.good()) {

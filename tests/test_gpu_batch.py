@@ -106,7 +106,7 @@ def test_batch_autotune_returns_a_shape_that_renders_the_same(lib):
         batch.append((sc, api.SquareImage(w, h, f2w), out, spp))
     r = api.Renderer()
     t = r.autotune_batch(batch, s, sample_budget=1 << 16)
-    assert 21 <= t["slots_log2"] <= 24 and 3 <= t["trace_min_blocks"] <= 5
+    assert 23 <= t["slots_log2"] <= 26 and 3 <= t["trace_min_blocks"] <= 5
     r.render_batch(batch, s, t)
     for out, ref in zip(outs, refs):
         assert np.array_equal(bits(out), bits(ref))
