@@ -210,7 +210,7 @@ def run_batched(args, rank, world, local_rank):
     tris = sum(sc.sizes()["triangles"] for sc, _, _, _ in batch)
     r = api.Renderer()
     t0 = time.time()
-    tuning = r.autotune_batch(items, settings, sample_budget=1 << 24)
+    tuning = r.autotune_batch(items, settings)
     setup_s = time.time() - t0
     build_s = r.stats()["bvh_build_seconds"]
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

@@ -379,7 +379,8 @@ path_status path_render_batch(path_renderer *renderer, const path_batch_item *it
                               uint32_t n_items, const path_settings *settings,
                               const path_batch_tuning *tuning, double *seconds);
 /* Times candidate launch shapes on the batch's first samples (at most
- * sample_budget of them, no image output) and returns the fastest. */
+ * sample_budget of them, 0 = 2^27; no image output) and returns the
+ * fastest. */
 path_status path_batch_autotune(path_renderer *renderer, const path_batch_item *items,
                                 uint32_t n_items, const path_settings *settings,
                                 uint64_t sample_budget, path_batch_tuning *out);

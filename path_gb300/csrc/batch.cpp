@@ -695,14 +695,18 @@ Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_
   stats_ = path_render_stats{};
   stats_.bvh_build_seconds = batch_.build_seconds;
   if (sample_budget == 0) {
-    sample_budget = 1ull << 24;
+    // twice the largest candidate's paths in flight, so that every
+    // candidate refills its slots
+    sample_budget = 1ull << 27;
   }
   path_settings quiet = st;
   quiet.count_work = 0;
-  // candidates: paths in flight x trace occupancy x shade grid
+  // candidates: paths in flight x trace occupancy x shade grid (trace CTAs
+  // per SM other than 4 and shade grids below 4 CTAs per SM never won on
+  // the batched workload)
   const uint32_t slots[] = {23, 24, 25, 26};
-  const uint32_t mins[] = {3, 4, 5};
-  const uint32_t shades[] = {2, 4, 8};
+  const uint32_t mins[] = {4};
+  const uint32_t shades[] = {4, 8};
   path_batch_tuning best = resolved(nullptr);
   float best_ms = -1.f;
   for (uint32_t sl : slots) {
