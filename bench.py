@@ -14,18 +14,27 @@ step is one full render.
   host buffers: every step re-copies the scene's device arrays from pinned
   host memory and copies the image back to the host, all inside the timed
   wall-clock region.
-* roofline: algorithmic bytes of the render kernel (wide nodes x 80 B +
-  triangles tested x 48 B + rays x 96 B of shading data, counted by a
-  counting run of the same render) over the kernel's event time, against the
-  measured HBM copy bandwidth.
-* cpu_baseline: the CPU oracle (a restatement of the reference's CPU path:
-  OpenMP over WorkDivision blocks) on a band of image rows of the same
-  workload, all host threads.
+* roofline: the dominant kernel (the persistent trace) against both sides of
+  the path's roofline -- algorithmic bytes (wide nodes x 80 B + triangles
+  tested x 48 B + rays x 40 B, counted by a counting run of the same render)
+  against the measured HBM copy bandwidth, and the instructions it issues
+  (per node visit, from the committed ncu summary) against the SMs' issue
+  rate -- with `bound` the side that is nearer its peak.
+* parity_vs_oracle: the timed image against the CPU oracle (a restatement
+  of the reference's CPU path) on spread rows of the same render.
+* error_vs_4096spp_fp64: the timed image against 4096 samples per pixel
+  summed in FP64, by the GPU (whole image) and by the oracle (spread rows).
+* time_to_0.02_rmse, adjoint_forward_ratio: the other two parts of the
+  metric (the radiance-cache and adjoint workloads, smaller runs than
+  --workload cache / the adjoint tests).
+* cpu_baseline: the CPU oracle on the spread rows, all host threads.
 
-``--impl reference`` times that CPU restatement alone (the reference itself
-cannot be built here: it needs clang as its CUDA compiler and libraries that
-are not installed).  N > 1 runs independent
-replicas, one per GPU (the render has no data-path exchange).
+``--impl reference`` times that CPU restatement alone, on the same spread
+rows, with the scene built in NumPy (scenes.ArrayScene) so that the
+library is not loaded (the reference itself cannot be built here: it needs
+clang as its CUDA compiler and libraries that are not installed).  N > 1
+runs independent replicas, one per GPU (the render has no data-path
+exchange).
 """
 
 import argparse
@@ -131,59 +140,98 @@ def _profiled_traffic(kernel, args, shape):
     return traffic if profiled_shape == shape else None
 
 
-def make_workload(name, size=None, spp_override=None):
+def _profiled_issue(kernel, args, shape):
+    """Instructions the dominant kernel issues per wide-node visit (warp and
+    thread level) from the committed ncu summary of this workload's kernel
+    (lines 'warp_inst_per_node_visit: N', 'thread_inst_per_node_visit: N'
+    and 'launch_shape:' in profiles/<kernel>_issue_<workload>.txt), or None
+    when it is missing or was taken at another launch shape."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_issue_{args.workload}.txt")
+    vals, profiled_shape = {}, None
+    try:
+        with open(path) as f:
+            for ln in f:
+                key, _, val = ln.partition(":")
+                if key in ("warp_inst_per_node_visit", "thread_inst_per_node_visit"):
+                    vals[key] = float(val)
+                elif key == "launch_shape":
+                    profiled_shape = val.strip()
+    except (OSError, ValueError):
+        return None
+    return vals if profiled_shape == shape and len(vals) == 2 else None
+
+
+def make_workload(name, size=None, spp_override=None, scene_cls=None):
     from path_gb300 import scenes
     if name == "large_mesh":
-        scene = scenes.large_mesh_room(subdivisions=8)
+        scene = scenes.large_mesh_room(subdivisions=8, scene_cls=scene_cls)
         w = h = size or 1024
         spp, depth = spp_override or 64, 8
         desc = ("large-mesh room: 1,310,720-tri displaced icosphere (GGX a=0.2 F0=0.04) + "
                 f"19,800-tri glass sphere (IOR 1.5), {w}x{h}, {spp} spp, depth 8")
     else:
-        scene = scenes.cornell_box()
+        scene = scenes.cornell_box(scene_cls=scene_cls)
         w = h = size or 256
         spp, depth = spp_override or 16, 5
         desc = f"Cornell box: 36 triangles, {w}x{h}, {spp} spp, depth 5"
     return scene, w, h, spp, depth, desc
 
 
-def cpu_sample(scene, settings, spp, w, h, f2w, rows, threads):
-    """The oracle on a band of rows; returns (samples, seconds)."""
+def spread_rows(h, rows):
+    """`rows` rows spread over the image: every (h // rows)-th row, starting
+    half a stride in."""
+    stride = max(1, h // max(1, rows))
+    start = stride // 2
+    return start, stride, np.arange(start, h, stride)
+
+
+def oracle_prepare(scene_arrays, settings, reduce_order, threads):
     from oracle import oracle_lib as ol
-    arr = ol.SceneArrays(scene.export())
-    s = ol.settings_from(settings, reduce_order=0, n_threads=threads)
-    r0 = h // 2 - rows // 2
-    _, secs = ol.render(arr, s, spp, w, h, f2w, rows=(r0, r0 + rows))
-    return rows * w * spp, secs
+    s = ol.settings_from(settings, reduce_order=reduce_order, n_threads=threads)
+    return ol.Prepared(scene_arrays, s), s
+
+
+def cpu_sample(prep, s, spp, w, h, f2w, rows):
+    """The oracle on spread rows; returns (image with those rows, row
+    indices, samples, seconds)."""
+    start, stride, sel = spread_rows(h, rows)
+    img, secs = prep.render(s, spp, w, h, f2w, rows=(start, h), stride=stride)
+    return img, sel, len(sel) * w * spp, secs
 
 
 def run_reference(args, rank):
     if rank != 0:
         return
     from path_gb300 import scenes
-    scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
-    settings = scenes.path_settings(depth, "binary")
-    f2w = scenes.cornell_camera(w, h)
+    from oracle import oracle_lib as ol
+    scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp,
+                                                  scene_cls=scenes.ArrayScene)
+    f2w = scenes.cornell_camera(w, h, ol.camera_transform)
     threads = os.cpu_count() or 1
+    # the reference's CPU execution model: lane-order reduction
+    s = ol.workload_settings(depth, reduce_order=0, n_threads=threads)
+    prep = ol.Prepared(ol.SceneArrays(scene.export()), s)
     rows = args.cpu_rows
     for _ in range(args.warmup):
-        cpu_sample(scene, settings, spp, w, h, f2w, rows, threads)
+        cpu_sample(prep, s, spp, w, h, f2w, rows)
     total_s, total_samples = 0.0, 0
     for _ in range(args.steps):
-        n, secs = cpu_sample(scene, settings, spp, w, h, f2w, rows, threads)
+        _, sel, n, secs = cpu_sample(prep, s, spp, w, h, f2w, rows)
         total_s += secs
         total_samples += n
     value = total_samples / total_s / 1e6
+    sample = (f"{len(sel)} rows spread over the image (1 in {h // rows}) x {w} px x {spp} "
+              "spp per step")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": desc, "sample": f"{rows} rows x {w} px x {spp} spp per step"},
+        "config": {"workload": desc, "sample": sample},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows of {w} px at {spp} spp per step (oracle: CPU "
-                                   "restatement of the reference CPU path)"},
+                         "sample": sample + " (oracle: CPU restatement of the reference CPU "
+                                            "path; scene built in NumPy, library not loaded)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -259,20 +307,156 @@ def run_batched(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def time_to_rmse(r, scene, w, h, f2w, settings, ref, cfg, max_frames, base, target=0.02):
+    """Frames of 4 new samples each (from Sobol sample `base` on),
+    accumulated in FP64 until the relative RMSE against `ref` is <= target:
+    plain renders (cfg None) or radiance-cache frames (cfg: the vertex where
+    paths end into the cache, training records and Adam steps per frame,
+    training-only frames first).  Wall time of the render + training calls."""
+    import torch
+    from path_gb300 import api
+    ref_norm = float(torch.linalg.norm(ref))
+    out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    cache = api.RadianceCache(seed=1) if cfg is not None else None
+    acc = torch.zeros_like(ref)
+    wall, frames, err, curve = 0.0, 0, None, []
+
+    def frame(offset):
+        spec = api.SquareImage(w, h, f2w, sample_offset=offset)
+        if cache is None:
+            r.render(api.ExecutionModel.GPU, spec, out, scene, 4, settings)
+        else:
+            r.render_cached(cache, spec, out, scene, 4, settings,
+                            cache_depth=cfg["cache_depth"], train_paths=cfg["train_paths"],
+                            train_steps=cfg["train_steps"])
+
+    if cfg is not None and cfg["pretrain_frames"] > 0:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for f in range(cfg["pretrain_frames"]):
+            frame(base + 4 * (max_frames + f))
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t
+    while frames < max_frames:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        frame(base + 4 * frames)
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t
+        frames += 1
+        acc += out.double()
+        err = float(torch.linalg.norm(acc / frames - ref)) / ref_norm
+        if frames in (1, 2, 4, 8, 16, 32, 64, 128, 256) or err <= target:
+            curve.append((frames, round(wall, 4), round(err, 5)))
+        if err <= target:
+            break
+    res = {"frames": frames, "seconds": wall, "rel_rmse": err,
+           "reached": err is not None and err <= target, "curve": curve}
+    if cfg is not None:
+        res["cache"] = (
+            "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
+            f"paths end into the cache at vertex {cfg['cache_depth']}, "
+            f"{cfg['train_paths']} records x {cfg['train_steps']} steps per frame, "
+            f"{cfg['pretrain_frames']} training-only frames first")
+    return res
+
+
+def gpu_reference(r, scene, w, h, f2w, settings, first_sample, n_samples=4096, per_render=64):
+    """n_samples samples per pixel from Sobol sample first_sample on, each
+    render of per_render samples summed into an FP64 image (mean)."""
+    import torch
+    from path_gb300 import api
+    out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    n = max(1, n_samples // per_render)
+    for f in range(n):
+        r.render(api.ExecutionModel.GPU,
+                 api.SquareImage(w, h, f2w, sample_offset=first_sample + per_render * f), out,
+                 scene, per_render, settings)
+        ref += out.double()
+    return ref / n
+
+
+def cache_study(r, scene, w, h, f2w, settings, ref, args, ref_note):
+    """Time to 0.02 relative RMSE of the plain tracer and of the radiance
+    cache (the configuration on the command line -- by default the
+    specified one: paths end at vertex 2, 2^16 records x 4 Adam steps per
+    frame -- and a tuned one with its untrained control), frames starting
+    after the reference's samples."""
+    base = 64 + 4096 + 64
+    plain = time_to_rmse(r, scene, w, h, f2w, settings, ref, None, args.max_frames, base)
+    spec_cfg = {"cache_depth": args.cache_depth, "train_paths": args.train_paths,
+                "train_steps": args.train_steps, "pretrain_frames": args.pretrain_frames}
+    runs = {"cached": time_to_rmse(r, scene, w, h, f2w, settings, ref, spec_cfg,
+                                   args.max_frames, base)}
+    controls = {}
+    if not args.no_tuned_cache:
+        tuned = {"cache_depth": 3, "train_paths": 1 << 14, "train_steps": 2,
+                 "pretrain_frames": 0}
+        runs["cached_tuned"] = time_to_rmse(r, scene, w, h, f2w, settings, ref, tuned,
+                                            args.max_frames, base)
+        controls["cached_tuned_untrained"] = time_to_rmse(
+            r, scene, w, h, f2w, settings, ref, dict(tuned, train_steps=0), args.max_frames,
+            base)
+    reached = [k for k in runs if runs[k]["reached"]]
+    best = min(reached, key=lambda k: runs[k]["seconds"]) if reached else None
+    return {
+        "value": runs[best]["seconds"] if best else None, "unit": "s", "value_from": best,
+        "ratio_cached_over_plain": (runs[best]["seconds"] / plain["seconds"]
+                                    if plain["reached"] and best else None),
+        "target_ratio": 0.25, "reference": ref_note,
+        "plain": plain, **runs, **controls,
+    }
+
+
+def adjoint_study(steps=5):
+    """Adjoint / forward cost on the 16-material Cornell patches (128 x 128,
+    64 spp, depth 4, L2 loss to a target from parameters perturbed by up to
+    10%, seed 2), kernel time of each, plus the adjoint's agreement with
+    central differences (step 1e-3, common random numbers) on four
+    reflectance / emission parameters."""
+    from path_gb300 import api, diff, scenes
+    w = h = 128
+    sc, mats = scenes.patch_cornell(seed=1)
+    s = scenes.path_settings(4, "wide")
+    s.kernel_approach = 1
+    rend = diff.Renderable(sc, mats, api.SquareImage(w, h, scenes.cornell_camera(w, h)), 64, s)
+    p0 = diff.params_of(mats)
+    target = rend.render(scenes.perturbed_params(p0, mats, seed=2)).astype(np.float64)
+    img = rend.render(p0)
+    d_img = (2.0 * (img.astype(np.float64) - target)).astype(np.float32)
+    r = rend.renderer
+    fwd, adj = [], []
+    for _ in range(steps):
+        rend.render(p0)
+        fwd.append(r.stats()["kernel_ms"])
+        g = rend.adjoint(p0, d_img)
+        adj.append(r.stats()["kernel_ms"])
+
+    def loss(p):
+        d = rend.render(p).astype(np.float64) - target
+        return float((d * d).sum())
+
+    pairs = [(0, 0), (3, 1), (15, 4), (8, 2)]
+    fd, ad = [], []
+    for i, j in pairs:
+        hi, lo = p0.copy(), p0.copy()
+        hi[i, j] += 1e-3
+        lo[i, j] -= 1e-3
+        fd.append((loss(hi) - loss(lo)) / 2e-3)
+        ad.append(g[i, j])
+    fd, ad = np.array(fd), np.array(ad)
+    return {"value": float(np.median(adj) / np.median(fwd)), "unit": "x", "target": 3.0,
+            "forward_ms": float(np.median(fwd)), "adjoint_ms": float(np.median(adj)),
+            "fd_rel_err": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
+            "workload": "16-material Cornell patches, 128x128, 64 spp, depth 4, L2 loss; "
+                        "adjoint = forward render + path replay"}
+
+
 def run_cache(args, rank, world, local_rank):
     """Time to 0.02 relative RMSE, plain tracer against the radiance cache,
-    on the large-mesh room at 1024 x 1024 in frames of 4 spp (depth 8).
-    Reference: 4096 spp of the plain tracer accumulated in FP64 (64 frames
-    of 64 spp).  Plain: frames of 4 new samples each, accumulated in FP64
-    until the error is <= 0.02.  Cache: frames whose paths end into the
-    cache after 2 bounces, each followed by 4 Adam steps on 2^16 records
-    from fresh full-length paths, accumulated the same way (the first
-    frames, with an untrained cache, included).  Then a tuned cache (paths
-    end at vertex 3, 2^14 records x 2 steps per frame) and, as its control,
-    the same truncation with the cache left untrained (what ending the paths
-    early does without the network).  Wall time of render +
-    training calls."""
-    import torch
+    on the large-mesh room at 1024 x 1024 in frames of 4 spp (depth 8)
+    against 4096 spp of the plain tracer accumulated in FP64."""
     from path_gb300 import api, scenes
     size = args.size or 1024
     scene, w, h, _, depth, desc = make_workload("large_mesh", size, 4)
@@ -280,90 +464,18 @@ def run_cache(args, rank, world, local_rank):
     settings.kernel_approach = 1
     f2w = scenes.cornell_camera(w, h)
     r = api.Renderer()
-    out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
     t0 = time.time()
-    ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
-    ref_frames = 64
-    for f in range(ref_frames):
-        r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w, sample_offset=64 * f), out,
-                 scene, 64, settings)
-        ref += out.double()
-    ref /= ref_frames
+    ref = gpu_reference(r, scene, w, h, f2w, settings, 64)
     ref_s = time.time() - t0
-    ref_norm = float(torch.linalg.norm(ref))
-
-    def run(cached, cfg=None, target=0.02):
-        cache = api.RadianceCache(seed=1) if cached else None
-        acc = torch.zeros_like(ref)
-        wall, frames, err = 0.0, 0, None
-        curve = []
-        base = 64 * ref_frames  # samples the reference did not use
-        if cached and cfg["pretrain_frames"] > 0:
-            # training-only frames (their images are not kept; time counted)
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            for f in range(cfg["pretrain_frames"]):
-                spec = api.SquareImage(w, h, f2w, sample_offset=base + 4 * (args.max_frames + f))
-                r.render_cached(cache, spec, out, scene, 4, settings,
-                                cache_depth=cfg["cache_depth"], train_paths=cfg["train_paths"],
-                                train_steps=cfg["train_steps"])
-            torch.cuda.synchronize()
-            wall += time.perf_counter() - t
-        while frames < args.max_frames:
-            spec = api.SquareImage(w, h, f2w, sample_offset=base + 4 * frames)
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            if cached:
-                r.render_cached(cache, spec, out, scene, 4, settings,
-                                cache_depth=cfg["cache_depth"], train_paths=cfg["train_paths"],
-                                train_steps=cfg["train_steps"])
-            else:
-                r.render(api.ExecutionModel.GPU, spec, out, scene, 4, settings)
-            torch.cuda.synchronize()
-            wall += time.perf_counter() - t
-            frames += 1
-            acc += out.double()
-            err = float(torch.linalg.norm(acc / frames - ref)) / ref_norm
-            if frames in (1, 2, 4, 8, 16, 32, 64, 128, 256) or err <= target:
-                curve.append((frames, round(wall, 4), round(err, 5)))
-            if err <= target:
-                break
-        out_d = {"frames": frames, "seconds": wall, "rel_rmse": err,
-                 "reached": err is not None and err <= target, "curve": curve}
-        if cfg is not None:
-            out_d["cache"] = (
-                "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
-                f"paths end into the cache at vertex {cfg['cache_depth']}, "
-                f"{cfg['train_paths']} records x {cfg['train_steps']} steps per frame, "
-                f"{cfg['pretrain_frames']} training-only frames first")
-        return out_d
-
-    plain = run(False)
-    # the configuration on the command line (defaults: the specified one),
-    # then a tuned one (picked by a search on this scene over the depth, the
-    # records and the steps per frame) and its untrained control
-    spec_cfg = {"cache_depth": args.cache_depth, "train_paths": args.train_paths,
-                "train_steps": args.train_steps, "pretrain_frames": args.pretrain_frames}
-    runs = {"cached": run(True, spec_cfg)}
-    controls = {}
-    if not args.no_tuned_cache:
-        tuned = {"cache_depth": 3, "train_paths": 1 << 14, "train_steps": 2,
-                 "pretrain_frames": 0}
-        runs["cached_tuned"] = run(True, tuned)
-        controls["cached_tuned_untrained"] = run(True, dict(tuned, train_steps=0))
-    reached = [k for k in runs if runs[k]["reached"]]
-    best = min(reached, key=lambda k: runs[k]["seconds"]) if reached else None
+    study = cache_study(r, scene, w, h, f2w, settings, ref, args,
+                        "4096 spp (samples 64..4159), FP64 sum")
     line = {
         "metric": "seconds to 0.02 relative RMSE", "unit": "s", "higher_is_better": False,
-        "value": runs[best]["seconds"] if best else None,
-        "n_gpus": 1, "dtype": "f32 render, bf16 cache MLP", "data": "synthetic",
+        "value": study.pop("value"), "n_gpus": 1, "dtype": "f32 render, bf16 cache MLP",
+        "data": "synthetic",
         "config": {"workload": f"{desc} in 4-spp frames; reference 4096 spp FP64",
-                   "value_from": best,
-                   "cache": runs[best]["cache"] if best else runs["cached"]["cache"]},
-        "plain": plain, **runs, **controls,
-        "ratio_cached_over_plain": (runs[best]["seconds"] / plain["seconds"]
-                                    if plain["reached"] and best else None),
-        "reference_seconds": ref_s,
+                   "value_from": study["value_from"]},
+        **study, "reference_seconds": ref_s,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -394,7 +506,13 @@ def main():
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
                     help="wavefront (streaming) or megakernel integration")
     ap.add_argument("--cpu-rows", type=int, default=128,
-                    help="image rows (centred) in the CPU baseline sample: about 7 s on 16 cores")
+                    help="image rows (spread over the image) in the CPU baseline sample: "
+                         "about 7 s on 16 cores")
+    ap.add_argument("--fp64-oracle-rows", type=int, default=8,
+                    help="rows (spread) of the oracle's 4096-spp FP64 reference: about 25 s "
+                         "on 16 cores")
+    ap.add_argument("--no-extra-metrics", action="store_true",
+                    help="skip the time-to-0.02-RMSE and adjoint/forward legs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-megakernel", action="store_true",
                     help="skip the megakernel comparison render")
@@ -505,6 +623,7 @@ def main():
 
     peak, peak_kind = _peaks()
     mean_ms = total_ms / args.steps
+    timed_img = dev_out.cpu().numpy()
     if streaming:
         # dominant kernel: the persistent trace.  Per ray it reads its origin
         # and direction (32 B) and writes its hit (8 B); per visit 80 B of
@@ -522,11 +641,47 @@ def main():
         launches_per_render = 1
         kern_ms = mean_ms
         kernel_name = "k_render"
+    clock_summary = clocks.summary()
+    launch_s = kern_ms / launches_per_render / 1e3
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     shape = (f"slots_log2={args.slots_log2 or 26} trace_min_blocks={args.trace_min_blocks or 4} "
              f"bvh={'gpu' if args.gpu_build else 'sbvh'}")
-    traffic = _profiled_traffic(kernel_name, args, shape) if args.size is None and \
-        args.spp is None else None
+    full_size = args.size is None and args.spp is None
+    traffic = _profiled_traffic(kernel_name, args, shape) if full_size else None
+    issue = _profiled_issue(kernel_name, args, shape) if full_size and streaming else None
+    # the other side of the roofline: FP32 work (22 operations per box test,
+    # 8 box tests per wide node, 45 per Moller-Trumbore test) against the
+    # FP32 lanes' issue rate, and -- from the ncu summary -- the warp
+    # instructions the kernel actually issues against the schedulers' rate
+    n_sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+    clk_hz = (clock_summary.get("sm_mhz") or 2070.0) * 1e6
+    nodes_per_launch = counts["nodes_visited"] / launches_per_render
+    fp32_ops = (22 * 8 * counts["nodes_visited"] + 45 * counts["triangles_tested"]) / \
+        launches_per_render
+    fp32_peak = n_sms * 128 * clk_hz / 1e12
+    sides = {
+        "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": peak_kind, "bytes": "algorithmic (node, triangle and ray bytes "
+                                                 "the traversal reads and writes)",
+                "dram_frac": (traffic / launch_s / 1e9 / peak) if traffic else None},
+        "fp32": {"achieved": fp32_ops / launch_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                 "frac": fp32_ops / launch_s / 1e12 / fp32_peak,
+                 "peak_kind": f"{n_sms} SMs x 128 FP32 lanes x sampled SM clock",
+                 "ops_per_launch": fp32_ops},
+    }
+    if issue is not None:
+        winst = issue["warp_inst_per_node_visit"] * nodes_per_launch
+        issue_peak = n_sms * 4 * clk_hz / 1e9
+        sides["issue"] = {
+            "achieved": winst / launch_s / 1e9, "peak": issue_peak, "unit": "Ginst/s",
+            "frac": winst / launch_s / 1e9 / issue_peak,
+            "peak_kind": f"{n_sms} SMs x 4 schedulers x 1 warp instruction per clock",
+            "warp_inst_per_node_visit": issue["warp_inst_per_node_visit"],
+            "thread_inst_per_node_visit": issue["thread_inst_per_node_visit"],
+            "lanes_active": issue["thread_inst_per_node_visit"] /
+            issue["warp_inst_per_node_visit"]}
+    bound = max(("hbm", "issue"), key=lambda k: sides[k]["frac"] if k in sides else -1)
+    b = sides[bound]
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms,
@@ -544,37 +699,32 @@ def main():
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "peak_kind": peak_kind, "kernel": kernel_name,
+        "roofline": {"bound": bound, "achieved": b["achieved"], "peak": b["peak"],
+                     "unit": b["unit"], "frac": b["frac"], "traffic": traffic,
+                     "peak_kind": b["peak_kind"], "kernel": kernel_name,
                      "launches_per_step": launches_per_render,
                      "kernel_ms_per_step": kern_ms,
-                     "algorithmic_bytes_per_launch": alg_bytes / launches_per_render},
+                     "algorithmic_bytes_per_launch": alg_bytes / launches_per_render,
+                     "sides": sides},
         "mrays_per_s": counts["rays_traced"] / (mean_ms / 1e3) / 1e6,
         "work_counts": {"rays": counts["rays_traced"], "wide_nodes": counts["nodes_visited"],
                         "triangles": counts["triangles_tested"]},
         "setup_s": setup_s, "bvh_build_s": st0["bvh_build_seconds"],
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
     }
+    rs = settings.copy()
+    rs.time_kernels = 0
+    ref = None
     if not args.no_reference_error and rank == 0:
-        # the timed image's error against a 4096-spp render of the same
-        # scene accumulated in FP64 (64 renders of 64 new samples each)
-        ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
-        rs = settings.copy()
-        rs.time_kernels = 0
-        n_ref = max(1, 4096 // 64)
-        for f in range(n_ref):
-            r.render(api.ExecutionModel.GPU,
-                     api.SquareImage(w, h, f2w, sample_offset=spp + 64 * f), dev_out, scene,
-                     64, rs)
-            ref += dev_out.double()
-        ref /= n_ref
-        r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, rs)
-        err = float(torch.linalg.norm(dev_out.double() - ref) / torch.linalg.norm(ref))
+        # the timed image's error against 4096 samples per pixel (samples
+        # spp .. spp + 4095) accumulated in FP64 by the GPU
+        ref = gpu_reference(r, scene, w, h, f2w, rs, spp)
+        err = float(np.linalg.norm(timed_img - ref.cpu().numpy()) /
+                    float(torch.linalg.norm(ref)))
         line["error_vs_4096spp_fp64"] = {
-            "rel_rmse": err, "reference": "4096 spp (samples spp..spp+4095), FP64 sum",
+            "rel_rmse": err, "reference": "4096 spp (samples spp..spp+4095), FP64 sum, GPU",
             "image": f"the timed {spp}-spp render"}
-    if streaming and args.size is None and args.spp is None and not args.no_megakernel:
+    if streaming and full_size and not args.no_megakernel:
         # the same render through the megakernel (identical image), for the
         # wavefront-versus-megakernel comparison of this workload
         ms = settings.copy()
@@ -586,14 +736,55 @@ def main():
         r.render(api.ExecutionModel.GPU, spec, dev_out, scene, spp, ms)
         mk = r.stats()["kernel_ms"]
         line["megakernel"] = {"value": samples / (mk / 1e3) / 1e6, "unit": METRIC,
-                              "ms_per_step": mk, "steps": 1}
+                              "ms_per_step": mk, "steps": 1,
+                              "same_image": bool(np.array_equal(dev_out.cpu().numpy(),
+                                                                timed_img))}
+    if rank == 0 and world == 1 and ref is not None and full_size and \
+            args.workload == "large_mesh" and not args.no_extra_metrics:
+        # the other two parts of the metric
+        cs = scenes.path_settings(8, "wide")
+        cs.kernel_approach = 1
+        line["time_to_0.02_rmse"] = cache_study(
+            r, scene, w, h, f2w, cs, ref, args,
+            "4096 spp (samples 64..4159), FP64 sum, GPU; frames from sample 4224")
+        line["adjoint_forward_ratio"] = adjoint_study()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle_lib as ol
         threads = os.cpu_count() or 1
-        n, secs = cpu_sample(scene, settings, spp, w, h, f2w, args.cpu_rows, threads)
+        t0 = time.time()
+        # summed in the GPU path's shuffle-tree order, so that the band is
+        # comparable with the timed image bit for bit
+        prep, os_ = oracle_prepare(ol.SceneArrays(scene.export()), settings, 1, threads)
+        prep_s = time.time() - t0
+        band, sel, n, secs = cpu_sample(prep, os_, spp, w, h, f2w, args.cpu_rows)
         line["cpu_baseline"] = {
             "value": n / secs / 1e6, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{args.cpu_rows} rows of {w} px at {spp} spp (oracle: CPU restatement "
-                      f"of the reference CPU path, {threads} threads)"}
+            "sample": f"{len(sel)} rows spread over the image (1 in {h // len(sel)}) x {w} px "
+                      f"x {spp} spp (oracle: CPU restatement of the reference CPU path, "
+                      f"{threads} threads; SBVH build {prep_s:.1f} s not timed)"}
+        a, o = timed_img[sel].astype(np.float64), band[sel].astype(np.float64)
+        line["parity_vs_oracle"] = {
+            "rel_rmse": float(np.linalg.norm(a - o) / np.linalg.norm(o)),
+            "bit_exact_pixels": float(np.mean(np.all(timed_img[sel] == band[sel], axis=-1))),
+            "rows": f"{len(sel)} rows (1 in {h // len(sel)} from row {sel[0]}) of the timed image",
+            "tolerance": 1e-4,
+            "oracle": "CPU restatement of the reference CPU path, binary SBVH traversal with "
+                      "the reference's tie rule"}
+        if ref is not None and args.fp64_oracle_rows > 0:
+            # 4096 samples per pixel summed in FP64 by the oracle, on spread rows
+            start, stride, fsel = spread_rows(h, args.fp64_oracle_rows)
+            f64, fsecs = prep.render_f64(os_, 4096, w, h, f2w, rows=(start, h), stride=stride,
+                                         sample_offset=spp)
+            g = ref.cpu().numpy()
+            o64 = f64[fsel]
+            line["error_vs_4096spp_fp64"]["oracle"] = {
+                "rel_rmse": float(np.linalg.norm(timed_img[fsel] - o64) / np.linalg.norm(o64)),
+                "gpu_reference_vs_oracle_reference": float(np.linalg.norm(g[fsel] - o64) /
+                                                           np.linalg.norm(o64)),
+                "rows": f"{len(fsel)} rows (1 in {stride} from row {start})",
+                "reference": "4096 spp (samples spp..spp+4095), every sample summed in FP64 "
+                             "by the CPU oracle",
+                "oracle_seconds": fsecs}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -429,6 +429,16 @@ path_status path_sobol_table_curand(uint32_t dimension_bound, uint32_t count,
  * fn 0 sin, 1 cos, 2 asin, 3 acos, 4 pow(x, y); host arrays of n */
 path_status path_debug_pmath(uint32_t fn, const float *x, const float *y,
                              float *out, uint32_t n);
+/* evaluates the kernels' BSDF code on the GPU for one material (GB300
+ * addition, for tests): n records of 9 floats in `in` (host arrays);
+ *   op 0: continuous_eval (bsdf::BSDF::continuous_eval, include/bsdf/bsdf.h
+ *         :10-46), record = (incoming dir, outgoing dir, normal), out [n][3];
+ *   op 1: continuous_sample (bsdf.h) drawing u0, u1, u2 in turn, record =
+ *         (incoming dir, normal, u0, u1, u2), out [n][6] = (dir, multiplier);
+ *   op 2: the GGX normal distribution D, record = (n.h, alpha, unused),
+ *         out [n]. */
+path_status path_debug_bsdf(const path_material *material, uint32_t op, const float *in,
+                            uint32_t n, float *out);
 /* kernel::WorkDivision (src/kernel/work_division.cpp:12-69): out receives
  * [block_size, base_samples_per_thread, n_threads_per_unit_extra,
  *  sample_block_size, x_block_size, y_block_size, num_sample_blocks,

@@ -25,6 +25,31 @@
 
 namespace {
 
+// Transcendental functions of the integrator.  The default build shares
+// path_gb300/csrc/pmath.h with the kernels, so that CPU and GPU round every
+// bounce direction identically.  Built with -DORACLE_LIBM (liboracle_libm.so)
+// the oracle calls the C library's sinf / cosf / asinf / acosf / powf where
+// the reference calls std::sin, std::cos, std::asin, std::acos and std::pow
+// (include/bsdf/diffuse.h:30-45, glossy.h:26-49, lib/projection.h:9-32,
+// dielectric_refractive.h:24-33, multiplier_func.h:19-30): the two builds
+// measure how far the shared polynomials move an image from the C library's
+// arithmetic.
+namespace om {
+#ifdef ORACLE_LIBM
+inline float sin(float x) { return ::sinf(x); }
+inline float cos(float x) { return ::cosf(x); }
+inline float asin(float x) { return ::asinf(x); }
+inline float acos(float x) { return ::acosf(x); }
+inline float pow(float x, float y) { return ::powf(x, y); }
+#else
+inline float sin(float x) { return pm::sin(x); }
+inline float cos(float x) { return pm::cos(x); }
+inline float asin(float x) { return pm::asin(x); }
+inline float acos(float x) { return pm::acos(x); }
+inline float pow(float x, float y) { return pm::pow(x, y); }
+#endif
+} // namespace om
+
 constexpr float kFloatMax = std::numeric_limits<float>::max();
 constexpr float kFloatLowest = std::numeric_limits<float>::lowest();
 
@@ -810,8 +835,8 @@ float sah_cost_impl(const BVH &bvh, float trav, unsigned idx) {
 // include/lib/projection.h:9-32: rotation by an angle about an axis
 // (Rodrigues' formula v c + (a x v) s + a (a.v)(1 - c))
 V3 rotate_axis_angle(V3 v, float angle, V3 axis) {
-  float c = pm::cos(angle);
-  float s = pm::sin(angle);
+  float c = om::cos(angle);
+  float s = om::sin(angle);
   V3 term0 = v * c;
   V3 term1 = cross(axis, v) * s;
   V3 term2 = axis * ((1.f - c) * dot(axis, v));
@@ -819,18 +844,18 @@ V3 rotate_axis_angle(V3 v, float angle, V3 axis) {
 }
 
 V3 rotate_to(V3 inp, V3 target, float sign) {
-  float angle = pm::acos(dot(inp, target));
+  float angle = om::acos(dot(inp, target));
   V3 axis = normalized(cross(inp, target));
   return rotate_axis_angle(inp, sign * angle, axis);
 }
 
 // projection.h:24-32
 V3 find_relative_vec(V3 vec, float phi, float theta) {
-  float sin_theta = pm::sin(theta);
-  V3 local = {sin_theta * pm::cos(phi), sin_theta * pm::sin(phi),
-              pm::cos(theta)};
+  float sin_theta = om::sin(theta);
+  V3 local = {sin_theta * om::cos(phi), sin_theta * om::sin(phi),
+              om::cos(theta)};
   V3 z = {0.f, 0.f, 1.f};
-  float angle = pm::acos(dot(vec, z));
+  float angle = om::acos(dot(vec, z));
   V3 axis = normalized(cross(vec, z));
   return normalized(rotate_axis_angle(local, -angle, axis));
 }
@@ -848,7 +873,7 @@ V3 refract_by_normal(float ior, V3 vec, V3 normal) {
   float in_sqrt = 1 - frac * frac * (1 - cos_to_normal * cos_to_normal);
   V3 n_eff = exiting ? -normal : normal;
   if (in_sqrt > 0.f) {
-    float angle = pm::acos(pm::sqrt(in_sqrt));
+    float angle = om::acos(pm::sqrt(in_sqrt));
     V3 axis = normalized(cross(vec, n_eff));
     return normalized(rotate_axis_angle(-n_eff, angle, axis));
   }
@@ -1012,7 +1037,7 @@ RGB diffuse_eval(RGB albedo) { return albedo * kInvPi; }
 
 RGB glossy_eval(const Material &m, RGB spec, V3 in, V3 out, V3 n) {
   float c = std::max(dot(reflect_over_normal(in, n), out), 0.0f);
-  return (spec * m.glossy_norm) * pm::pow(c, m.shininess);
+  return (spec * m.glossy_norm) * om::pow(c, m.shininess);
 }
 
 // GGX microfacet reflection (Walter et al. 2007, "Microfacet Models for
@@ -1029,6 +1054,13 @@ RGB schlick(RGB f0, float c) {
           f0.b + (1.f - f0.b) * m5};
 }
 
+// GGX normal distribution D(h) = a2 / (pi ((n.h)^2 (a2 - 1) + 1)^2)
+// (Walter et al. 2007, eq. 33)
+float ggx_d(float ch, float a2) {
+  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
+  return a2 / (((float)M_PI * dd) * dd);
+}
+
 RGB ggx_eval(const Material &m, V3 in, V3 out, V3 n) {
   V3 wo = -in;
   if (dot(wo, n) < 0.f) {
@@ -1043,8 +1075,7 @@ RGB ggx_eval(const Material &m, V3 in, V3 out, V3 n) {
   float a2 = a * a;
   V3 h = normalized(wo + out);
   float ch = dot(h, n);
-  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
-  float d = a2 / (((float)M_PI * dd) * dd);
+  float d = ggx_d(ch, a2);
   float g = ggx_g1(co, a2) * ggx_g1(ci, a2);
   RGB f = schlick(m.specular, dot(wo, h));
   float scale = (d * g) / ((4.f * ci) * co);
@@ -1081,7 +1112,7 @@ BSDFSample diffuse_sample(RGB albedo, V3 in, V3 n, RngState &rng) {
   float v0 = rng.next();
   float v1 = rng.next();
   float phi = (float)(2 * M_PI * (double)v0);
-  float theta = pm::asin(pm::sqrt(v1));
+  float theta = om::asin(pm::sqrt(v1));
   V3 aligned = n;
   if (dot(in, n) > 0.f) {
     aligned = -n;
@@ -1094,7 +1125,7 @@ BSDFSample glossy_sample(const Material &m, V3 in, V3 n, RngState &rng) {
   float v1 = rng.next();
   V3 reflection = reflect_over_normal(in, n);
   float phi = (float)(2 * M_PI * (double)v0);
-  float psi = pm::acos(pm::pow(v1, m.inv_shininess_p_1));
+  float psi = om::acos(om::pow(v1, m.inv_shininess_p_1));
   return {find_relative_vec(reflection, phi, psi), m.specular};
 }
 
@@ -1124,7 +1155,7 @@ BSDFSample ggx_sample(const Material &m, V3 in, V3 n, RngState &rng) {
   float sin_t = pm::sqrt(std::max(0.f, 1.f - cos_t * cos_t));
   V3 b1, b2;
   onb(n, b1, b2);
-  V3 h = normalized((b1 * (sin_t * pm::cos(phi)) + b2 * (sin_t * pm::sin(phi))) +
+  V3 h = normalized((b1 * (sin_t * om::cos(phi)) + b2 * (sin_t * om::sin(phi))) +
                     n * cos_t);
   float k = 2.f * dot(wo, h);
   V3 wi = normalized(h * k - wo);
@@ -1338,7 +1369,7 @@ float term_prob(const oracle_settings &st, unsigned iters, RGB mult) {
     RGB q = {mult.r / (mult.r + 1), mult.g / (mult.g + 1), mult.b / (mult.b + 1)};
     q = q * 0.57f;
     float sq = std::clamp((q.r * q.r + q.g * q.g) + q.b * q.b, 0.0f, 1.0f);
-    float p = std::fabs(pm::pow(1 - sq, st.term_prob_exp));
+    float p = std::fabs(om::pow(1 - sq, st.term_prob_exp));
     return std::max(p, st.term_prob_min_prob);
   }
   default: {
@@ -1354,7 +1385,7 @@ BSDFSample uniform_dir_sample(const Material &m, V3 in, V3 n, RngState &rng) {
   float v1 = rng.next();
   bool whole = !is_brdf(m);
   float phi = (float)(2 * M_PI * (double)v0);
-  float theta = pm::acos(whole ? 2 * v1 - 1 : v1);
+  float theta = om::acos(whole ? 2 * v1 - 1 : v1);
   V3 dir = find_relative_vec(n, phi, theta);
   float inv_prob = (float)((whole ? 4 : 2) * M_PI);
   RGB f = continuous_eval(m, in, dir, n);
@@ -1391,6 +1422,7 @@ struct RenderCtx {
   const unsigned *idxs = nullptr; // InitialIdxAndDir: BVH-order hit triangle per location
   unsigned n_steps = 0;           // OutputPerStep: steps per path, 0 = off
   unsigned spp = 0;               // samples per location (Uniform RNG seed)
+  unsigned sample_offset = 0;     // Sobol row of sample s is s + sample_offset
 };
 
 // rendering_equation.h:27-129 + rendering_equation_iteration.h:9-153 for one
@@ -1405,9 +1437,12 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
   unsigned location = x + y * c.x_dim;
   RngState rng;
   if (st.rng == 1) {
-    get_uniform_generator(sample_idx, location, c.spp, rng);
+    // a progressive frame seeds as the kernels do: sample + location x spp
+    // + offset x locations (the reference's seed for offset 0)
+    get_uniform_generator(sample_idx + c.sample_offset * (c.x_dim * c.y_dim), location, c.spp,
+                          rng);
   } else {
-    get_generator(*c.sobol, sample_idx, location, rng);
+    get_generator(*c.sobol, sample_idx + c.sample_offset, location, rng);
   }
   Ray ray;
   if (c.rays != nullptr) {
@@ -1759,19 +1794,59 @@ struct SpecExtras {
   unsigned n_steps = 0;             // OutputPerStep
 };
 
+// The flattened scene and its SBVH, built once for renders that share the
+// scene and the accel settings (flat_triangle.h:79-146, generator.cu:17-66).
+struct Prepared {
+  FlatScene sc;
+  BVH bvh;
+  oracle_settings st; // the settings the BVH and light table were built with
+};
+
+void prepare(const oracle_scene &scene, const oracle_settings &st, Prepared &out) {
+  out.sc = flatten(scene);
+  if (st.light_sampler != 0) {
+    out.sc.light_tris.clear();
+    out.sc.light_cdf.clear();
+  }
+  out.bvh = build_bvh(out.sc.tris, st.overlap_threshold, st.use_spatial_splits != 0,
+                      st.traversal_per_intersect_cost, st.target_objects);
+  out.st = st;
+}
+
+// which rows of the image a render covers: row_start, row_start + stride, ...
+// below row_end
+struct RowSet {
+  unsigned start = 0, end = 0, stride = 1;
+  bool has(unsigned y) const {
+    return y >= start && y < end && (y - start) % stride == 0;
+  }
+};
+
+bool render_prepared(const Prepared &pr, const oracle_settings &st, unsigned spp,
+                     unsigned x_dim, unsigned y_dim, const float *f2w, RowSet rows,
+                     unsigned sample_offset, RenderOut &out, double *seconds,
+                     const SpecExtras &ex = SpecExtras());
+
 bool render_image(const oracle_scene &scene, const oracle_settings &st,
                   unsigned spp, unsigned x_dim, unsigned y_dim,
                   const float *f2w, unsigned row_start, unsigned row_end,
                   RenderOut &out, double *seconds, const SpecExtras &ex = SpecExtras()) {
-  FlatScene sc = flatten(scene);
-  if (st.light_sampler != 0) {
-    sc.light_tris.clear();
-    sc.light_cdf.clear();
-  }
-  BVH bvh = build_bvh(sc.tris, st.overlap_threshold, st.use_spatial_splits != 0,
-                      st.traversal_per_intersect_cost, st.target_objects);
+  Prepared pr;
+  prepare(scene, st, pr);
+  RowSet rows;
+  rows.start = row_start;
+  rows.end = row_end;
+  return render_prepared(pr, st, spp, x_dim, y_dim, f2w, rows, 0, out, seconds, ex);
+}
+
+bool render_prepared(const Prepared &pr, const oracle_settings &st, unsigned spp,
+                     unsigned x_dim, unsigned y_dim, const float *f2w, RowSet rows,
+                     unsigned sample_offset, RenderOut &out, double *seconds,
+                     const SpecExtras &ex) {
+  const FlatScene &sc = pr.sc;
+  const BVH &bvh = pr.bvh;
   SobolTable sobol;
-  if (!sobol_table(st.max_sample_size, spp, sobol)) {
+  if (!sobol_table(st.max_sample_size, sample_offset + spp, sobol)) {
     return false;
   }
   oracle_work_division w;
@@ -1793,8 +1868,8 @@ bool render_image(const oracle_scene &scene, const oracle_settings &st,
       bvh_idxs[i] = orig_to_bvh[ex.idxs[i]];
     }
   }
-  RenderCtx ctx{&sc, &bvh, &st, &sobol, read_affine(f2w ? f2w : identity), x_dim, y_dim,
-                ex.rays, ex.idxs ? bvh_idxs.data() : nullptr, ex.n_steps, spp};
+  RenderCtx ctx{&sc,    &bvh,  &st, &sobol, read_affine(f2w ? f2w : identity), x_dim, y_dim,
+                ex.rays, ex.idxs ? bvh_idxs.data() : nullptr, ex.n_steps, spp, sample_offset};
   const unsigned n_out = ex.n_steps ? ex.n_steps : 1;
   const size_t n_pix = (size_t)x_dim * y_dim;
   auto t0 = std::chrono::steady_clock::now();
@@ -1805,7 +1880,7 @@ bool render_image(const oracle_scene &scene, const oracle_settings &st,
   run_blocks_n(
       w, st.n_threads, st.reduce_order, n_out,
       [&](unsigned, const ThreadInfo &ti, RGB *vals) {
-        if (ti.y < row_start || ti.y >= row_end) {
+        if (!rows.has(ti.y)) {
           return;
         }
         if (ex.n_steps) {
@@ -1870,6 +1945,52 @@ bool render_image(const oracle_scene &scene, const oracle_settings &st,
     *seconds = std::chrono::duration<double>(t1 - t0).count();
   }
   return true;
+}
+
+// selected rows in order
+std::vector<unsigned> row_list(RowSet rows) {
+  std::vector<unsigned> out;
+  for (unsigned y = rows.start; y < rows.end; y += rows.stride) {
+    out.push_back(y);
+  }
+  return out;
+}
+
+// Per-pixel loop shared by the FP64 and per-sample modes: fn(ctx, x, y, row
+// index) for every pixel of the selected rows, pixels in parallel.
+template <typename PixelFn>
+bool for_pixels(const Prepared &pr, const oracle_settings &st, unsigned spp, unsigned x_dim,
+                unsigned y_dim, const float *f2w, RowSet rows, unsigned sample_offset,
+                double *seconds, PixelFn fn) {
+  SobolTable sobol;
+  if (!sobol_table(st.max_sample_size, sample_offset + spp, sobol)) {
+    return false;
+  }
+  RenderCtx ctx{&pr.sc, &pr.bvh, &st, &sobol, read_affine(f2w), x_dim, y_dim};
+  ctx.spp = spp;
+  ctx.sample_offset = sample_offset;
+  std::vector<unsigned> ys = row_list(rows);
+  const long n = (long)ys.size() * x_dim;
+  int nt = st.n_threads ? (int)st.n_threads : omp_get_max_threads();
+  auto t0 = std::chrono::steady_clock::now();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+  for (long i = 0; i < n; ++i) {
+    unsigned r = (unsigned)(i / x_dim);
+    unsigned x = (unsigned)(i % x_dim);
+    fn(ctx, x, ys[r], r);
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) {
+    *seconds = std::chrono::duration<double>(t1 - t0).count();
+  }
+  return true;
+}
+
+bool settings_match_prepared(const Prepared &pr, const oracle_settings &st) {
+  return pr.st.overlap_threshold == st.overlap_threshold &&
+         pr.st.use_spatial_splits == st.use_spatial_splits &&
+         pr.st.traversal_per_intersect_cost == st.traversal_per_intersect_cost &&
+         pr.st.target_objects == st.target_objects && pr.st.light_sampler == st.light_sampler;
 }
 
 std::vector<Tri> read_tris(const float *p, size_t n) {
@@ -2146,6 +2267,164 @@ int oracle_render_bgra(const oracle_scene *scene,
     out[4 * i + 3] = 0;
   }
   return 0;
+}
+
+// src/scene/camera.cpp:4-27: film_to_world = (scale * view)^-1 with
+// s = f x up, u = s x f, view rows (s, -s.pos), (u, -u.pos), (-f, f.pos),
+// scale = diag(1 / tan_w, 1 / tan_h, 1); evaluated in double from the float
+// vectors and rounded to float (Eigen's float 4x4 inverse is not restated).
+void oracle_camera_transform(const float *look, const float *up, const float *pos,
+                             float height_angle_deg, float width_height_ratio, float *out) {
+  V3 f = normalized(read_v3(look));
+  V3 u0 = normalized(read_v3(up));
+  V3 p = read_v3(pos);
+  V3 s = cross(f, u0);
+  V3 u = cross(s, f);
+  float half = (float)M_PI * height_angle_deg / 360.f;
+  double tan_h = std::tan((double)half);
+  double tan_w = (double)width_height_ratio * tan_h;
+  double sc[3] = {1.0 / tan_w, 1.0 / tan_h, 1.0};
+  double rows[3][4] = {{s.x, s.y, s.z, -(double)dot(s, p)},
+                       {u.x, u.y, u.z, -(double)dot(u, p)},
+                       {-f.x, -f.y, -f.z, (double)dot(f, p)}};
+  double r[3][3], t[3];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) {
+      r[i][j] = rows[i][j] * sc[i];
+    }
+    t[i] = rows[i][3] * sc[i];
+  }
+  // inverse of [r t; 0 1] = [r^-1, -r^-1 t], r^-1 by cofactors
+  double det = r[0][0] * (r[1][1] * r[2][2] - r[1][2] * r[2][1]) -
+               r[0][1] * (r[1][0] * r[2][2] - r[1][2] * r[2][0]) +
+               r[0][2] * (r[1][0] * r[2][1] - r[1][1] * r[2][0]);
+  double inv[3][3] = {
+      {(r[1][1] * r[2][2] - r[1][2] * r[2][1]) / det, (r[0][2] * r[2][1] - r[0][1] * r[2][2]) / det,
+       (r[0][1] * r[1][2] - r[0][2] * r[1][1]) / det},
+      {(r[1][2] * r[2][0] - r[1][0] * r[2][2]) / det, (r[0][0] * r[2][2] - r[0][2] * r[2][0]) / det,
+       (r[0][2] * r[1][0] - r[0][0] * r[1][2]) / det},
+      {(r[1][0] * r[2][1] - r[1][1] * r[2][0]) / det, (r[0][1] * r[2][0] - r[0][0] * r[2][1]) / det,
+       (r[0][0] * r[1][1] - r[0][1] * r[1][0]) / det}};
+  for (int i = 0; i < 3; ++i) {
+    double ti = -(inv[i][0] * t[0] + inv[i][1] * t[1] + inv[i][2] * t[2]);
+    for (int j = 0; j < 3; ++j) {
+      out[4 * i + j] = (float)inv[i][j];
+    }
+    out[4 * i + 3] = (float)ti;
+  }
+}
+
+int oracle_debug_bsdf(const oracle_material *material, uint32_t op, const float *in,
+                      uint32_t n, float *out) {
+  Material m = make_material(*material);
+  SobolTable draws;
+  draws.dimension_bound = 4;
+  draws.initial_dimension_bound = 4;
+  for (uint32_t i = 0; i < n; ++i) {
+    const float *a = in + (size_t)9 * i;
+    if (op == 0) {
+      RGB f = continuous_eval(m, read_v3(a), read_v3(a + 3), read_v3(a + 6));
+      out[3 * i] = f.r;
+      out[3 * i + 1] = f.g;
+      out[3 * i + 2] = f.b;
+    } else if (op == 1) {
+      draws.vals.assign(a + 6, a + 9);
+      draws.vals.push_back(0.f);
+      RngState rng;
+      rng.table = &draws;
+      rng.sample = 0;
+      rng.dim = 0;
+      BSDFSample smp = continuous_sample(m, read_v3(a), read_v3(a + 3), rng);
+      float *o = out + (size_t)6 * i;
+      o[0] = smp.dir.x;
+      o[1] = smp.dir.y;
+      o[2] = smp.dir.z;
+      o[3] = smp.mult.r;
+      o[4] = smp.mult.g;
+      o[5] = smp.mult.b;
+    } else if (op == 2) {
+      out[i] = ggx_d(a[0], a[1] * a[1]);
+    } else {
+      return 1;
+    }
+  }
+  return 0;
+}
+
+void *oracle_prepare(const oracle_scene *scene, const oracle_settings *settings) {
+  Prepared *p = new Prepared();
+  prepare(*scene, *settings, *p);
+  return p;
+}
+
+void oracle_prepared_free(void *p) { delete static_cast<Prepared *>(p); }
+
+int oracle_render_prepared(void *prepared, const oracle_settings *settings,
+                           uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
+                           const float *film_to_world, const oracle_render_options *opt,
+                           float *out, double *out_f64, double *seconds) {
+  const Prepared &pr = *static_cast<const Prepared *>(prepared);
+  if (!settings_match_prepared(pr, *settings)) {
+    return 2;
+  }
+  RowSet rows;
+  rows.start = opt->row_start;
+  rows.end = opt->row_end ? std::min(opt->row_end, y_dim) : y_dim;
+  rows.stride = opt->row_stride ? opt->row_stride : 1;
+  const unsigned off = opt->sample_offset;
+  const unsigned spp = samples_per;
+  if (spp == 0 || x_dim == 0 || y_dim == 0 || film_to_world == nullptr) {
+    return 1;
+  }
+  if (opt->mode == 0) {
+    RenderOut r;
+    if (!render_prepared(pr, *settings, spp, x_dim, y_dim, film_to_world, rows, off, r,
+                         seconds)) {
+      return 1;
+    }
+    for (size_t i = 0; i < r.rgb.size(); ++i) {
+      if (!rows.has((unsigned)(i / x_dim))) {
+        continue;
+      }
+      out[3 * i] = r.rgb[i].r;
+      out[3 * i + 1] = r.rgb[i].g;
+      out[3 * i + 2] = r.rgb[i].b;
+    }
+    return 0;
+  }
+  if (opt->mode == 1) {
+    // FP64 accumulation: each sample's radiance summed per pixel in double
+    bool ok = for_pixels(pr, *settings, spp, x_dim, y_dim, film_to_world, rows, off, seconds,
+                         [&](const RenderCtx &ctx, unsigned x, unsigned y, unsigned) {
+                           double a = 0, b = 0, c = 0;
+                           for (unsigned s = 0; s < spp; ++s) {
+                             RGB v = integrate_sample(ctx, s, x, y);
+                             a += (double)v.r;
+                             b += (double)v.g;
+                             c += (double)v.b;
+                           }
+                           size_t i = 3 * ((size_t)x + (size_t)y * x_dim);
+                           out_f64[i] = a / spp;
+                           out_f64[i + 1] = b / spp;
+                           out_f64[i + 2] = c / spp;
+                         });
+    return ok ? 0 : 1;
+  }
+  if (opt->mode == 2) {
+    // per-sample radiance [selected row][x][sample][3]
+    bool ok = for_pixels(pr, *settings, spp, x_dim, y_dim, film_to_world, rows, off, seconds,
+                         [&](const RenderCtx &ctx, unsigned x, unsigned y, unsigned r) {
+                           float *o = out + 3 * (((size_t)r * x_dim + x) * spp);
+                           for (unsigned s = 0; s < spp; ++s) {
+                             RGB v = integrate_sample(ctx, s, x, y);
+                             o[3 * s] = v.r;
+                             o[3 * s + 1] = v.g;
+                             o[3 * s + 2] = v.b;
+                           }
+                         });
+    return ok ? 0 : 1;
+  }
+  return 1;
 }
 
 int oracle_render_samples(const oracle_scene *scene,

@@ -15,7 +15,11 @@
  * multiply-add (built with -ffp-contract=off); transcendental functions come
  * from path_gb300/csrc/pmath.h so that the oracle and the kernels agree bit
  * for bit (the reference's own -Ofast build is not reproducible at the ulp
- * level, see CMakeLists.txt:35-40).
+ * level, see CMakeLists.txt:35-40).  A second build, liboracle_libm.so
+ * (-DORACLE_LIBM), calls the C library's sinf / cosf / asinf / acosf / powf
+ * where the reference calls the std:: functions instead: the distance
+ * between the two builds' images is how far the shared polynomials move an
+ * image from the C library's arithmetic.
  *
  * Parity pins: closest-hit ids against the reference's brute-force LoopAll
  * rule and hand-written rays (tests/src/intersection.cu:120-177), clipped
@@ -169,6 +173,47 @@ int oracle_render(const oracle_scene *scene, const oracle_settings *settings,
                   uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
                   const float *film_to_world, uint32_t row_start,
                   uint32_t row_end, float *out, double *seconds);
+
+/* scene::get_camera_transform (src/scene/camera.cpp:4-27): 3x4 row-major
+ * film_to_world */
+void oracle_camera_transform(const float *look, const float *up, const float *pos,
+                             float height_angle_deg, float width_height_ratio, float *out);
+
+/* BSDF evaluation for tests, n records of 9 floats in `in`:
+ *   op 0: continuous_eval, in = (in dir, out dir, normal), out [n][3];
+ *   op 1: continuous_sample with the draws u0, u1, u2 in that order,
+ *         in = (in dir, normal, u0, u1, u2), out [n][6] = (dir, multiplier);
+ *   op 2: the GGX distribution D, in = (n.h, alpha, -), out [n]. */
+int oracle_debug_bsdf(const oracle_material *material, uint32_t op, const float *in,
+                      uint32_t n, float *out);
+
+/* Options of a render of a prepared scene. */
+typedef struct {
+  uint32_t row_start;     /* rows row_start, row_start + row_stride, ... */
+  uint32_t row_end;       /* below row_end (0 = y_dim) */
+  uint32_t row_stride;    /* 0 or 1 = every row */
+  uint32_t sample_offset; /* Sobol row of sample s is s + sample_offset */
+  uint32_t mode;          /* 0: FP32 image through WorkDivision and the
+                             reducer (the reference's CPU path), out =
+                             [y_dim][x_dim][3] floats, selected rows written;
+                             1: every sample summed per pixel in double,
+                             out_f64 = [y_dim][x_dim][3] mean radiance;
+                             2: per-sample radiance, out = [selected rows]
+                             [x_dim][samples_per][3] */
+} oracle_render_options;
+
+/* The flattened scene and its SBVH, built once (free with
+ * oracle_prepared_free) for renders with the same accel settings and light
+ * sampler. */
+void *oracle_prepare(const oracle_scene *scene, const oracle_settings *settings);
+void oracle_prepared_free(void *prepared);
+/* returns 0, 1 on invalid arguments, 2 when the settings' accel fields or
+ * light sampler differ from the ones the scene was prepared with.  seconds =
+ * wall time of the integration (+ reduction in mode 0). */
+int oracle_render_prepared(void *prepared, const oracle_settings *settings,
+                           uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
+                           const float *film_to_world, const oracle_render_options *opt,
+                           float *out, double *out_f64, double *seconds);
 
 /* InitialRays (idxs NULL) or InitialIdxAndDir (idxs = scene-order triangle
  * hit at distance 1 along each ray) sample spec.  out = [n_rays][3]

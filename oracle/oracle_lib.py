@@ -18,6 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "liboracle.so")
+# the same oracle with the C library's sinf / cosf / asinf / acosf / powf in
+# place of the shared polynomials (the reference calls std:: functions)
+LIB_LIBM = os.path.join(BUILD_DIR, "liboracle_libm.so")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 c_u32 = ctypes.c_uint32
@@ -60,6 +63,11 @@ class OracleSettings(ctypes.Structure):
                 ("rng", c_u32)]
 
 
+class RenderOptions(ctypes.Structure):
+    _fields_ = [("row_start", c_u32), ("row_end", c_u32), ("row_stride", c_u32),
+                ("sample_offset", c_u32), ("mode", c_u32)]
+
+
 class WorkDivision(ctypes.Structure):
     _fields_ = [(n, c_u32) for n in ["block_size", "base_samples_per_thread",
                                      "n_threads_per_unit_extra", "sample_block_size",
@@ -67,35 +75,48 @@ class WorkDivision(ctypes.Structure):
                                      "num_x_blocks", "num_y_blocks", "x_dim", "y_dim"]]
 
 
-def build(force=False):
+def _build_one(lib_path, defines, force):
     src = os.path.join(HERE, "oracle.cpp")
     deps = [src, os.path.join(HERE, "oracle.h"),
             os.path.join(ROOT, "path_gb300", "csrc", "pmath.h"),
             os.path.join(ROOT, "path_gb300", "csrc", "pmath_coeffs.h")]
-    if not force and os.path.exists(LIB) and all(
-            os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
-        return LIB
+    if not force and os.path.exists(lib_path) and all(
+            os.path.getmtime(d) <= os.path.getmtime(lib_path) for d in deps):
+        return None
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = ["g++", "-O2", "-std=gnu++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-           "-I" + os.path.join(CUDA_HOME, "include"), src, "-o", tmp,
+           *defines, "-I" + os.path.join(CUDA_HOME, "include"), src, "-o", tmp,
            "-L" + os.path.join(CUDA_HOME, "lib64"), "-lcurand",
            "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
-    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
-    if proc.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + proc.stdout)
-    os.replace(tmp, LIB)
+    return subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True), \
+        tmp, lib_path
+
+
+def build(force=False):
+    """Compiles liboracle.so and liboracle_libm.so (in parallel) when stale."""
+    jobs = [j for j in (_build_one(LIB, [], force), _build_one(LIB_LIBM, ["-DORACLE_LIBM"], force))
+            if j is not None]
+    for proc, tmp, lib_path in jobs:
+        out, _ = proc.communicate()
+        if proc.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + out)
+        os.replace(tmp, lib_path)
     return LIB
 
 
+_libs = {}
 _lib = None
 
 
-def load():
+def load(libm=False):
+    """The oracle library; libm=True loads the build that calls the C
+    library's transcendental functions."""
     global _lib
-    if _lib is None:
+    key = bool(libm)
+    if key not in _libs:
         build()
-        lib = ctypes.CDLL(LIB)
+        lib = ctypes.CDLL(LIB_LIBM if key else LIB)
         lib.oracle_sbvh_build.restype = ctypes.c_void_p
         lib.oracle_sbvh_build.argtypes = [_PF, c_u32, c_f32, c_u32, c_f32, c_u32]
         for name in ["oracle_sbvh_free", "oracle_sbvh_sizes", "oracle_sbvh_export",
@@ -134,8 +155,20 @@ def load():
         lib.oracle_clipped_new_bounds.argtypes = [_PF, _PF, c_f32, c_f32, c_u32, _PF]
         lib.oracle_rotate_to.argtypes = [_PF, _PF, _PF]
         lib.oracle_find_relative_vec.argtypes = [_PF, c_f32, c_f32, _PF]
-        _lib = lib
-    return _lib
+        lib.oracle_camera_transform.argtypes = [_PF, _PF, _PF, c_f32, c_f32, _PF]
+        lib.oracle_debug_bsdf.argtypes = [ctypes.POINTER(OracleMaterial), c_u32, _PF, c_u32, _PF]
+        lib.oracle_prepare.restype = ctypes.c_void_p
+        lib.oracle_prepare.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(OracleSettings)]
+        lib.oracle_prepared_free.argtypes = [ctypes.c_void_p]
+        lib.oracle_render_prepared.argtypes = [ctypes.c_void_p, ctypes.POINTER(OracleSettings),
+                                               c_u32, c_u32, c_u32, _PF,
+                                               ctypes.POINTER(RenderOptions), _PF,
+                                               ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_double)]
+        _libs[key] = lib
+        if not key:
+            _lib = lib
+    return _libs[key]
 
 
 def _f(a):
@@ -213,6 +246,29 @@ class SBVH:
         return load().oracle_sah_cost(self._h, traversal_cost)
 
 
+def camera_transform(look, up, pos, height_angle_deg, width_height_ratio):
+    """get_camera_transform (camera.cpp:4-27) restated: 3x4 film_to_world."""
+    arr = [np.ascontiguousarray(v, np.float32) for v in (look, up, pos)]
+    out = np.zeros(12, np.float32)
+    load().oracle_camera_transform(_f(arr[0]), _f(arr[1]), _f(arr[2]), height_angle_deg,
+                                   width_height_ratio, _f(out))
+    return out
+
+
+def debug_bsdf(material, op, records):
+    """The oracle's BSDF code (oracle_debug_bsdf), same ops and layout as
+    path_gb300.api.debug_bsdf; material = any ctypes structure with the
+    path_material layout."""
+    rec = np.ascontiguousarray(records, np.float32).reshape(-1, 9)
+    width = {0: 3, 1: 6, 2: 1}[op]
+    out = np.zeros((len(rec), width), np.float32)
+    m = OracleMaterial()
+    ctypes.memmove(ctypes.byref(m), ctypes.byref(material), ctypes.sizeof(OracleMaterial))
+    if load().oracle_debug_bsdf(ctypes.byref(m), op, _f(rec), len(rec), _f(out)) != 0:
+        raise ValueError("bad BSDF probe arguments")
+    return out[:, 0] if op == 2 else out
+
+
 def clipped_new_bounds(tri, bounds, left, right, axis):
     tri = np.ascontiguousarray(tri, np.float32).reshape(9)
     bounds = np.ascontiguousarray(bounds, np.float32).reshape(6)
@@ -284,6 +340,19 @@ def settings_from(s, reduce_order=1, n_threads=0):
                           r.dir_sampler, r.term_prob, r.term_prob_prob, r.term_prob_iters,
                           r.term_prob_exp, r.term_prob_min_prob, r.max_sample_size,
                           r.back_cull_emission, reduce_order, n_threads, r.rng)
+
+
+def workload_settings(max_depth, reduce_order=0, n_threads=0):
+    """Oracle settings for 'max depth D, no Russian roulette, Sobol' without
+    the library: render::Settings{} defaults (include/render/settings.h
+    :27-45 -- WorkDivision {256, 32, no forcing, 8, 16384, 0.5, 32}, reducer
+    x-block 256, 128 CPU blocks per launch, SBVH overlap 1e-5 without
+    spatial splits, traversal cost 0.5, 4 target objects, RandomTriangle,
+    BSDF sampler) with NIters{D - 1}, 256 Sobol dimensions and back-face
+    culled emission."""
+    return OracleSettings(WD(256, 32, 0, 8, 16384, 0.5, 32), WD(256, 256, 0, 8, 16384, 0.5, 32),
+                          128, 1e-5, 0, 0.5, 4, 0, 0, 1, 0.5, max_depth - 1, 50.0, 0.1, 256, 1,
+                          reduce_order, n_threads, 0)
 
 
 class SceneArrays:
@@ -364,3 +433,63 @@ def render_steps(scene_arrays, settings, samples_per, x_dim, y_dim, film_to_worl
     if rc != 0:
         raise RuntimeError("oracle render failed")
     return out
+
+
+class Prepared:
+    """A scene flattened and its SBVH built once (oracle_prepare), for
+    several renders with the same accel settings and light sampler.
+    libm=True uses the build with the C library's transcendental functions."""
+
+    def __init__(self, scene_arrays, settings, libm=False):
+        self._arrays = scene_arrays
+        self._lib = load(libm)
+        self._h = self._lib.oracle_prepare(ctypes.byref(scene_arrays.c), ctypes.byref(settings))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.oracle_prepared_free(h)
+            self._h = None
+
+    def _run(self, settings, spp, x_dim, y_dim, f2w, rows, stride, sample_offset, mode, out,
+             out64):
+        r0, r1 = (0, y_dim) if rows is None else rows
+        opt = RenderOptions(r0, r1, max(1, stride), sample_offset, mode)
+        f2w = np.ascontiguousarray(f2w, np.float32).reshape(12)
+        secs = ctypes.c_double()
+        rc = self._lib.oracle_render_prepared(
+            self._h, ctypes.byref(settings), spp, x_dim, y_dim, _f(f2w), ctypes.byref(opt),
+            None if out is None else _f(out),
+            None if out64 is None else out64.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            ctypes.byref(secs))
+        if rc == 2:
+            raise ValueError("settings differ from the ones the scene was prepared with")
+        if rc != 0:
+            raise RuntimeError("oracle render failed")
+        return secs.value
+
+    def render(self, settings, spp, x_dim, y_dim, f2w, rows=None, stride=1, sample_offset=0):
+        """FP32 image through WorkDivision and the reducer (the reference's
+        CPU path): ([y_dim, x_dim, 3] with the selected rows written,
+        seconds)."""
+        out = np.zeros((y_dim, x_dim, 3), np.float32)
+        secs = self._run(settings, spp, x_dim, y_dim, f2w, rows, stride, sample_offset, 0, out,
+                         None)
+        return out, secs
+
+    def render_f64(self, settings, spp, x_dim, y_dim, f2w, rows=None, stride=1, sample_offset=0):
+        """Mean radiance with every sample summed in double: ([y_dim, x_dim,
+        3] float64 with the selected rows written, seconds)."""
+        out = np.zeros((y_dim, x_dim, 3), np.float64)
+        secs = self._run(settings, spp, x_dim, y_dim, f2w, rows, stride, sample_offset, 1, None,
+                         out)
+        return out, secs
+
+    def sample_values(self, settings, spp, x_dim, y_dim, f2w, rows=None, stride=1,
+                      sample_offset=0):
+        """Per-sample radiance [selected rows, x_dim, spp, 3]."""
+        r0, r1 = (0, y_dim) if rows is None else rows
+        n_rows = len(range(r0, min(r1, y_dim), max(1, stride)))
+        out = np.zeros((n_rows, x_dim, spp, 3), np.float32)
+        self._run(settings, spp, x_dim, y_dim, f2w, rows, stride, sample_offset, 2, out, None)
+        return out

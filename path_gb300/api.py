@@ -475,6 +475,19 @@ def debug_pmath(fn, x, y=None):
     return out
 
 
+def debug_bsdf(material, op, records):
+    """The kernels' BSDF code on the GPU (path_debug_bsdf): op 0 eval
+    (records [n, 9] = in dir, out dir, normal) -> [n, 3]; op 1 sample
+    (records = in dir, normal, u0, u1, u2) -> [n, 6] (dir, multiplier); op 2
+    GGX D (records [:, 0] = n.h, [:, 1] = alpha) -> [n]."""
+    rec = np.ascontiguousarray(records, np.float32).reshape(-1, 9)
+    width = {0: 3, 1: 6, 2: 1}[op]
+    out = np.zeros((len(rec), width), np.float32)
+    capi.check(capi.load().path_debug_bsdf(ctypes.byref(material), op, _fptr(rec), len(rec),
+                                           _fptr(out)))
+    return out[:, 0] if op == 2 else out
+
+
 def work_division(wd_settings, samples_per, x_dim, y_dim):
     out = (ctypes.c_uint32 * 11)()
     capi.check(capi.load().path_work_division(ctypes.byref(wd_settings), samples_per, x_dim,

@@ -667,6 +667,36 @@ path_status path_debug_pmath(uint32_t fn, const float *x, const float *y, float 
   });
 }
 
+path_status path_debug_bsdf(const path_material *material, uint32_t op, const float *in,
+                            uint32_t n, float *out) {
+  if (!material || !in || !out || op > 2 || material->type > PATH_BSDF_GGX) {
+    return fail(PATH_ERR_ARGUMENT, "bad BSDF probe arguments");
+  }
+  return guarded([&] {
+    const size_t out_floats = op == 0 ? 3 : op == 1 ? 6 : 1;
+    pg::DevMaterial dm = pg::to_dev(*material);
+    pg::DeviceBuffer dmat, din, dout;
+    pg::Status st = pg::cuda_status(dmat.upload(&dm, sizeof(dm), 0), "material");
+    if (st.good()) {
+      st = pg::cuda_status(din.upload(in, (size_t)n * 36, 0), "records");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(dout.ensure((size_t)n * out_floats * 4 + 4), "out");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(pg::launch_bsdf(dmat.as<pg::DevMaterial>(), op, din.as<float>(), n,
+                                           dout.as<float>(), 0),
+                           "BSDF kernel");
+    }
+    if (st.good() && n > 0) {
+      st = pg::cuda_status(
+          cudaMemcpy(out, dout.get(), (size_t)n * out_floats * 4, cudaMemcpyDeviceToHost),
+          "copy");
+    }
+    return from(st);
+  });
+}
+
 path_status path_work_division(const path_work_division_settings *settings,
                                uint32_t samples_per, uint32_t x_dim, uint32_t y_dim,
                                uint32_t *out) {

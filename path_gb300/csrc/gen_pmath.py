@@ -1,7 +1,7 @@
 """Fit the polynomial coefficients used by ``pmath.h``.
 
-The renderer's transcendental functions (sin, cos, asin, acos, log2, exp2)
-are evaluated by our own polynomial approximations so that the CUDA kernels
+The renderer's single-precision transcendental functions (sin, cos, asin,
+acos; pow is evaluated in double precision by pmath.h itself) are evaluated by our own polynomial approximations so that the CUDA kernels
 and the CPU oracle produce the same bits: both sides run the same sequence of
 IEEE-754 single-precision multiplies, adds, divides and square roots, with no
 fused multiply-add.  The coefficients come from a weighted least-squares fit
@@ -62,15 +62,6 @@ def fit_all():
              1e-12, 0.25, 6, lambda u: u,
              lambda u: u * np.sqrt(u) / np.arcsin(np.sqrt(u)))
     out["ASIN"] = a
-    # log2(m) = s * L(s^2), s = (m - 1) / (m + 1), m in [sqrt(1/2), sqrt(2))
-    smax = (np.sqrt(2) - 1) / (np.sqrt(2) + 1)
-    lg = _fit(lambda u: np.log2((1 + np.sqrt(u)) / (1 - np.sqrt(u))) / np.sqrt(u),
-              1e-12, smax ** 2, 4, lambda u: u, lambda u: np.ones_like(u))
-    out["LOG2"] = lg
-    # exp2(f) = E(f), |f| <= 0.5
-    e = _fit(lambda f: np.exp2(f), -0.5, 0.5, 7, lambda f: f,
-             lambda f: 1.0 / np.exp2(f))
-    out["EXP2"] = e
     return out
 
 
@@ -95,8 +86,6 @@ def report(coefs):
     x2 = (x * x).astype(np.float32)
     as_a = (x + (x * x2).astype(np.float32) * _horner32(c32["ASIN"], x2)).astype(np.float32)
     print("asin ulps", _ulps(as_a, np.arcsin(x.astype(np.float64))))
-    f = np.linspace(-0.5, 0.5, 200001).astype(np.float32)
-    print("exp2 ulps", _ulps(_horner32(c32["EXP2"], f), np.exp2(f.astype(np.float64))))
 
 
 def write_header(coefs, path):

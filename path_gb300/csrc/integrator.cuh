@@ -742,6 +742,13 @@ __device__ __forceinline__ rgb schlick(rgb f0, float c) {
                f0.b + (1.f - f0.b) * m5);
 }
 
+// GGX normal distribution D(h) = a2 / (pi ((n.h)^2 (a2 - 1) + 1)^2)
+// (Walter et al. 2007, eq. 33)
+__device__ __forceinline__ float ggx_d(float ch, float a2) {
+  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
+  return a2 / ((0x1.921fb6p+1f * dd) * dd); // (float)M_PI
+}
+
 // GGX microfacet reflection (Walter et al. 2007): D GGX, separable Smith G,
 // Schlick Fresnel
 __device__ rgb ggx_eval(const Mat &m, f3 in, f3 out, f3 n) {
@@ -757,8 +764,7 @@ __device__ rgb ggx_eval(const Mat &m, f3 in, f3 out, f3 n) {
   float a2 = m.roughness * m.roughness;
   f3 h = normalize(wo + out);
   float ch = dot(h, n);
-  float dd = (ch * ch) * (a2 - 1.f) + 1.f;
-  float d = a2 / ((0x1.921fb6p+1f * dd) * dd); // (float)M_PI
+  float d = ggx_d(ch, a2);
   float g = ggx_g1(co, a2) * ggx_g1(ci, a2);
   rgb f = schlick(m.specular, dot(wo, h));
   float scale = (d * g) / ((4.f * ci) * co);

@@ -179,6 +179,9 @@ cudaError_t launch_sobol_curand(const uint32_t *dirs, const uint32_t *scramble,
 
 cudaError_t launch_pmath(uint32_t fn, const float *x, const float *y,
                          float *out, uint32_t n, cudaStream_t s);
+// BSDF probe over n records of 9 floats (ops as path_debug_bsdf)
+cudaError_t launch_bsdf(const DevMaterial *mat, uint32_t op, const float *in, uint32_t n,
+                        float *out, cudaStream_t s);
 
 // tensor-core self-test: D [128][n] = A [128][k] . B [n][k]^T (BF16 in, FP32
 // out), one CTA; err set when the MMA did not complete

@@ -15,9 +15,13 @@
 // the library, held until the process exits.  Its device address is looked
 // up once per device, with that device current, by the first call made on
 // that device (cudaGetSymbolAddress); that first call should come before
-// any stream capture begins.  All calls share the array and it keeps the
-// last call's contents: the status word and counters are cleared by every
-// call, and calls whose GPU work overlaps in time race on the array.
+// any stream capture begins.  The cached address belongs to the device's
+// current context: like the renderer's own device buffers and stream it
+// does not survive cudaDeviceReset, so a process that resets a device must
+// not call this entry point on that device afterwards.  All calls share the
+// array and it keeps the last call's contents: the status word and counters
+// are cleared by every call, and calls whose GPU work overlaps in time race
+// on the array.
 #include "kernels.h"
 #include "renderer.h"
 
@@ -91,15 +95,17 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
       prep_.sbvh.overlap_threshold != st.overlap_threshold ||
       prep_.sbvh.use_spatial_splits != (st.use_spatial_splits != 0) ||
       prep_.sbvh.traversal_per_intersect_cost != st.traversal_per_intersect_cost ||
-      prep_.sbvh.target_objects != st.target_objects) {
+      prep_.sbvh.target_objects != st.target_objects ||
+      prep_.gpu_built != (st.gpu_build != 0)) {
     return Status::err(PATH_ERR_ARGUMENT,
                        "scene not resident on this renderer: render it once with path_render");
   }
   if (st.rng == PATH_RNG_SOBEL &&
-      (sobol_bound_ != st.max_sample_size || sobol_count_ < spp || !sobol_table_.get())) {
+      (sobol_bound_ != st.max_sample_size ||
+       sobol_count_ < (uint64_t)spec.sample_offset + spp || !sobol_table_.get())) {
     return Status::err(PATH_ERR_ARGUMENT,
-                       "Sobol table for this max_sample_size / samples_per not resident: "
-                       "render once with path_render");
+                       "Sobol table for this max_sample_size / sample_offset + samples_per "
+                       "not resident: render once with path_render");
   }
   Status sf = traversal_fits(st);
   if (!sf.good()) {
@@ -153,6 +159,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   p.x_dim = spec.x_dim;
   p.y_dim = spec.y_dim;
   p.spp = spp;
+  p.sample_offset = spec.sample_offset;
   p.wd = wd;
   const bool direct = !bgra && nsb == 1;
   p.out_rgb = direct ? static_cast<float *>(output.data) : part_a;

@@ -15,8 +15,8 @@
 // Accuracy (float32 ulps against the exact function): the polynomial
 // kernels are within 1.5 ulps on their reduced ranges (gen_pmath.py); after
 // argument reduction sin / cos are within 4e-7 absolute on [-2 pi, 2 pi],
-// asin / acos within 3 ulps on [-1, 1], and pow within 2e-5 relative for
-// exponents up to 60 (tests/test_oracle_pins.py::test_pmath_accuracy).
+// asin / acos within 3 ulps on [-1, 1]; pow is evaluated in double precision
+// and is within 1 ulp (tests/test_oracle_pins.py::test_pmath_accuracy).
 #pragma once
 
 #include <stdint.h>
@@ -209,46 +209,96 @@ PM_HD float acos(float x) {
   return PM_PI_HI - (2.0f * a - PM_PI_LO);
 }
 
-// log2 for finite x > 0
-PM_HD float log2_pos(float x) {
-  const float c[] = PM_LOG2_COEFFS;
-  int e = 0;
-  if (x < 0x1p-126f) {
-    x = x * 0x1p23f;
-    e = -23;
-  }
-  uint32_t b = as_uint(x);
-  e += (int)((b >> 23) & 0xffu) - 127;
-  float m = as_float((b & 0x007fffffu) | 0x3f800000u);
-  if (m > PM_SQRT2) {
-    m = m * 0.5f;
-    e += 1;
-  }
-  float s = (m - 1.0f) / (m + 1.0f);
-  float s2 = s * s;
-  return (float)e + s * horner(c, s2);
+// ---- pow, evaluated in double precision --------------------------------
+// pow(x, y) = 2^(y log2 x) with log2 and exp2 evaluated in IEEE double (+, -,
+// *, / only, which host and device round identically; no contraction) and
+// the result rounded once to float, so it is within one float ulp of the
+// exact power (tests/test_oracle_pins.py::test_pmath_accuracy).  log2 of the
+// mantissa m in [sqrt(1/2), sqrt(2)) is 2 atanh(s) / ln 2 with s = (m - 1) /
+// (m + 1), |s| <= 0.1716, by its Taylor series to s^25 (truncation below
+// 1e-19); 2^f for |f| <= 1/2 is exp(f ln 2) by its Taylor series to degree
+// 14 (truncation below 1e-18).
+
+PM_HD uint64_t as_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, sizeof(u));
+  return u;
+#endif
 }
 
-PM_HD float exp2(float t) {
-  const float c[] = PM_EXP2_COEFFS;
-  if (!(t == t)) {
-    return t;
+PM_HD double from_bits(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, sizeof(x));
+  return x;
+#endif
+}
+
+// round to nearest, ties to even, for |t| < 2^51
+PM_HD double rint_d(double t) {
+  const double shift = 6755399441055744.0; // 1.5 * 2^52
+  double r = t + shift;
+  return r - shift;
+}
+
+// log2 of a positive normal double
+PM_HD double log2_d(double x) {
+  uint64_t b = as_bits(x);
+  int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  double m = from_bits((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
   }
-  if (t > 128.0f) {
-    return as_float(0x7f800000u);
-  }
-  if (t < -150.0f) {
-    return 0.0f;
-  }
-  float nf = rint(t);
-  float f = t - nf;
-  float p = horner(c, f);
-  int n = (int)nf;
-  // scale by 2^n in two steps so intermediate powers stay normal
-  int n1 = n / 2;
-  int n2 = n - n1;
-  float s1 = as_float((uint32_t)(n1 + 127) << 23);
-  float s2 = as_float((uint32_t)(n2 + 127) << 23);
+  double s = (m - 1.0) / (m + 1.0);
+  double s2 = s * s;
+  double p = 1.0 / 25.0;
+  p = p * s2 + 1.0 / 23.0;
+  p = p * s2 + 1.0 / 21.0;
+  p = p * s2 + 1.0 / 19.0;
+  p = p * s2 + 1.0 / 17.0;
+  p = p * s2 + 1.0 / 15.0;
+  p = p * s2 + 1.0 / 13.0;
+  p = p * s2 + 1.0 / 11.0;
+  p = p * s2 + 1.0 / 9.0;
+  p = p * s2 + 1.0 / 7.0;
+  p = p * s2 + 1.0 / 5.0;
+  p = p * s2 + 1.0 / 3.0;
+  p = p * s2 + 1.0;
+  // 2 / ln 2
+  return (double)e + (2.8853900817779268 * s) * p;
+}
+
+// 2^t for -1100 < t < 1100
+PM_HD double exp2_d(double t) {
+  double n = rint_d(t);
+  double g = (t - n) * 0.69314718055994531; // ln 2
+  double p = 1.0 / 87178291200.0;           // 1/14!
+  p = p * g + 1.0 / 6227020800.0;
+  p = p * g + 1.0 / 479001600.0;
+  p = p * g + 1.0 / 39916800.0;
+  p = p * g + 1.0 / 3628800.0;
+  p = p * g + 1.0 / 362880.0;
+  p = p * g + 1.0 / 40320.0;
+  p = p * g + 1.0 / 5040.0;
+  p = p * g + 1.0 / 720.0;
+  p = p * g + 1.0 / 120.0;
+  p = p * g + 1.0 / 24.0;
+  p = p * g + 1.0 / 6.0;
+  p = p * g + 0.5;
+  p = p * g + 1.0;
+  p = p * g + 1.0;
+  // scale by 2^n in two steps so both factors are normal doubles
+  int k = (int)n;
+  int k1 = k / 2;
+  int k2 = k - k1;
+  double s1 = from_bits((uint64_t)(k1 + 1023) << 52);
+  double s2 = from_bits((uint64_t)(k2 + 1023) << 52);
   return (p * s1) * s2;
 }
 
@@ -260,10 +310,23 @@ PM_HD float pow(float x, float y) {
   if (x == 0.0f) {
     return y > 0.0f ? 0.0f : as_float(0x7f800000u);
   }
-  if (!(x > 0.0f)) {
+  if (!(x > 0.0f) || !(y == y)) {
     return as_float(0x7fc00000u);
   }
-  return exp2(y * log2_pos(x));
+  if (!isfinite(x) || !isfinite(y)) {
+    // the limits of 2^(y log2 x): infinite or zero by the sign of y log2 x
+    // (x == 1 was handled above, so that product is not zero)
+    double lx = isfinite(x) ? log2_d((double)x) : 1.0;
+    return (double)y * lx > 0.0 ? as_float(0x7f800000u) : 0.0f;
+  }
+  double t = (double)y * log2_d((double)x);
+  if (t > 129.0) {
+    return as_float(0x7f800000u);
+  }
+  if (t < -151.0) {
+    return 0.0f;
+  }
+  return (float)exp2_d(t);
 }
 
 } // namespace pm

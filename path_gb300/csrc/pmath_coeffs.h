@@ -11,8 +11,3 @@
 #define PM_ASIN_DEGREE 6
 #define PM_ASIN_COEFFS {1.666666716e-01f, 7.499948889e-02f, 4.465997219e-02f, 3.011252731e-02f, 2.460470051e-02f, 7.509509567e-03f, 3.464628384e-02f}
 
-#define PM_LOG2_DEGREE 4
-#define PM_LOG2_COEFFS {2.885390043e+00f, 9.617967010e-01f, 5.770835876e-01f, 4.116724432e-01f, 3.407351375e-01f}
-
-#define PM_EXP2_DEGREE 7
-#define PM_EXP2_COEFFS {1.000000000e+00f, 6.931471825e-01f, 2.402265072e-01f, 5.550410226e-02f, 9.618027136e-03f, 1.333392225e-03f, 1.546929125e-04f, 1.520191836e-05f}

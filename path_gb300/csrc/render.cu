@@ -280,6 +280,48 @@ __global__ void k_intersect(const RenderParams P, const float *rays, uint32_t n,
   t_out[i] = h.ok ? h.t : __int_as_float(0x7fc00000);
 }
 
+// draws handed out in order (BSDF probe)
+struct FixedDraws {
+  float v[3];
+  uint32_t k;
+  __device__ float next() { return v[(k++) % 3]; }
+};
+
+// BSDF probe: op 0 continuous_eval, op 1 continuous_sample with the record's
+// draws, op 2 the GGX distribution D (records of 9 floats, see
+// path_debug_bsdf)
+__global__ void k_bsdf(const DevMaterial *mat, uint32_t op, const float *in, uint32_t n,
+                       float *out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) {
+    return;
+  }
+  const Mat m = load_mat(mat);
+  const float *a = in + (size_t)9 * i;
+  if (op == 0) {
+    rgb f = continuous_eval(m, mk(a[0], a[1], a[2]), mk(a[3], a[4], a[5]), mk(a[6], a[7], a[8]));
+    out[3 * i] = f.r;
+    out[3 * i + 1] = f.g;
+    out[3 * i + 2] = f.b;
+  } else if (op == 1) {
+    FixedDraws d;
+    d.v[0] = a[6];
+    d.v[1] = a[7];
+    d.v[2] = a[8];
+    d.k = 0;
+    Sample smp = continuous_sample(m, mk(a[0], a[1], a[2]), mk(a[3], a[4], a[5]), d);
+    float *o = out + (size_t)6 * i;
+    o[0] = smp.dir.x;
+    o[1] = smp.dir.y;
+    o[2] = smp.dir.z;
+    o[3] = smp.mult.r;
+    o[4] = smp.mult.g;
+    o[5] = smp.mult.b;
+  } else {
+    out[i] = ggx_d(a[0], a[1] * a[1]);
+  }
+}
+
 __global__ void k_pmath(uint32_t fn, const float *x, const float *y, float *out,
                         uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -391,6 +433,17 @@ cudaError_t launch_intersect(const RenderParams &p, uint32_t traversal,
     dev::k_intersect<kTravBinary><<<nb, bs, 0, s>>>(p, rays, n_rays, bvh_to_orig,
                                                     idx_out, t_out);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bsdf(const DevMaterial *mat, uint32_t op, const float *in, uint32_t n,
+                        float *out, cudaStream_t s) {
+  const uint32_t bs = 128;
+  const uint32_t nb = (n + bs - 1) / bs;
+  if (nb == 0) {
+    return cudaSuccess;
+  }
+  dev::k_bsdf<<<nb, bs, 0, s>>>(mat, op, in, n, out);
   return cudaGetLastError();
 }
 

@@ -344,6 +344,33 @@ bool pnpoly(const float *vx, const float *vy, float tx, float ty) {
 }
 
 // ear clipping of one polygon (tinyobjloader v1.x triangulation)
+//
+// The steps below follow tinyobjloader v1.1.0's triangulation (projection
+// axes, corner epsilon, round limit) so that polygon faces split into the
+// same triangles, in the same order, as the reference's loader.  That
+// algorithm is used under tinyobjloader's licence:
+//
+//   The MIT License (MIT)
+//   Copyright (c) 2012-2017 Syoyo Fujita and many contributors.
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a
+//   copy of this software and associated documentation files (the
+//   "Software"), to deal in the Software without restriction, including
+//   without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and/or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to
+//   the following conditions:
+//
+//   The above copyright notice and this permission notice shall be included
+//   in all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS
+//   OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF
+//   MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT.
+//   IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY
+//   CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT,
+//   TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE
+//   SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 void triangulate(const std::vector<Corner> &face, const std::vector<float> &v,
                  std::vector<Corner> &out) {
   size_t n = face.size();

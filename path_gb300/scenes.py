@@ -77,8 +77,95 @@ def _box(width, height, depth, angle_deg, centre_xz):
     return np.stack(out)
 
 
-def cornell_camera(x_dim, y_dim):
-    return api.camera_transform((0, 0, -1), (0, 1, 0), (0, 0, 3.5), 40.0, x_dim / y_dim)
+class ArrayScene:
+    """The same scene description as api.Scene (scene::TriangleConstructor),
+    held in NumPy arrays instead of the library: add_material / add_mesh /
+    sizes / export behave as path_scene_add_material / path_scene_add_mesh /
+    path_scene_sizes / path_scene_export, bit for bit (face normals in
+    float32 without contraction, one emissive cluster per emissive
+    triangle, one identity instance per mesh).  For callers that must not
+    load libpath_gb300.so: the CPU oracle's timed baseline builds its scenes
+    with it."""
+
+    def __init__(self):
+        self._mats = []
+        self._tris, self._normals, self._tri_mat = [], [], []
+        self._mesh_ends, self._cluster_ends, self._clusters, self._xforms = [], [], [], []
+        self._n = 0
+
+    def add_material(self, m):
+        self._mats.append(m)
+        return len(self._mats) - 1
+
+    @staticmethod
+    def _emissive(m):
+        e = [np.float32(v) for v in m.emission]
+        return ((e[0] * e[0] + e[1] * e[1]) + e[2] * e[2]) > np.float32(1e-9)
+
+    @staticmethod
+    def _face_normals(tris):
+        t = tris.reshape(-1, 3, 3)
+        a, b = t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]
+        n = np.stack([a[:, 1] * b[:, 2] - a[:, 2] * b[:, 1],
+                      a[:, 2] * b[:, 0] - a[:, 0] * b[:, 2],
+                      a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]], 1)
+        n2 = (n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]
+        with np.errstate(invalid="ignore", divide="ignore"):
+            unit = n / np.sqrt(n2)[:, None]
+        unit = np.where((n2 > 0)[:, None], unit, n).astype(np.float32)
+        return np.tile(unit, (1, 3))
+
+    def add_mesh(self, triangles, material_idx, normals=None, object_to_world=None):
+        tris = np.ascontiguousarray(triangles, np.float32).reshape(-1, 9)
+        mats = np.ascontiguousarray(material_idx, np.uint32).reshape(-1)
+        if mats.size == 1 and len(tris) > 1:
+            mats = np.full(len(tris), mats[0], np.uint32)
+        if len(mats) != len(tris) or (len(mats) and int(mats.max()) >= len(self._mats)):
+            raise ValueError("material index out of range")
+        nrm = self._face_normals(tris) if normals is None else \
+            np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+        emissive = np.array([self._emissive(m) for m in self._mats], bool)
+        for i in np.nonzero(emissive[mats])[0] if len(mats) else []:
+            self._clusters.append((int(mats[i]), self._n + int(i), self._n + int(i) + 1))
+        self._tris.append(tris)
+        self._normals.append(nrm)
+        self._tri_mat.append(mats)
+        self._n += len(tris)
+        self._mesh_ends.append(self._n)
+        self._cluster_ends.append(len(self._clusters))
+        xf = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32) if object_to_world is \
+            None else np.ascontiguousarray(object_to_world, np.float32).reshape(12)
+        self._xforms.append(xf)
+
+    def sizes(self):
+        return {"triangles": self._n, "meshes": len(self._mesh_ends),
+                "instances": len(self._xforms), "clusters": len(self._clusters),
+                "materials": len(self._mats)}
+
+    def export(self):
+        from . import capi
+        cat = (lambda xs, shape, dt: np.concatenate(xs).astype(dt) if xs else
+               np.zeros(shape, dt))
+        mats = (capi.PathMaterial * max(len(self._mats), 1))(*self._mats)
+        return {
+            "triangles": cat(self._tris, (0, 9), np.float32),
+            "normals": cat(self._normals, (0, 9), np.float32),
+            "tri_material": cat(self._tri_mat, (0,), np.uint32),
+            "mesh_ends": np.array(self._mesh_ends, np.uint32),
+            "cluster_ends_per_mesh": np.array(self._cluster_ends, np.uint32),
+            "instance_xforms": np.array(self._xforms, np.float32).reshape(-1, 12),
+            "instance_mesh": np.arange(len(self._xforms), dtype=np.uint32),
+            "clusters": np.array(self._clusters, np.uint32).reshape(-1, 3),
+            "materials": mats, "n_materials": len(self._mats),
+        }
+
+
+def cornell_camera(x_dim, y_dim, transform=None):
+    """film_to_world of the pinhole camera at z = 3.5 looking down -z with a
+    40 degree vertical field of view; transform defaults to
+    api.camera_transform (any function of the same signature will do)."""
+    return (transform or api.camera_transform)((0, 0, -1), (0, 1, 0), (0, 0, 3.5), 40.0,
+                                               x_dim / y_dim)
 
 
 def _add_room(scene, with_boxes):
@@ -105,9 +192,9 @@ def _add_room(scene, with_boxes):
     return white
 
 
-def cornell_box():
-    """The 36-triangle Cornell box; returns (scene, camera builder)."""
-    scene = api.Scene()
+def cornell_box(scene_cls=None):
+    """The 36-triangle Cornell box (an api.Scene, or scene_cls())."""
+    scene = (scene_cls or api.Scene)()
     _add_room(scene, with_boxes=True)
     return scene
 
@@ -234,9 +321,10 @@ def uv_sphere(n_lat=100, n_lon=100, radius=0.3, centre=(-0.45, -0.7, 0.3)):
     return pos.reshape(-1, 9).astype(np.float32), n.reshape(-1, 9).astype(np.float32)
 
 
-def large_mesh_room(subdivisions=8, glass_lat=100, glass_lon=100):
-    """Room + light, displaced GGX icosphere and a glass sphere."""
-    scene = api.Scene()
+def large_mesh_room(subdivisions=8, glass_lat=100, glass_lon=100, scene_cls=None):
+    """Room + light, displaced GGX icosphere and a glass sphere (an
+    api.Scene, or scene_cls())."""
+    scene = (scene_cls or api.Scene)()
     _add_room(scene, with_boxes=False)
     ggx = scene.add_material(api.material("GGX", specular=(0.04, 0.04, 0.04), roughness=0.2))
     glass = scene.add_material(api.material("DielectricRefractive", specular=(1, 1, 1), ior=1.5))

@@ -1,0 +1,154 @@
+"""Parity of the benchmarked configuration and of the additions with the
+CPU oracle (GPU tests).
+
+* The large-mesh room at its full size (1,330,532 triangles: the 8x
+  subdivided displaced GGX icosphere and the glass sphere, SBVH built
+  exactly as in the benchmark) rendered at a small image (48 x 48, 4 spp,
+  depth 8) through both traversals and both integration approaches, against
+  the oracle: bit for bit through the binary traversal (the reference's tie
+  rule); within 1e-4 relative RMSE through the 8-wide traversal, whose
+  closest hit is order-independent and may differ only at exact-distance
+  ties.
+* The 4096-spp error reference: 4096 samples per pixel of the small Cornell
+  box summed in FP64 on the GPU (64 renders of 64 samples) against the
+  oracle's, every sample summed in FP64 (tests/golden/cornell_fp64_4096spp.npz,
+  made by tests/golden/make_fp64_reference.py): relative difference
+  below 1e-5 (the two differ only in the order of the sums).
+* GGX: the kernels' BSDF code (path_debug_bsdf) equals the oracle's bit for
+  bit on random records, and passes the same checks against Walter et al.
+  2007 as the oracle (tests/test_ggx.py).
+* Batched render against the oracle: each image of a three-scene batch
+  within 1e-4 relative RMSE of the oracle's render of its scene.
+"""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from path_gb300 import api, scenes
+from oracle import oracle_lib as ol
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import test_ggx  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+RMSE_TOL = 1e-4
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def large_mesh(lib, oracle):
+    scene = scenes.large_mesh_room(subdivisions=8)
+    st = ol.settings_from(scenes.path_settings(8, "binary"), reduce_order=1)
+    prep = ol.Prepared(ol.SceneArrays(scene.export()), st)
+    return scene, prep, st
+
+
+@pytest.mark.parametrize("case", ["binary_mega", "wide_mega", "wide_streaming"])
+def test_large_mesh_full_geometry_matches_oracle(large_mesh, case):
+    scene, prep, st = large_mesh
+    w = h = 48
+    spp = 4
+    f2w = scenes.cornell_camera(w, h)
+    want, _ = prep.render(st, spp, w, h, f2w)
+    s = scenes.path_settings(8, "binary" if case.startswith("binary") else "wide")
+    s.kernel_approach = 1 if case.endswith("streaming") else 0
+    got = np.zeros((h, w, 3), np.float32)
+    r = api.Renderer()
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), got, scene, spp, s)
+    assert r.stats()["device_status"] == 0
+    err = rel_rmse(got, want)
+    print(f"{case}: rel RMSE {err:.2e}, bit-exact pixels "
+          f"{np.mean(np.all(got == want, axis=-1)):.4f}")
+    if case == "binary_mega":
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert err <= RMSE_TOL
+
+
+def test_gpu_fp64_reference_matches_the_oracle_fp64_reference(lib):
+    g = np.load(os.path.join(HERE, "golden", "cornell_fp64_4096spp.npz"))
+    size, spp, depth = int(g["size"]), int(g["spp"]), int(g["depth"])
+    s = scenes.path_settings(depth, "wide")
+    s.kernel_approach = 1
+    f2w = scenes.cornell_camera(size, size)
+    scene = scenes.cornell_box()
+    r = api.Renderer()
+    acc = np.zeros((size, size, 3), np.float64)
+    out = np.zeros((size, size, 3), np.float32)
+    n = int(g["ref_spp"]) // 64
+    for f in range(n):
+        r.render(api.ExecutionModel.GPU,
+                 api.SquareImage(size, size, f2w, sample_offset=int(g["sample_offset"]) + 64 * f),
+                 out, scene, 64, s)
+        acc += out
+    acc /= n
+    err = rel_rmse(acc[g["rows"]], g["image"])
+    print(f"GPU FP64 4096-spp reference vs oracle FP64: {err:.2e}")
+    assert err < 1e-5
+    # and the 16-spp image's error against it, as the bench states it
+    r.render(api.ExecutionModel.GPU, api.SquareImage(size, size, f2w), out, scene, spp, s)
+    e16 = rel_rmse(out[g["rows"]], g["image"])
+    assert 0.005 < e16 < 0.05
+
+
+def test_ggx_device_code_equals_the_oracle_and_its_definition(lib, oracle):
+    rng = np.random.default_rng(11)
+    n = 50000
+    for alpha, f0 in ((0.05, 0.04), (0.2, 0.04), (0.6, 0.9)):
+        m = test_ggx.ggx(alpha, f0)
+        rec = np.zeros((n, 9), np.float32)
+        rec[:, 0:6] = rng.normal(size=(n, 6))
+        rec[:, 0:3] /= np.linalg.norm(rec[:, 0:3], axis=1, keepdims=True)
+        rec[:, 3:6] /= np.linalg.norm(rec[:, 3:6], axis=1, keepdims=True)
+        nrm = rng.normal(size=(n, 3))
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+        rec[:, 6:9] = nrm
+        for op in (0, 2):
+            assert np.array_equal(api.debug_bsdf(m, op, rec).view(np.uint32),
+                                  ol.debug_bsdf(m, op, rec).view(np.uint32)), op
+        srec = rec.copy()
+        srec[:, 3:6] = nrm
+        srec[:, 6:9] = rng.random((n, 3))
+        assert np.array_equal(api.debug_bsdf(m, 1, srec).view(np.uint32),
+                              ol.debug_bsdf(m, 1, srec).view(np.uint32))
+
+    def dev_d(r):
+        return api.debug_bsdf(test_ggx.ggx(0.1), 2, r)
+
+    test_ggx.check_normalisation(dev_d)
+    test_ggx.check_weights_match_eval_over_pdf(lambda m, r: api.debug_bsdf(m, 0, r),
+                                               lambda m, r: api.debug_bsdf(m, 1, r), dev_d)
+    test_ggx.check_mean_weight_is_albedo(lambda m, r: api.debug_bsdf(m, 0, r),
+                                         lambda m, r: api.debug_bsdf(m, 1, r))
+
+
+def test_batch_images_match_the_oracle(lib, oracle):
+    batch = scenes.batch_scenes(3, seed=5)
+    s = scenes.path_settings(6, "wide")
+    st = ol.settings_from(scenes.path_settings(6, "binary"), reduce_order=1)
+    items, outs, sizes = [], [], []
+    for k, (sc, _, _, spp) in enumerate(batch):
+        w, h = (32, 24) if k == 1 else (24, 24)
+        spp = min(spp, 8)
+        out = np.zeros((h, w, 3), np.float32)
+        outs.append(out)
+        sizes.append((w, h, spp))
+        items.append((sc, api.SquareImage(w, h, scenes.cornell_camera(w, h)), out, spp))
+    r = api.Renderer()
+    r.render_batch(items, s)
+    assert r.stats()["device_status"] == 0
+    for (sc, _, _, _), out, (w, h, spp) in zip(batch, outs, sizes):
+        want, _ = ol.render(ol.SceneArrays(sc.export()), st, spp, w, h,
+                            scenes.cornell_camera(w, h))
+        err = rel_rmse(out, want)
+        print(f"batch item {sc.sizes()['triangles']} triangles: rel RMSE {err:.2e}")
+        assert err <= RMSE_TOL

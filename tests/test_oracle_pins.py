@@ -250,12 +250,22 @@ def test_pmath_accuracy(oracle):
     assert ol.pmath(3, np.array([1.0], np.float32))[0] == 0.0
     assert ol.pmath(2, np.array([1.0], np.float32))[0] == np.float32(np.pi / 2)
     assert np.isnan(ol.pmath(3, np.array([1.0000001], np.float32))[0])
-    b = rng.uniform(0, 1, 100000).astype(np.float32)
-    e = rng.uniform(0, 60, 100000).astype(np.float32)
+    # pow (evaluated in double precision): within one float ulp of the exact
+    # power, over the bases and exponents the renderer uses (Phong lobes up
+    # to shininess 10^4, their samplers' 1 / (n + 1), MultiplierFunc's 50)
+    b = np.concatenate([rng.uniform(0, 1, 100000), rng.uniform(0, 4, 20000)]).astype(np.float32)
+    e = np.concatenate([rng.uniform(0, 60, 60000), 10.0 ** rng.uniform(-4, 4, 60000)]
+                       ).astype(np.float32)
     got = ol.pmath(4, b, e).astype(np.float64)
-    want = np.power(b.astype(np.float64), e.astype(np.float64))
-    mask = want > 1e-30
-    assert np.max(np.abs(got[mask] - want[mask]) / want[mask]) < 2e-5
+    with np.errstate(over="ignore"):
+        want = np.power(b.astype(np.float64), e.astype(np.float64))
+    ok = (want > 1e-37) & (want < 1e38)
+    ulp = np.spacing(want[ok].astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(got[ok] - want[ok]) / ulp) <= 1.0
+    assert np.all(got[want < 1e-46] == 0) and np.all(np.isinf(got[want > 4e38]))
+    special = ol.pmath(4, np.array([0, 0, 1, 2, 0.5, np.inf, np.inf, 2, 0.5], np.float32),
+                       np.array([2, -1, 7, 0, np.inf, 2, -2, -np.inf, -np.inf], np.float32))
+    assert special.tolist() == [0, np.inf, 1, 1, 0, np.inf, 0, 0, np.inf]
 
 
 def test_sobol_table_is_a_net(oracle):

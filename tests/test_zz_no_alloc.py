@@ -10,9 +10,12 @@ buffer) lives in one fixed device array inside the library.
 These checks call it through the C ABI twice in a row and compare each image
 bit for bit with path_render's on the same scene (the binary traversal is
 bit-exact, the tolerance the parity tests hold it to), with the image written
-straight to the output and with partial sums reduced through the scratch
-array.  The file is named to be collected last so that a run stopping at the
-first failure has already run every other test.
+straight to the output, with partial sums reduced through the scratch array
+and for a progressive frame (a nonzero sample_offset).  Around each call
+after the first, the device's free memory (cudaMemGetInfo) must not change:
+the property the entry point exists for.  The file is named to be collected
+last so that a run stopping at the first failure has already run every other
+test.
 """
 
 import ctypes
@@ -45,7 +48,8 @@ def _sample_block_settings():
     return s
 
 
-@pytest.mark.parametrize("case", ["direct", "sample_blocks", "bgra", "uniform_rng"])
+@pytest.mark.parametrize("case", ["direct", "sample_blocks", "bgra", "uniform_rng",
+                                  "sample_offset"])
 def test_noalloc_matches_path_render_twice(lib, case):
     torch = pytest.importorskip("torch")
     scene = scenes.cornell_box()
@@ -55,7 +59,8 @@ def test_noalloc_matches_path_render_twice(lib, case):
         scenes.path_settings(5, "binary")
     if case == "uniform_rng":
         settings.rng = 1
-    spec = api.SquareImage(w, h, scenes.cornell_camera(w, h))
+    offset = 48 if case == "sample_offset" else 0
+    spec = api.SquareImage(w, h, scenes.cornell_camera(w, h), sample_offset=offset)
     r = api.Renderer()
     if case == "bgra":
         ref = torch.zeros((h, w, 4), dtype=torch.uint8, device="cuda")
@@ -64,10 +69,25 @@ def test_noalloc_matches_path_render_twice(lib, case):
     r.render(api.ExecutionModel.GPU, spec, ref, scene, spp, settings)
     torch.cuda.synchronize()
     expect = ref.cpu().numpy()
-    for _ in range(2):
-        out = torch.full_like(ref, 7)
+    if offset:
+        # a frame of later samples is a different image
+        r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, spec.film_to_world), ref, scene,
+                 spp, settings)
+        assert not np.array_equal(ref.cpu().numpy(), expect)
+    outs = [torch.full_like(ref, 7) for _ in range(3)]
+    torch.cuda.synchronize()
+    free_after_first = None
+    for k, out in enumerate(outs):
+        free_before = torch.cuda.mem_get_info()[0]
         capi.check(_noalloc(r, spec, out, scene, spp, settings))
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+        if k == 0:
+            free_after_first = free_after
+        else:
+            # the first call on a device may load the library's module (and
+            # with it the scratch array); later calls allocate nothing
+            assert free_after == free_before == free_after_first
         got = out.cpu().numpy()
         assert np.array_equal(got.view(np.uint8), expect.view(np.uint8))
         assert r.stats()["device_status"] == 0
