@@ -781,6 +781,8 @@ def main():
                 "rel_rmse": float(np.linalg.norm(timed_img[fsel] - o64) / np.linalg.norm(o64)),
                 "gpu_reference_vs_oracle_reference": float(np.linalg.norm(g[fsel] - o64) /
                                                            np.linalg.norm(o64)),
+                "gpu_reference_same_rows": float(np.linalg.norm(timed_img[fsel] - g[fsel]) /
+                                                 np.linalg.norm(g[fsel])),
                 "rows": f"{len(fsel)} rows (1 in {stride} from row {start})",
                 "reference": "4096 spp (samples spp..spp+4095), every sample summed in FP64 "
                              "by the CPU oracle",

@@ -779,7 +779,12 @@ BVH build_bvh(const std::vector<Tri> &in, float overlap_threshold,
 
 // include/intersect/accel/detail/bvh/bvh_impl.h:12-89 (stack of 64 nodes,
 // candidate batch of up to 10 triangles)
-Hit bvh_intersect(const BVH &bvh, const Ray &ray) {
+// order_independent: the closest hit of the GPU's 8-wide traversal instead
+// of the reference's tie rule -- at equal distance the smallest BVH-order
+// index wins, and a box is pruned only when the best distance is strictly
+// below its entry distance, so that no equal-distance candidate is skipped.
+// Results then do not depend on the order nodes are visited in.
+Hit bvh_intersect(const BVH &bvh, const Ray &ray, bool order_independent = false) {
   Hit best;
   if (bvh.nodes.empty()) {
     return best;
@@ -795,7 +800,7 @@ Hit bvh_intersect(const BVH &bvh, const Ray &ray) {
       const Node &node = bvh.nodes[stack[--sp]];
       float tmin, tmax;
       if (node.aabb.solve(ray.o, inv, &tmin, &tmax) &&
-          (!best.ok || best.t > tmin)) {
+          (!best.ok || best.t > tmin || (order_independent && best.t == tmin))) {
         if (node.is_split()) {
           stack[sp++] = node.second();
           stack[sp++] = node.first();
@@ -812,7 +817,11 @@ Hit bvh_intersect(const BVH &bvh, const Ray &ray) {
     for (unsigned k = 0; k < n_obj; ++k) {
       Hit h = tri_intersect(bvh.tris[objects[k]], ray);
       h.idx = objects[k];
-      fold_min(best, h);
+      if (!order_independent) {
+        fold_min(best, h);
+      } else if (h.ok && (!best.ok || h.t < best.t || (h.t == best.t && h.idx < best.idx))) {
+        best = h;
+      }
     }
     n_obj = 0;
   }
@@ -1489,7 +1498,7 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
     // intersect all pending rays (light ray first, then the next ray)
     Hit light_hit, next_hit;
     if (has_light) {
-      light_hit = bvh_intersect(*c.bvh, light_ray);
+      light_hit = bvh_intersect(*c.bvh, light_ray, st.tie_rule != 0);
     }
     if (has_next) {
       if (step == 0 && c.idxs != nullptr) {
@@ -1499,7 +1508,7 @@ RGB integrate_sample(const RenderCtx &c, unsigned sample_idx, unsigned x,
         next_hit.back = false;
         next_hit.idx = c.idxs[x];
       } else {
-        next_hit = bvh_intersect(*c.bvh, ray);
+        next_hit = bvh_intersect(*c.bvh, ray, st.tie_rule != 0);
       }
     }
     if (has_light) {

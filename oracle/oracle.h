@@ -103,6 +103,10 @@ typedef struct {
   uint32_t reduce_order; /* 0: CPU lane order, 1: GPU shuffle-tree order */
   uint32_t n_threads;    /* OpenMP threads, 0 = default */
   uint32_t rng;          /* 0 Sobel, 1 Uniform (std::mt19937) */
+  uint32_t tie_rule;     /* closest hit at equal distance: 0 the reference's
+                            (a later candidate wins, optional_min.h), 1 the
+                            GPU 8-wide traversal's (smallest BVH-order index,
+                            independent of the visit order) */
 } oracle_settings;
 
 typedef struct {

@@ -60,7 +60,7 @@ class OracleSettings(ctypes.Structure):
                 ("term_prob_prob", c_f32), ("term_prob_iters", c_u32), ("term_prob_exp", c_f32),
                 ("term_prob_min_prob", c_f32), ("max_sample_size", c_u32),
                 ("back_cull_emission", c_u32), ("reduce_order", c_u32), ("n_threads", c_u32),
-                ("rng", c_u32)]
+                ("rng", c_u32), ("tie_rule", c_u32)]
 
 
 class RenderOptions(ctypes.Structure):
@@ -328,8 +328,10 @@ def sobol_table(dimension_bound, count):
     return out.reshape(count, dimension_bound)
 
 
-def settings_from(s, reduce_order=1, n_threads=0):
-    """Oracle settings from a path_gb300 api.Settings (same field meaning)."""
+def settings_from(s, reduce_order=1, n_threads=0, tie_rule=0):
+    """Oracle settings from a path_gb300 api.Settings (same field meaning);
+    tie_rule 1 takes the 8-wide traversal's closest hit at equal distance
+    (smallest BVH-order index) instead of the reference's."""
     r = s.raw
     w = lambda x: WD(x.block_size, x.target_x_block_size, x.force_target_samples,  # noqa: E731
                      x.forced_target_samples_per_thread, x.base_num_threads,
@@ -339,10 +341,10 @@ def settings_from(s, reduce_order=1, n_threads=0):
                           r.traversal_per_intersect_cost, r.target_objects, r.light_sampler,
                           r.dir_sampler, r.term_prob, r.term_prob_prob, r.term_prob_iters,
                           r.term_prob_exp, r.term_prob_min_prob, r.max_sample_size,
-                          r.back_cull_emission, reduce_order, n_threads, r.rng)
+                          r.back_cull_emission, reduce_order, n_threads, r.rng, tie_rule)
 
 
-def workload_settings(max_depth, reduce_order=0, n_threads=0):
+def workload_settings(max_depth, reduce_order=0, n_threads=0, tie_rule=0):
     """Oracle settings for 'max depth D, no Russian roulette, Sobol' without
     the library: render::Settings{} defaults (include/render/settings.h
     :27-45 -- WorkDivision {256, 32, no forcing, 8, 16384, 0.5, 32}, reducer
@@ -352,7 +354,7 @@ def workload_settings(max_depth, reduce_order=0, n_threads=0):
     culled emission."""
     return OracleSettings(WD(256, 32, 0, 8, 16384, 0.5, 32), WD(256, 256, 0, 8, 16384, 0.5, 32),
                           128, 1e-5, 0, 0.5, 4, 0, 0, 1, 0.5, max_depth - 1, 50.0, 0.1, 256, 1,
-                          reduce_order, n_threads, 0)
+                          reduce_order, n_threads, 0, tie_rule)
 
 
 class SceneArrays:

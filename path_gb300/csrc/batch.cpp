@@ -297,6 +297,12 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
   PG_TRY_CUDA(b_wtris_.upload(h_wtris.data(), h_wtris.size() * 4, stream_), "batch upload");
   PG_TRY_CUDA(b_tris_.upload(h_tris.data(), h_tris.size() * 4, stream_), "batch upload");
   PG_TRY_CUDA(b_data_.upload(h_data.data(), h_data.size() * 4, stream_), "batch upload");
+  b_mat_types_ = 0;
+  for (const BatchItem &it : items) {
+    for (const path_material &m : it.scene->materials) {
+      b_mat_types_ |= 1u << (m.type & 31u);
+    }
+  }
   PG_TRY_CUDA(b_mats_.upload(h_mats.data(), h_mats.size() * sizeof(DevMaterial), stream_),
               "batch upload");
   PG_TRY_CUDA(b_lights_.upload(h_lights.data(), h_lights.size() * 4, stream_), "batch upload");
@@ -464,6 +470,7 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   }
   w.scenes = b_scenes_.as<const BatchScene>();
   w.n_scenes = (uint32_t)n;
+  w.feat = work_features(b_mat_types_, p);
 
   uint32_t *h = wf_host_.as<uint32_t>();
   std::memset(h, 0, 64);

@@ -62,6 +62,30 @@ constexpr uint32_t kMaxNodeTris = 32;     // 5-bit offset in meta
 // node groups a wide traversal keeps waiting: at most one per tree level
 constexpr uint32_t kWideStackDepth = 64;
 
+// Feature set of a path kernel, a template parameter: bit t allows BSDF
+// type t (0 Diffuse, 1 Glossy, 2 DiffuseGlossy, 3 DiffuseMirror, 4 Mirror,
+// 5 DielectricRefractive, 6 GGX), and the flag bits fix termination to
+// NIters, direction sampling to the BSDF sampler and light sampling to
+// RandomTriangle.  A kernel specialised to a scene's features carries none
+// of the other code (the shade kernel's largest stall is instruction
+// fetch); the host only launches a specialisation whose feature set covers
+// the scene and the settings.
+constexpr uint32_t kFeatAllMats = 0x7fu;
+constexpr uint32_t kFeatNIters = 1u << 8;
+constexpr uint32_t kFeatBsdfDir = 1u << 9;
+constexpr uint32_t kFeatLightTri = 1u << 10;
+constexpr uint32_t kFeatAll = kFeatAllMats; // every choice made at run time
+// Diffuse, GGX and dielectric materials under NIters, the BSDF sampler and
+// RandomTriangle: the large-mesh, batched and Cornell workloads
+constexpr uint32_t kFeatPlain = (1u << 0) | (1u << 5) | (1u << 6) | kFeatNIters |
+                                kFeatBsdfDir | kFeatLightTri;
+// whether a kernel compiled for `kernel` may run work whose features are
+// `need` (the material types it shades and the fixed choices it assumes)
+inline constexpr bool feat_covers(uint32_t kernel, uint32_t need) {
+  return (need & kFeatAllMats & ~kernel) == 0 &&
+         (kernel & ~kFeatAllMats & ~need) == 0;
+}
+
 // device status word codes (first error wins)
 enum DeviceStatus : uint32_t {
   kStatusOk = 0,

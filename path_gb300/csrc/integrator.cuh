@@ -704,8 +704,15 @@ enum : uint32_t {
   kGGX = 6,
 };
 
+// Compile-time feature set of a path kernel (kFeat* in devtypes.h): the
+// cases of BSDF types outside F compile to nothing.
+template <uint32_t F, uint32_t T> __device__ __forceinline__ constexpr bool has_mat() {
+  return ((F >> T) & 1u) != 0;
+}
+
 __device__ __forceinline__ bool is_brdf(const Mat &m) { return m.type != kDielectric; }
 
+template <uint32_t F = kFeatAll>
 __device__ __forceinline__ float prob_continuous(const Mat &m) {
   switch (m.type) {
   case kDiffuse:
@@ -717,7 +724,7 @@ __device__ __forceinline__ float prob_continuous(const Mat &m) {
   case kDielectric:
     return 0.0f;
   default:
-    return m.w_d;
+    return has_mat<F, kDiffuseMirror>() ? m.w_d : 1.0f;
   }
 }
 
@@ -817,24 +824,40 @@ __device__ bool bsdf_log_grad(const Mat &m, f3 in, f3 out, f3 n, rgb &refl, floa
   return true;
 }
 
+template <uint32_t F = kFeatAll>
 __device__ rgb continuous_eval(const Mat &m, f3 in, f3 out, f3 n) {
   switch (m.type) {
   case kDiffuse:
-    return m.diffuse * kInvPi;
+    if constexpr (has_mat<F, kDiffuse>()) {
+      return m.diffuse * kInvPi;
+    }
+    break;
   case kGlossy:
-    return glossy_eval(m, in, out, n);
-  case kDiffuseGlossy: {
-    float w0 = m.cont_inclusive0 - 0.f;
-    float w1 = 1.f - m.cont_inclusive0;
-    return (m.diffuse * kInvPi) * w0 + glossy_eval(m, in, out, n) * w1;
-  }
+    if constexpr (has_mat<F, kGlossy>()) {
+      return glossy_eval(m, in, out, n);
+    }
+    break;
+  case kDiffuseGlossy:
+    if constexpr (has_mat<F, kDiffuseGlossy>()) {
+      float w0 = m.cont_inclusive0 - 0.f;
+      float w1 = 1.f - m.cont_inclusive0;
+      return (m.diffuse * kInvPi) * w0 + glossy_eval(m, in, out, n) * w1;
+    }
+    break;
   case kDiffuseMirror:
-    return (m.diffuse * kInvPi) * (1.f - 0.f);
+    if constexpr (has_mat<F, kDiffuseMirror>()) {
+      return (m.diffuse * kInvPi) * (1.f - 0.f);
+    }
+    break;
   case kGGX:
-    return ggx_eval(m, in, out, n);
+    if constexpr (has_mat<F, kGGX>()) {
+      return ggx_eval(m, in, out, n);
+    }
+    break;
   default:
-    return zero_rgb();
+    break;
   }
+  return zero_rgb();
 }
 
 struct Sample {
@@ -915,47 +938,68 @@ __device__ Sample ggx_sample(const Mat &m, f3 in, f3 n, R &rng) {
   return s;
 }
 
-template <class R>
+template <uint32_t F = kFeatAll, class R>
 __device__ Sample continuous_sample(const Mat &m, f3 in, f3 n, R &rng) {
   switch (m.type) {
   case kDiffuse:
-    return diffuse_sample(m.diffuse, in, n, rng);
-  case kGlossy:
-    return glossy_sample(m, in, n, rng);
-  case kDiffuseGlossy: {
-    float loc = rng.next();
-    if (loc <= m.cont_inclusive0) {
+    if constexpr (has_mat<F, kDiffuse>()) {
       return diffuse_sample(m.diffuse, in, n, rng);
     }
-    return glossy_sample(m, in, n, rng);
-  }
+    break;
+  case kGlossy:
+    if constexpr (has_mat<F, kGlossy>()) {
+      return glossy_sample(m, in, n, rng);
+    }
+    break;
+  case kDiffuseGlossy:
+    if constexpr (has_mat<F, kDiffuseGlossy>()) {
+      float loc = rng.next();
+      if (loc <= m.cont_inclusive0) {
+        return diffuse_sample(m.diffuse, in, n, rng);
+      }
+      return glossy_sample(m, in, n, rng);
+    }
+    break;
   case kDiffuseMirror:
-    (void)rng.next();
-    return diffuse_sample(m.diffuse, in, n, rng);
+    if constexpr (has_mat<F, kDiffuseMirror>()) {
+      (void)rng.next();
+      return diffuse_sample(m.diffuse, in, n, rng);
+    }
+    break;
   case kGGX:
-    return ggx_sample(m, in, n, rng);
-  default: {
-    Sample s;
-    s.dir = in;
-    s.mult = zero_rgb();
-    return s;
+    if constexpr (has_mat<F, kGGX>()) {
+      return ggx_sample(m, in, n, rng);
+    }
+    break;
+  default:
+    break;
   }
-  }
+  Sample s;
+  s.dir = in;
+  s.mult = zero_rgb();
+  return s;
 }
 
-template <class R>
+template <uint32_t F = kFeatAll, class R>
 __device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, R &rng) {
   Sample s;
   s.mult = m.specular;
   switch (m.type) {
   case kMirror:
-    s.dir = reflect(in, n);
-    return s;
+    if constexpr (has_mat<F, kMirror>()) {
+      s.dir = reflect(in, n);
+      return s;
+    }
+    break;
   case kDiffuseMirror:
-    (void)rng.next();
-    s.dir = reflect(in, n);
-    return s;
-  case kDielectric: {
+    if constexpr (has_mat<F, kDiffuseMirror>()) {
+      (void)rng.next();
+      s.dir = reflect(in, n);
+      return s;
+    }
+    break;
+  case kDielectric:
+    if constexpr (has_mat<F, kDielectric>()) {
     float c = pm::fabs(dot(in, n));
     double x = (double)(1.f - c);
     double x2 = x * x;
@@ -967,12 +1011,14 @@ __device__ Sample discrete_sample(const Mat &m, f3 in, f3 n, R &rng) {
       s.dir = refract(m.ior, in, n);
     }
     return s;
-  }
+    }
+    break;
   default:
-    s.dir = in;
-    s.mult = zero_rgb();
-    return s;
+    break;
   }
+  s.dir = in;
+  s.mult = zero_rgb();
+  return s;
 }
 
 template <class R>
@@ -1060,8 +1106,12 @@ __device__ bool sample_light(const LightSet &L, f3 pos, const Mat &m, f3 normal,
 }
 
 // include/integrate/term_prob/*
+template <uint32_t F = kFeatAll>
 __device__ __forceinline__ float term_prob(const RenderParams &P, uint32_t iters,
                                            rgb mult) {
+  if constexpr ((F & kFeatNIters) != 0) {
+    return iters >= P.term_iters ? 1.0f : 0.0f;
+  }
   switch (P.term_prob) {
   case 0:
     return P.term_prob_prob;
@@ -1223,12 +1273,12 @@ __device__ __forceinline__ rgb albedo_of(const Mat &m) {
   }
 }
 
-template <bool kUniform>
+template <bool kUniform, uint32_t F = kFeatAll>
 __device__ __forceinline__ bool path_step(const RenderParams &P, const LightSet &L,
                                        PathStateT<kUniform> &s,
                                        const Hit &lh, const Hit &nh,
                                        StepTrace *tr = nullptr) {
-  const bool performs_samples = P.light_sampler == 0;
+  const bool performs_samples = (F & kFeatLightTri) != 0 || P.light_sampler == 0;
   const bool cull = P.back_cull != 0;
   if (tr != nullptr) {
     tr->light_added = tr->emit_added = tr->hit = tr->nee = tr->continuous = false;
@@ -1276,11 +1326,11 @@ __device__ __forceinline__ bool path_step(const RenderParams &P, const LightSet 
   rgb new_light_mult = zero_rgb();
   float new_light_target = 0.f;
   f3 new_ld = s.ld;
-  float pc = prob_continuous(mat);
+  float pc = prob_continuous<F>(mat);
   if (pc > 0.f && performs_samples) {
     LightSample ls;
     if (sample_light(L, point, mat, normal, s.rng, ls)) {
-      rgb f = continuous_eval(mat, s.d, ls.dir, normal);
+      rgb f = continuous_eval<F>(mat, s.d, ls.dir, normal);
       new_light_mult = ((s.multiplier * f) * pc) / ls.mult;
       new_light_target = ls.target;
       new_ld = ls.dir;
@@ -1301,9 +1351,9 @@ __device__ __forceinline__ bool path_step(const RenderParams &P, const LightSet 
   }
   Sample smp;
   if (take_discrete) {
-    smp = discrete_sample(mat, s.d, normal, s.rng);
-  } else if (P.dir_sampler == 0) {
-    smp = continuous_sample(mat, s.d, normal, s.rng);
+    smp = discrete_sample<F>(mat, s.d, normal, s.rng);
+  } else if ((F & kFeatBsdfDir) != 0 || P.dir_sampler == 0) {
+    smp = continuous_sample<F>(mat, s.d, normal, s.rng);
   } else {
     smp = uniform_dir_sample(mat, s.d, normal, s.rng);
   }
@@ -1312,7 +1362,7 @@ __device__ __forceinline__ bool path_step(const RenderParams &P, const LightSet 
     tr->next_dir = smp.dir;
   }
   rgb new_multiplier = s.multiplier * smp.mult;
-  float p = term_prob(P, s.iters, new_multiplier);
+  float p = term_prob<F>(P, s.iters, new_multiplier);
   bool next = s.rng.next() > p;
   s.iters += 1;
   s.count_emission = take_discrete;

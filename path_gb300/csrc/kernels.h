@@ -121,7 +121,18 @@ struct WaveParams {
   float *cache_beta;
   // Uniform RNG: the XORWOW state words of slot i at rng_state[k * n_slots + i]
   uint32_t *rng_state;
+  // features of the work (kFeat* in devtypes.h: the BSDF types of the
+  // scenes' materials and the fixed setting choices), for the choice of a
+  // specialised shade kernel
+  uint32_t feat;
 };
+
+// the features (kFeat*) of rendering a scene whose materials have the BSDF
+// types mat_types (bit per type) with the settings in p
+inline uint32_t work_features(uint32_t mat_types, const RenderParams &p) {
+  return (mat_types & kFeatAllMats) | (p.term_prob == 1 ? kFeatNIters : 0u) |
+         (p.dir_sampler == 0 ? kFeatBsdfDir : 0u) | (p.light_sampler == 0 ? kFeatLightTri : 0u);
+}
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
 // resident blocks per SM of the trace kernel compiled for min_blocks

@@ -327,8 +327,10 @@ Status Renderer::prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t 
 // materials and the light table (which depends on emission) into staging
 void Renderer::stage_materials(const FlatScene &flat, const std::vector<path_material> &mats) {
   DevMaterial *dm = st_mats_.as<DevMaterial>();
+  mat_types_ = 0;
   for (size_t i = 0; i < mats.size(); ++i) {
     dm[i] = to_dev(mats[i]);
+    mat_types_ |= 1u << (mats[i].type & 31u);
   }
   float *lt = st_lights_.as<float>();
   for (size_t i = 0; i < flat.light_v0.size(); ++i) {
@@ -909,6 +911,7 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   w.total_samples = first + total;
   w.sample_rgb = wf_samples_.as<float>();
   w.n_slots = n_slots;
+  w.feat = work_features(mat_types_, p);
   if (p.cache_depth != 0 && cache_ != nullptr) {
     if (total >= (1ull << 32)) {
       return Status::err(PATH_ERR_UNSUPPORTED, "more than 2^32 samples with the cache");

@@ -186,6 +186,8 @@ private:
                        const AdjointState *adj = nullptr);
   RenderParams last_params_{};
   uint32_t slots_log2_ = 21; // paths in flight of the streaming render, log2
+  uint32_t mat_types_ = kFeatAllMats; // BSDF types of the resident scene (bit per type)
+  uint32_t b_mat_types_ = kFeatAllMats; // ... of the resident batch
   class RadianceCache *cache_ = nullptr; // set during a cached render
   uint32_t cache_depth_ = 0;
   uint32_t frame_counter_ = 0;

@@ -312,7 +312,7 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // which measured faster than fewer warps without register spills.  kCache
 // (paths end into the radiance cache) is a template parameter so that the
 // plain kernel carries none of the cache-query code.
-template <bool kGrad, bool kUniform, bool kCache>
+template <bool kGrad, bool kUniform, bool kCache, uint32_t kFeat = kFeatAll>
 __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_t parity) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t count = W.q->active[parity];
@@ -344,8 +344,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
       if (!kGrad) {
         StepTrace tr;
         StepTrace *trp = kCache ? &tr : nullptr;
-        bool cont =
-            path_continues(W.P, s, path_step(W.P, scene_lights(W, scene), s, lh, nh, trp));
+        bool cont = path_continues(
+            W.P, s, path_step<kUniform, kFeat>(W.P, scene_lights(W, scene), s, lh, nh, trp));
         if (trp != nullptr && tr.cache_query) {
           // the path ends into the radiance cache: its query and throughput
           const size_t k = (size_t)(id - W.first_sample);
@@ -573,6 +573,8 @@ cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_
     }
   } else if (u) {
     dev::k_wf_shade<false, true, false><<<shade_grid, 256, 0, s>>>(w, parity);
+  } else if (feat_covers(kFeatPlain, w.feat)) {
+    dev::k_wf_shade<false, false, false, kFeatPlain><<<shade_grid, 256, 0, s>>>(w, parity);
   } else {
     dev::k_wf_shade<false, false, false><<<shade_grid, 256, 0, s>>>(w, parity);
   }

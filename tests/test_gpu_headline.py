@@ -18,7 +18,10 @@ CPU oracle (GPU tests).
   bit on random records, and passes the same checks against Walter et al.
   2007 as the oracle (tests/test_ggx.py).
 * Batched render against the oracle: each image of a three-scene batch
-  within 1e-4 relative RMSE of the oracle's render of its scene.
+  equals, bit for bit, the oracle's render of its scene under the 8-wide
+  traversal's tie rule (smallest BVH-order index at equal distance); under
+  the reference's tie rule only the paths that met an exact tie differ
+  (fewer than 0.5% of the samples).
 """
 
 import os
@@ -132,9 +135,14 @@ def test_ggx_device_code_equals_the_oracle_and_its_definition(lib, oracle):
 
 
 def test_batch_images_match_the_oracle(lib, oracle):
+    # The batch renders through the 8-wide BVH, whose closest hit at equal
+    # distance is the smallest BVH-order triangle (order-independent); the
+    # oracle with that tie rule must give the same image bit for bit.  With
+    # the reference's tie rule (a later candidate wins) the images differ
+    # only in the paths that met an exact tie -- on the tessellated spheres,
+    # rays through a shared edge -- which the test counts.
     batch = scenes.batch_scenes(3, seed=5)
     s = scenes.path_settings(6, "wide")
-    st = ol.settings_from(scenes.path_settings(6, "binary"), reduce_order=1)
     items, outs, sizes = [], [], []
     for k, (sc, _, _, spp) in enumerate(batch):
         w, h = (32, 24) if k == 1 else (24, 24)
@@ -147,8 +155,18 @@ def test_batch_images_match_the_oracle(lib, oracle):
     r.render_batch(items, s)
     assert r.stats()["device_status"] == 0
     for (sc, _, _, _), out, (w, h, spp) in zip(batch, outs, sizes):
-        want, _ = ol.render(ol.SceneArrays(sc.export()), st, spp, w, h,
-                            scenes.cornell_camera(w, h))
-        err = rel_rmse(out, want)
-        print(f"batch item {sc.sizes()['triangles']} triangles: rel RMSE {err:.2e}")
-        assert err <= RMSE_TOL
+        f2w = scenes.cornell_camera(w, h)
+        st_ref = ol.settings_from(scenes.path_settings(6, "binary"), reduce_order=1)
+        st_wide = ol.settings_from(scenes.path_settings(6, "binary"), reduce_order=1, tie_rule=1)
+        prep = ol.Prepared(ol.SceneArrays(sc.export()), st_ref)
+        want, _ = prep.render(st_wide, spp, w, h, f2w)
+        ref, _ = prep.render(st_ref, spp, w, h, f2w)
+        a = prep.sample_values(st_ref, spp, w, h, f2w)
+        b = prep.sample_values(st_wide, spp, w, h, f2w)
+        tied = int(np.sum(np.any(a != b, axis=-1)))
+        print(f"batch item {sc.sizes()['triangles']} triangles: bit-exact under the wide tie "
+              f"rule {np.array_equal(out, want)}; vs the reference tie rule rel RMSE "
+              f"{rel_rmse(out, ref):.2e}, {tied} of {a.shape[0] * a.shape[1] * a.shape[2]} "
+              "samples changed by ties")
+        assert np.array_equal(out.view(np.uint32), want.view(np.uint32))
+        assert tied <= 0.005 * a.shape[0] * a.shape[1] * a.shape[2]
