@@ -527,6 +527,9 @@ def main():
                     help="build the 8-wide BVH on the GPU (linear BVH) instead of the SBVH")
     ap.add_argument("--trace-min-blocks", type=int, default=0,
                     help="streaming trace kernel variant (resident blocks per SM, 3..6)")
+    ap.add_argument("--staged-nodes", type=int, default=None,
+                    help="streaming trace: top BVH nodes staged in shared memory per CTA "
+                         "(default: the library's)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -557,6 +560,8 @@ def main():
     settings.trace_min_blocks = args.trace_min_blocks
     settings.gpu_build = 1 if args.gpu_build else 0
     settings.wavefront_slots_log2 = args.slots_log2
+    if args.staged_nodes is not None:
+        settings.trace_staged_nodes = args.staged_nodes
     f2w = scenes.cornell_camera(w, h)
     spec = api.SquareImage(w, h, f2w)
     r = api.Renderer()
@@ -645,7 +650,8 @@ def main():
     launch_s = kern_ms / launches_per_render / 1e3
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     shape = (f"slots_log2={args.slots_log2 or 26} trace_min_blocks={args.trace_min_blocks or 4} "
-             f"bvh={'gpu' if args.gpu_build else 'sbvh'}")
+             f"bvh={'gpu' if args.gpu_build else 'sbvh'} "
+             f"staged_nodes={settings.trace_staged_nodes}")
     full_size = args.size is None and args.spp is None
     traffic = _profiled_traffic(kernel_name, args, shape) if full_size else None
     issue = _profiled_issue(kernel_name, args, shape) if full_size and streaming else None
@@ -692,6 +698,7 @@ def main():
             "max_depth": depth, "traversal": args.traversal, "approach": args.approach,
             "trace_min_blocks": args.trace_min_blocks or 4,
             "slots_log2": args.slots_log2 or 26,
+            "staged_nodes": int(settings.trace_staged_nodes),
             "bvh": "GPU linear BVH collapsed to 8-wide" if args.gpu_build else
                    "SBVH (host) collapsed to 8-wide",
             "l2": "flushed (512 MB write) before every timed step",

@@ -141,6 +141,9 @@ typedef struct {
                                 wide traversal only, no binary SBVH */
   uint32_t wavefront_slots_log2; /* streaming: paths in flight = 2^this
                                     (10..26, 0 = default 26) */
+  uint32_t trace_staged_nodes; /* streaming trace kernel: the top nodes of the
+                                  8-wide BVH (breadth-first, at most 512)
+                                  each CTA keeps in shared memory; 0 = none */
 } path_settings;
 
 typedef enum {
@@ -429,6 +432,14 @@ path_status path_sobol_table_curand(uint32_t dimension_bound, uint32_t count,
  * fn 0 sin, 1 cos, 2 asin, 3 acos, 4 pow(x, y); host arrays of n */
 path_status path_debug_pmath(uint32_t fn, const float *x, const float *y,
                              float *out, uint32_t n);
+/* Fault injection for the out-of-memory paths (GB300 addition; the
+ * reference exits on a CUDA error, include/lib/cuda/utils.h:18-26): once the
+ * device memory the library's renderers hold would exceed `bytes`, further
+ * device allocations fail as a full device makes them fail, and the call
+ * that needed them returns PATH_ERR_OOM with its message; the renderer stays
+ * usable.  0 removes the cap.  Process-wide; for tests. */
+void path_debug_set_device_alloc_cap(uint64_t bytes);
+
 /* evaluates the kernels' BSDF code on the GPU for one material (GB300
  * addition, for tests): n records of 9 floats in `in` (host arrays);
  *   op 0: continuous_eval (bsdf::BSDF::continuous_eval, include/bsdf/bsdf.h

@@ -43,7 +43,8 @@ class PathSettings(ctypes.Structure):
                 ("back_cull_emission", c_u32), ("traversal", c_u32),
                 ("persistent_ctas_per_sm", c_u32), ("count_work", c_u32),
                 ("upload_scene_every_render", c_u32), ("trace_min_blocks", c_u32),
-                ("time_kernels", c_u32), ("gpu_build", c_u32), ("wavefront_slots_log2", c_u32)]
+                ("time_kernels", c_u32), ("gpu_build", c_u32), ("wavefront_slots_log2", c_u32),
+                ("trace_staged_nodes", c_u32)]
 
 
 class SampleSpec(ctypes.Structure):
@@ -127,6 +128,7 @@ SIGNATURES = {
     "path_sobol_table_curand": (ctypes.c_int, [c_u32, c_u32, _PF]),
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_debug_bsdf": (ctypes.c_int, [ctypes.POINTER(PathMaterial), c_u32, _PF, c_u32, _PF]),
+    "path_debug_set_device_alloc_cap": (None, [ctypes.c_uint64]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),
     "path_cache_create": (ctypes.c_int, [c_u32, c_f32, ctypes.POINTER(_P)]),

@@ -481,7 +481,7 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   const bool counting = st.count_work != 0;
   const uint32_t trace_grid =
       (uint32_t)num_sms_ *
-      (uint32_t)wavefront_trace_blocks_per_sm(tu.trace_min_blocks, counting);
+      (uint32_t)wavefront_trace_blocks_per_sm(tu.trace_min_blocks, counting, 0);
   const uint32_t shade_grid = (uint32_t)num_sms_ * tu.shade_ctas_per_sm;
   const uint32_t k_iters = tu.iterations_per_graph + (tu.iterations_per_graph & 1u);
 

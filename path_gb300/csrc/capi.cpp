@@ -667,6 +667,8 @@ path_status path_debug_pmath(uint32_t fn, const float *x, const float *y, float 
   });
 }
 
+void path_debug_set_device_alloc_cap(uint64_t bytes) { pg::set_device_alloc_cap(bytes); }
+
 path_status path_debug_bsdf(const path_material *material, uint32_t op, const float *in,
                             uint32_t n, float *out) {
   if (!material || !in || !out || op > 2 || material->type > PATH_BSDF_GGX) {

@@ -61,6 +61,8 @@ constexpr uint32_t kMaxLeafTris = 7;      // 3-bit count in meta
 constexpr uint32_t kMaxNodeTris = 32;     // 5-bit offset in meta
 // node groups a wide traversal keeps waiting: at most one per tree level
 constexpr uint32_t kWideStackDepth = 64;
+// most top nodes the streaming trace kernel stages in shared memory (40 KB)
+constexpr uint32_t kMaxStagedNodes = 512;
 
 // Feature set of a path kernel, a template parameter: bit t allows BSDF
 // type t (0 Diffuse, 1 Glossy, 2 DiffuseGlossy, 3 DiffuseMirror, 4 Mirror,

@@ -283,10 +283,13 @@ __device__ __forceinline__ bool shadow_settled(const WideWalk &w) {
 // current group (the rest of the old group waits on the stack), or a group
 // is taken from the stack, or the walk ends (w.done) once the returned
 // triangles are tested.
-template <bool kCount>
+// kStaged: nodes below n_top are read from `top`, the caller's shared-memory
+// copy of the BVH's first nodes (one generic load serves both copies).
+template <bool kCount, bool kStaged = false>
 __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
                                           uint32_t *st_base, uint32_t *st_bits, Counts &cnt,
-                                          uint32_t &tri_base, uint32_t &tmask) {
+                                          uint32_t &tri_base, uint32_t &tmask,
+                                          const uint4 *top = nullptr, uint32_t n_top = 0) {
   tmask = 0;
   tri_base = 0;
   const uint32_t j = __ffs(w.ng_bits >> 8) - 1;
@@ -304,12 +307,22 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
     st_bits[w.sp] = w.ng_bits;
     ++w.sp;
   }
-  const uint4 *np = P.wide_nodes + 5 * (size_t)node;
-  const uint4 n0 = __ldg(np);
-  const uint4 n1 = __ldg(np + 1);
-  const uint4 n2 = __ldg(np + 2);
-  const uint4 n3 = __ldg(np + 3);
-  const uint4 n4 = __ldg(np + 4);
+  uint4 n0, n1, n2, n3, n4;
+  if constexpr (kStaged) {
+    const uint4 *np = node < n_top ? top + 5 * node : P.wide_nodes + 5 * (size_t)node;
+    n0 = np[0];
+    n1 = np[1];
+    n2 = np[2];
+    n3 = np[3];
+    n4 = np[4];
+  } else {
+    const uint4 *np = P.wide_nodes + 5 * (size_t)node;
+    n0 = __ldg(np);
+    n1 = __ldg(np + 1);
+    n2 = __ldg(np + 2);
+    n3 = __ldg(np + 3);
+    n4 = __ldg(np + 4);
+  }
   if (kCount) {
     ++cnt.nodes;
   }

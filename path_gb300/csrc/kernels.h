@@ -56,6 +56,9 @@ struct RenderParams {
   uint32_t cache_depth;
   // Uniform RNG (cuRAND XORWOW per path) instead of the Sobol table
   uint32_t rng_uniform;
+  // streaming trace: wide nodes [0, n_staged) (the breadth-first top of the
+  // BVH) are read from a copy in shared memory
+  uint32_t n_staged;
 };
 
 enum Traversal : uint32_t { kTravBinary = 0, kTravWide = 1 };
@@ -136,7 +139,7 @@ inline uint32_t work_features(uint32_t mat_types, const RenderParams &p) {
 
 cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t s);
 // resident blocks per SM of the trace kernel compiled for min_blocks
-int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting);
+int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting, uint32_t n_staged);
 // one wavefront iteration: trace the queued rays, then reset the queues
 // and shade (launch_wavefront_shade)
 cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,

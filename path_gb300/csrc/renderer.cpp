@@ -5,11 +5,21 @@
 
 #include <curand.h>
 
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 
 namespace pg {
+
+namespace {
+// allocation cap for fault injection (path_debug_set_device_alloc_cap): the
+// bytes every DeviceBuffer holds, and the cap (0 = none)
+std::atomic<uint64_t> g_device_bytes{0};
+std::atomic<uint64_t> g_device_cap{0};
+} // namespace
+
+void set_device_alloc_cap(uint64_t bytes) { g_device_cap.store(bytes); }
 
 cudaError_t DeviceBuffer::ensure(size_t bytes) {
   if (bytes <= size_ && ptr_ != nullptr) {
@@ -19,6 +29,11 @@ cudaError_t DeviceBuffer::ensure(size_t bytes) {
   if (bytes == 0) {
     return cudaSuccess;
   }
+  const uint64_t cap = g_device_cap.load();
+  if (cap != 0 && g_device_bytes.load() + bytes > cap) {
+    // the allocation a capped device would refuse, refused on the host
+    return cudaErrorMemoryAllocation;
+  }
   cudaError_t e = cudaMalloc(&ptr_, bytes);
   if (e != cudaSuccess) {
     ptr_ = nullptr;
@@ -26,6 +41,7 @@ cudaError_t DeviceBuffer::ensure(size_t bytes) {
     return e;
   }
   size_ = bytes;
+  g_device_bytes.fetch_add(bytes);
   return cudaSuccess;
 }
 
@@ -40,6 +56,7 @@ cudaError_t DeviceBuffer::upload(const void *src, size_t bytes, cudaStream_t s) 
 void DeviceBuffer::release() {
   if (ptr_ != nullptr) {
     cudaFree(ptr_);
+    g_device_bytes.fetch_sub(size_);
   }
   ptr_ = nullptr;
   size_ = 0;
@@ -513,6 +530,9 @@ Status check_settings(const path_settings &s) {
   if (s.wavefront_slots_log2 != 0 && (s.wavefront_slots_log2 < 10 || s.wavefront_slots_log2 > 26)) {
     return Status::err(PATH_ERR_ARGUMENT, "wavefront_slots_log2 must be 0 or in [10, 26]");
   }
+  if (s.trace_staged_nodes > kMaxStagedNodes) {
+    return Status::err(PATH_ERR_ARGUMENT, "trace_staged_nodes must be at most 512");
+  }
   return Status::ok();
 }
 
@@ -725,6 +745,12 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   p.cache_depth = cache_ != nullptr ? cache_depth_ : 0u;
   p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   p.row_hi = row_hi;
+  // the streaming trace kernel's shared-memory copy of the BVH's top (host
+  // builds lay the top levels out breadth first; the default trace variant)
+  p.n_staged = st.traversal == PATH_TRAVERSAL_WIDE8 && !prep_.gpu_built &&
+                       (st.trace_min_blocks == 0 || st.trace_min_blocks == 4)
+                   ? std::min(st.trace_staged_nodes, prep_.wide.n_top)
+                   : 0u;
   const size_t pix0 = (size_t)row_lo * x_dim;           // first band pixel
   const size_t n_band = (size_t)(row_hi - row_lo) * x_dim;
 
@@ -951,7 +977,7 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   PG_TRY_CUDA(launch_wavefront_init(w, n_slots, stream_), "wavefront init");
   *launches += 1;
   const uint32_t trace_grid =
-      (uint32_t)num_sms_ * (uint32_t)wavefront_trace_blocks_per_sm(min_blocks, counting);
+      (uint32_t)num_sms_ * (uint32_t)wavefront_trace_blocks_per_sm(min_blocks, counting, p.n_staged);
   const uint32_t shade_grid = (uint32_t)num_sms_ * 4;
   uint32_t parity = 0;
   volatile uint32_t *live = h + 12;

@@ -20,6 +20,11 @@
 
 namespace pg {
 
+// Fault injection for the out-of-memory paths (path_debug_set_device_alloc_cap):
+// once the device memory DeviceBuffers hold would exceed `bytes` (0 = no cap),
+// further allocations fail as cudaMalloc does when the device is full.
+void set_device_alloc_cap(uint64_t bytes);
+
 class DeviceBuffer {
 public:
   DeviceBuffer() = default;

@@ -187,9 +187,20 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
 // (and the triangles of its leaf slots) per step; when a quarter of a warp's
 // lanes are idle they take new queue entries together (one atomic per
 // warp), so lanes rarely wait on the longest ray of a batch.
-template <bool kCount, int kMinBlocks>
+// kStaged: the CTA first copies the BVH's top nodes (W.P.n_staged of them,
+// breadth first from the root) into shared memory, where every lane reads
+// them from then on.
+template <bool kCount, int kMinBlocks, bool kStaged>
 __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W) {
+  extern __shared__ uint4 s_top[];
   const uint32_t lane = threadIdx.x & 31;
+  const uint32_t n_top = kStaged ? W.P.n_staged : 0u;
+  if constexpr (kStaged) {
+    for (uint32_t i = threadIdx.x; i < 5 * n_top; i += blockDim.x) {
+      s_top[i] = __ldg(W.P.wide_nodes + i);
+    }
+    __syncthreads();
+  }
   const uint32_t count = W.q->rays;
   Counts cnt = {0, 0, 0};
   WideWalk w;
@@ -236,7 +247,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
     }
     uint32_t tri_base = 0, tmask = 0;
     if (have && !w.done) {
-      wide_node<kCount>(W.P, w, st_base, st_bits, cnt, tri_base, tmask);
+      wide_node<kCount, kStaged>(W.P, w, st_base, st_bits, cnt, tri_base, tmask, s_top, n_top);
     }
     warp_triangles<kCount>(W.P, w, tri_base, tmask, lane, cnt);
     if (have && w.done) {
@@ -524,24 +535,32 @@ cudaError_t launch_wavefront_init(const WaveParams &w, uint32_t n0, cudaStream_t
 
 namespace {
 template <bool kCount>
-void *trace_kernel(uint32_t min_blocks) {
+void *trace_kernel(uint32_t min_blocks, bool staged) {
   switch (min_blocks) {
   case 3:
-    return (void *)dev::k_wf_trace<kCount, 3>;
+    return (void *)dev::k_wf_trace<kCount, 3, false>;
   case 5:
-    return (void *)dev::k_wf_trace<kCount, 5>;
+    return (void *)dev::k_wf_trace<kCount, 5, false>;
   case 6:
-    return (void *)dev::k_wf_trace<kCount, 6>;
+    return (void *)dev::k_wf_trace<kCount, 6, false>;
   default:
-    return (void *)dev::k_wf_trace<kCount, 4>;
+    return staged ? (void *)dev::k_wf_trace<kCount, 4, true>
+                  : (void *)dev::k_wf_trace<kCount, 4, false>;
   }
 }
+
+size_t staged_bytes(uint32_t n_staged) { return (size_t)n_staged * sizeof(WideNode); }
 } // namespace
 
-int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting) {
+int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting, uint32_t n_staged) {
   int n = 0;
-  void *k = counting ? trace_kernel<true>(min_blocks) : trace_kernel<false>(min_blocks);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, 0) != cudaSuccess || n < 1) {
+  const bool staged = n_staged > 0 && (min_blocks == 0 || min_blocks == 4);
+  void *k = counting ? trace_kernel<true>(min_blocks, staged)
+                     : trace_kernel<false>(min_blocks, staged);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256,
+                                                    staged ? staged_bytes(n_staged) : 0) !=
+          cudaSuccess ||
+      n < 1) {
     n = 1;
   }
   return n;
@@ -549,9 +568,12 @@ int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting) {
 
 cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
                                    uint32_t min_blocks, bool counting, cudaStream_t s) {
-  void *k = counting ? trace_kernel<true>(min_blocks) : trace_kernel<false>(min_blocks);
+  const bool staged = w.P.n_staged > 0 && (min_blocks == 0 || min_blocks == 4);
+  void *k = counting ? trace_kernel<true>(min_blocks, staged)
+                     : trace_kernel<false>(min_blocks, staged);
   void *args[] = {const_cast<WaveParams *>(&w)};
-  return cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args, 0, s);
+  return cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args,
+                          staged ? staged_bytes(w.P.n_staged) : 0, s);
 }
 
 cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_t shade_grid,

@@ -4,6 +4,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <deque>
 
 namespace pg {
 
@@ -262,11 +263,25 @@ WideBVH build_wide(const BinaryBVH &bvh) {
     uint32_t depth;
   };
   out.nodes.resize(1);
+  // Nodes of depth < kBfsDepth are expanded breadth first, so the nodes of
+  // depth <= kBfsDepth take the first indices level by level (a prefix of
+  // them is what the trace kernel stages in shared memory); below that the
+  // expansion is depth first, which keeps each subtree's nodes together.
+  std::deque<Job> queue;
   std::vector<Job> stack;
-  stack.push_back({0, 0, 0, 0});
-  while (!stack.empty()) {
-    Job job = stack.back();
-    stack.pop_back();
+  queue.push_back({0, 0, 0, 0});
+  while (!queue.empty() || !stack.empty()) {
+    Job job;
+    if (!queue.empty()) {
+      job = queue.front();
+      queue.pop_front();
+    } else {
+      if (out.n_top == 0) {
+        out.n_top = (uint32_t)out.nodes.size();
+      }
+      job = stack.back();
+      stack.pop_back();
+    }
     out.depth = std::max(out.depth, job.depth);
     std::vector<Slot> slots;
     const BinaryNode &root = bvh.nodes[job.bin];
@@ -347,9 +362,16 @@ WideBVH build_wide(const BinaryBVH &bvh) {
     }
     out.nodes.resize(out.nodes.size() + n_internal);
     out.nodes[job.wide] = wn;
-    for (size_t k = children.size(); k-- > 0;) {
-      stack.push_back(children[k]);
+    if (job.depth + 1 < kBfsDepth) {
+      queue.insert(queue.end(), children.begin(), children.end());
+    } else {
+      for (size_t k = children.size(); k-- > 0;) {
+        stack.push_back(children[k]);
+      }
     }
+  }
+  if (out.n_top == 0) {
+    out.n_top = (uint32_t)out.nodes.size();
   }
   return out;
 }

@@ -22,10 +22,16 @@
 
 namespace pg {
 
+// depth down to which the nodes are laid out breadth first (see build_wide)
+constexpr uint32_t kBfsDepth = 3;
+
 struct WideBVH {
   std::vector<WideNode> nodes;
   std::vector<uint32_t> tri_index; // wide-leaf slot -> BVH-order triangle
   uint32_t depth = 0;
+  // nodes [0, n_top) are the nodes of depth <= kBfsDepth in breadth-first
+  // order (root, its internal children, theirs, ...)
+  uint32_t n_top = 0;
 };
 
 WideBVH build_wide(const BinaryBVH &bvh);

@@ -170,3 +170,28 @@ def test_batch_images_match_the_oracle(lib, oracle):
               "samples changed by ties")
         assert np.array_equal(out.view(np.uint32), want.view(np.uint32))
         assert tied <= 0.005 * a.shape[0] * a.shape[1] * a.shape[2]
+
+
+@pytest.mark.parametrize("case", ["cornell", "large_mesh"])
+def test_staged_top_nodes_render_the_same_image(lib, case, request):
+    # the trace kernel's shared-memory copy of the BVH's top changes where
+    # nodes are read from, not which: the images are identical bit for bit
+    if case == "cornell":
+        scene = scenes.cornell_box()
+        w = h = 64
+    else:
+        scene = request.getfixturevalue("large_mesh")[0]
+        w = h = 48
+    s = scenes.path_settings(8, "wide")
+    s.kernel_approach = 1
+    f2w = scenes.cornell_camera(w, h)
+    r = api.Renderer()
+    imgs = []
+    for staged in (0, 1, 73, 512):
+        s.trace_staged_nodes = staged
+        out = np.zeros((h, w, 3), np.float32)
+        r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), out, scene, 8, s)
+        assert r.stats()["device_status"] == 0
+        imgs.append(out)
+    for img in imgs[1:]:
+        assert np.array_equal(img.view(np.uint32), imgs[0].view(np.uint32))

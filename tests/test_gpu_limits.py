@@ -56,3 +56,35 @@ def test_endless_path_is_cut_and_reported(lib, approach, traversal):
              img, sc, 4, s2)
     assert r.stats()["device_status"] == 0
     assert float(img.mean()) > 0.0
+
+
+PATH_ERR_OOM = 3
+
+
+@pytest.mark.parametrize("approach", [0, 1])
+def test_allocation_failure_is_reported_and_the_renderer_recovers(lib, approach):
+    # An allocation cap (host-side fault injection: the allocation a full
+    # device would refuse is refused before cudaMalloc is called) forces the
+    # out-of-memory path in the middle of a render: the call returns
+    # PATH_ERR_OOM with a message, and with the cap lifted the same renderer
+    # renders the image a fresh renderer renders.
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, "wide")
+    s.kernel_approach = approach
+    w = h = 32
+    spec = api.SquareImage(w, h, scenes.cornell_camera(w, h))
+    want = np.zeros((h, w, 3), np.float32)
+    api.Renderer().render(api.ExecutionModel.GPU, spec, want, sc, 4, s)
+    r = api.Renderer()
+    out = np.zeros((h, w, 3), np.float32)
+    try:
+        capi.load().path_debug_set_device_alloc_cap(64 * 1024)
+        with pytest.raises(capi.PathError) as e:
+            r.render(api.ExecutionModel.GPU, spec, out, sc, 4, s)
+        assert e.value.status == PATH_ERR_OOM
+        assert "memory" in str(e.value).lower() or "alloc" in str(e.value).lower()
+    finally:
+        capi.load().path_debug_set_device_alloc_cap(0)
+    r.render(api.ExecutionModel.GPU, spec, out, sc, 4, s)
+    assert r.stats()["device_status"] == 0
+    assert np.array_equal(out.view(np.uint32), want.view(np.uint32))

@@ -106,6 +106,30 @@ def test_wide_bvh_covers_every_triangle_and_children_contain_their_subtrees():
     subtree_box(0)
 
 
+def test_wide_bvh_top_levels_are_breadth_first():
+    # the nodes of depth <= 3 take the first indices, level by level, so a
+    # prefix of the node array is the top of the tree (the part the trace
+    # kernel keeps in shared memory)
+    tris, _ = scenes.displaced_icosphere(6)
+    nodes = api.wide_build(tris, api.Settings())["nodes"]
+    depth = np.full(len(nodes), -1)
+    depth[0] = 0
+    order = [0]
+    for i in order:
+        node = nodes[i]
+        rank = 0
+        for s in range(8):
+            if (int(node["imask"]) >> s) & 1:
+                c = int(node["child_base"]) + rank
+                rank += 1
+                depth[c] = depth[i] + 1
+                order.append(c)
+    assert np.all(depth >= 0)
+    top = int(np.sum(depth <= 3))
+    assert top > 73 and np.all(depth[:top] <= 3) and np.all(depth[top:] > 3)
+    assert np.all(np.diff(depth[:top]) >= 0)
+
+
 def _big_leaf_scene(rng):
     """90 copies of one triangle (the SBVH cannot split them: one binary leaf
     of 90, more than the 32 triangles a wide node addresses) among random
