@@ -353,12 +353,53 @@ def time_to_rmse(r, scene, w, h, f2w, settings, ref, cfg, max_frames, base, targ
     res = {"frames": frames, "seconds": wall, "rel_rmse": err,
            "reached": err is not None and err <= target, "curve": curve}
     if cfg is not None:
+        res["cache_bias"] = cache_bias(r, scene, settings, cache, cfg["cache_depth"])
         res["cache"] = (
             "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
             f"paths end into the cache at vertex {cfg['cache_depth']}, "
             f"{cfg['train_paths']} records x {cfg['train_steps']} steps per frame, "
             f"{cfg['pretrain_frames']} training-only frames first")
     return res
+
+
+def cache_bias(r, scene, settings, cache, depth, n_queries=4096, ref_spp=1024):
+    """The trained cache against converged radiance at its own queries: of
+    the last frame's paths that ended into the cache (a spread sample of
+    them), the network's prediction against the radiance the rest of the
+    path carries on average, estimated by ref_spp paths traced from each
+    query point (InitialRays from just in front of the point towards it,
+    with the depth the path had left) in two halves, whose difference
+    gives the estimate's own noise.  Queries on the light are left out (the
+    traced estimate counts the light's emission, the cache's target does
+    not)."""
+    from path_gb300 import api
+    q, beta = r.cached_frame_queries(max_n=n_queries, stride=997)
+    if len(q) == 0:
+        return None
+    pos, wo = q[:, 0:3], q[:, 3:6]
+    off_light = ~((pos[:, 1] > 0.99) & (np.abs(pos[:, 0]) < 0.26) & (np.abs(pos[:, 2]) < 0.26))
+    q, beta, pos, wo = q[off_light], beta[off_light], pos[off_light], wo[off_light]
+    rays = np.concatenate([pos + 1e-3 * wo, -wo], 1).astype(np.float32)
+    s = settings.copy()
+    s.set_term_prob("NIters", iters=max(0, int(settings.term_prob_iters) - depth))
+    out = np.zeros((len(rays), 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.InitialRays(rays), out, scene, ref_spp // 2, s)
+    half = out.astype(np.float64)  # the first half of the samples
+    r.render(api.ExecutionModel.GPU, api.InitialRays(rays), out, scene, ref_spp, s)
+    ref = out.astype(np.float64)
+    # ref - half = (second half - first half) / 2: the standard error of ref
+    pred = cache.query(q).astype(np.float64)
+    norm = np.linalg.norm(ref)
+    wnorm = np.linalg.norm(beta * ref)
+    rel = np.abs(pred - ref).sum(1) / (np.abs(ref).sum(1) + 1e-3)
+    return {
+        "queries": int(len(q)), "reference_spp": ref_spp,
+        "rel_l2": float(np.linalg.norm(pred - ref) / norm),
+        "rel_l2_throughput_weighted": float(np.linalg.norm(beta * (pred - ref)) / wnorm),
+        "mean_rel_bias": float(np.sum(pred - ref) / np.sum(ref)),
+        "median_rel_err": float(np.median(rel)), "p90_rel_err": float(np.percentile(rel, 90)),
+        "reference_noise_rel_l2": float(np.linalg.norm(ref - half) / norm),
+    }
 
 
 def gpu_reference(r, scene, w, h, f2w, settings, first_sample, n_samples=4096, per_render=64):

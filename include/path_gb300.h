@@ -347,6 +347,16 @@ path_status path_render_cached(path_renderer *renderer, path_cache *cache,
                                const path_settings *settings, uint32_t cache_depth,
                                uint32_t train_paths, uint32_t train_steps, double *seconds);
 
+/* The queries of the last path_render_cached frame (for judging the cache's
+ * bias): of every stride-th sample of the frame, those whose path ended into
+ * the cache, at most max_n, in sample order -- queries [n][12] (position,
+ * direction towards the previous vertex, shading normal, albedo: the
+ * network's input record) and the path throughput there [n][3]; n_out
+ * receives n.  Host buffers. */
+path_status path_cache_frame_queries(const path_renderer *renderer, uint32_t max_n,
+                                     uint32_t stride, float *queries, float *throughput,
+                                     uint32_t *n_out);
+
 /* ---- batched render (GB300 addition; the reference renders one scene per
  * call) ---- */
 /* One image of a batch: a scene, its square-image camera, samples per pixel

@@ -322,6 +322,16 @@ class Renderer:
             int(train_steps), ctypes.byref(secs)))
         return secs.value
 
+    def cached_frame_queries(self, max_n=1 << 16, stride=1):
+        """path_cache_frame_queries: (queries [n, 12], throughput [n, 3]) of
+        the last cached frame's samples whose paths ended into the cache."""
+        q = np.zeros((max_n, 12), np.float32)
+        b = np.zeros((max_n, 3), np.float32)
+        n = ctypes.c_uint32()
+        capi.check(capi.load().path_cache_frame_queries(self._h, int(max_n), int(stride),
+                                                        _fptr(q), _fptr(b), ctypes.byref(n)))
+        return q[:n.value], b[:n.value]
+
     @staticmethod
     def _output_c(output):
         """(capi.Output, array) for a numpy or torch FloatRGB / BGRA image."""

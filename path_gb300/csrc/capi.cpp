@@ -399,6 +399,17 @@ path_status path_render_cached(path_renderer *renderer, path_cache *cache,
   });
 }
 
+path_status path_cache_frame_queries(const path_renderer *renderer, uint32_t max_n,
+                                     uint32_t stride, float *queries, float *throughput,
+                                     uint32_t *n_out) {
+  if (!renderer || !queries || !throughput || !n_out) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    return from(renderer->r.cached_frame_queries(max_n, stride, queries, throughput, n_out));
+  });
+}
+
 path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k, uint32_t n,
                                float *d) {
   if (!a || !b || !d) {

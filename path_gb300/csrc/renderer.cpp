@@ -948,6 +948,7 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
                 "cache queries");
     w.cache_q = cache_q_.as<float>();
     w.cache_beta = cache_beta_.as<float>();
+    cached_samples_ = total;
   }
   const bool grad = adj != nullptr;
   if (grad) {
@@ -1199,6 +1200,34 @@ Status Renderer::render_adjoint(const path_sample_spec &spec, const Scene &scene
 } // namespace pg
 
 namespace pg {
+
+Status Renderer::cached_frame_queries(uint32_t max_n, uint32_t stride, float *queries,
+                                      float *throughput, uint32_t *n_out) const {
+  *n_out = 0;
+  if (stride == 0 || cached_samples_ == 0 || cache_q_.get() == nullptr) {
+    return Status::err(PATH_ERR_ARGUMENT, "no cached frame (or stride 0)");
+  }
+  const size_t n = (size_t)((cached_samples_ + stride - 1) / stride);
+  std::vector<float> q(n * 12), b(n * 3);
+  // every stride-th record, strided copies
+  PG_TRY_CUDA(cudaMemcpy2D(q.data(), 48, cache_q_.get(), (size_t)48 * stride, 48, n,
+                           cudaMemcpyDeviceToHost),
+              "cache queries");
+  PG_TRY_CUDA(cudaMemcpy2D(b.data(), 12, cache_beta_.get(), (size_t)12 * stride, 12, n,
+                           cudaMemcpyDeviceToHost),
+              "cache throughput");
+  uint32_t k = 0;
+  for (size_t i = 0; i < n && k < max_n; ++i) {
+    if (b[3 * i] == 0.f && b[3 * i + 1] == 0.f && b[3 * i + 2] == 0.f) {
+      continue; // the path ended before the cache vertex
+    }
+    std::memcpy(queries + (size_t)12 * k, &q[12 * i], 48);
+    std::memcpy(throughput + (size_t)3 * k, &b[3 * i], 12);
+    ++k;
+  }
+  *n_out = k;
+  return Status::ok();
+}
 
 // One frame with the radiance cache: render (paths end into the cache at
 // vertex cache_depth), then train the cache on fresh full-length paths.

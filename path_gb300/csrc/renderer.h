@@ -142,6 +142,10 @@ public:
                        const Scene &scene, uint32_t spp, const path_settings &settings,
                        class RadianceCache &cache, uint32_t cache_depth, uint32_t train_paths,
                        uint32_t train_steps, double *seconds);
+  // every stride-th sample of the last cached frame whose path ended into
+  // the cache: its query [12] and throughput [3] (at most max_n of them)
+  Status cached_frame_queries(uint32_t max_n, uint32_t stride, float *queries,
+                              float *throughput, uint32_t *n_out) const;
   // batched render and its launch-shape autotuner (defined in batch.cpp)
   Status render_batch(const std::vector<BatchItem> &items, const path_settings &settings,
                       const path_batch_tuning *tuning, double *seconds);
@@ -196,6 +200,7 @@ private:
   class RadianceCache *cache_ = nullptr; // set during a cached render
   uint32_t cache_depth_ = 0;
   uint32_t frame_counter_ = 0;
+  uint64_t cached_samples_ = 0; // samples of the last cached frame (cache_q_, cache_beta_)
   // cached render: training paths traced on a side stream while the frame
   // renders (cache_train_paths_ > 0 asks render() to launch them)
   uint32_t cache_train_paths_ = 0;
