@@ -338,8 +338,8 @@ path_status path_cache_access(path_cache *cache, float *weights, float *table,
  * paths end into the cache at vertex cache_depth (the cache's prediction of
  * the radiance leaving that vertex, times the path throughput, replaces the
  * rest of the path), then train_steps Adam steps on train_paths records from
- * full-length training paths (one random vertex each: its query and the
- * radiance the rest of its path carried back).  Square images, streaming
+ * full-length training paths (each its vertex at cache_depth: its query and
+ * the radiance the rest of its path carried back).  Square images, streaming
  * approach, 8-wide BVH. */
 path_status path_render_cached(path_renderer *renderer, path_cache *cache,
                                const path_sample_spec *sample_spec, const path_output *output,

@@ -1,7 +1,8 @@
-// 8-wide BVH built on the GPU: a linear BVH over Morton codes (Karras,
-// "Maximizing Parallelism in the Construction of BVHs, Octrees, and k-d
-// Trees", HPG 2012) collapsed top-down into the 80-byte quantised nodes of
-// the traversal, one tree level per launch.
+// 8-wide BVH built on the GPU: triangles sorted by the Morton codes of their
+// centroids, clustered bottom-up into a binary BVH by PLOC (Meister and
+// Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume
+// Hierarchy Construction", IEEE TVCG 2018), then collapsed top-down into the
+// 80-byte quantised nodes of the traversal, one tree level per launch.
 //
 // Any BVH over the triangles gives the traversal the same closest hits (the
 // 8-wide traversal takes the smallest distance, then the smallest BVH-order
@@ -10,25 +11,32 @@
 // exactly the same distance is reported.
 //
 // Stages: Morton code of each centroid (10 bits per axis) -> radix sort of
-// (code, triangle) pairs -> internal nodes of the radix tree (longest common
-// prefix, ties broken by position) with parent links -> boxes bottom-up (the
-// second child to arrive at a node merges), together with the surface-area
-// cost optimisation of the collapse (the host builder's: per binary node the
-// cheapest forest of at most 1..8 slots, from its children's) -> collapse:
-// every wide node takes the best forest of eight slots of its binary node's
-// children, places them in octant slots (as the host builder does),
-// quantises their boxes (the same exact-plane frame), and queues its
-// internal children.
+// (code, triangle) pairs -> PLOC rounds (nearest neighbour by merged surface
+// area within 16 clusters either side, mutual pairs merge, survivors
+// compacted) with parent links -> boxes bottom-up (the second child to
+// arrive at a node merges), together with the surface-area cost optimisation
+// of the collapse (the host builder's: per binary node the cheapest forest
+// of at most 1..8 slots -- a subtree of up to four triangles may be one leaf
+// slot -- from its children's) -> collapse: every wide node takes the best
+// forest of eight slots of its binary node's children, places them in
+// octant slots (as the host builder does), quantises their boxes (the same
+// exact-plane frame), and queues its internal children.
 #include "geom.h"
 #include "gpu_build.h"
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 namespace pg {
 namespace dev {
 namespace {
 
 constexpr uint32_t kLeafBit = 1u << 31; // node ids: internal i, or leaf k | kLeafBit
+// a wide-node slot holding every triangle of internal node i: i | kSlotBit
+constexpr uint32_t kSlotBit = 1u << 30;
+// most triangles of such a slot (eight slots of four stay within the 32
+// triangles a wide node addresses)
+constexpr uint32_t kSlotMaxTris = 4;
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
   v = (v * 0x00010001u) & 0xFF0000FFu;
@@ -59,62 +67,107 @@ __global__ void k_morton(const float *t9, uint32_t n, f3 lo, f3 inv_ext, uint32_
   vals[i] = i;
 }
 
-// common-prefix length of sorted positions i and j (-1 outside [0, n))
-__device__ __forceinline__ int delta(const uint32_t *keys, uint32_t n, int i, int j) {
-  if (j < 0 || j >= (int)n) {
-    return -1;
-  }
-  const uint32_t a = keys[i], b = keys[j];
-  if (a == b) {
-    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
-  }
-  return __clz(a ^ b);
-}
-
-__global__ void k_radix_tree(const uint32_t *keys, uint32_t n, uint32_t *left,
-                             uint32_t *right, uint32_t *parent) {
-  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (i >= (int)n - 1) {
-    return;
-  }
-  const int d = delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1) >= 0 ? 1 : -1;
-  const int dmin = delta(keys, n, i, i - d);
-  int lmax = 2;
-  while (delta(keys, n, i, i + lmax * d) > dmin) {
-    lmax *= 2;
-  }
-  int l = 0;
-  for (int t = lmax / 2; t >= 1; t /= 2) {
-    if (delta(keys, n, i, i + (l + t) * d) > dmin) {
-      l += t;
-    }
-  }
-  const int j = i + l * d;
-  const int dnode = delta(keys, n, i, j);
-  int s = 0;
-  int t = l;
-  do {
-    t = (t + 1) / 2;
-    if (delta(keys, n, i, i + (s + t) * d) > dnode) {
-      s += t;
-    }
-  } while (t > 1);
-  const int gamma = i + s * d + (d < 0 ? -1 : 0);
-  const uint32_t lc = (min(i, j) == gamma) ? ((uint32_t)gamma | kLeafBit) : (uint32_t)gamma;
-  const uint32_t rc =
-      (max(i, j) == gamma + 1) ? ((uint32_t)(gamma + 1) | kLeafBit) : (uint32_t)(gamma + 1);
-  left[i] = lc;
-  right[i] = rc;
-  parent[(lc & kLeafBit) ? (n - 1) + (lc & ~kLeafBit) : lc] = (uint32_t)i;
-  parent[(rc & kLeafBit) ? (n - 1) + (rc & ~kLeafBit) : rc] = (uint32_t)i;
-}
-
 __device__ __forceinline__ box tri_box(const float *t9, uint32_t i) {
   box b = empty_box();
   b = grow(b, vert(t9, i, 0));
   b = grow(b, vert(t9, i, 1));
   b = grow(b, vert(t9, i, 2));
   return b;
+}
+
+// ---- PLOC: parallel locally-ordered clustering (Meister and Bittner,
+// "Parallel Locally-Ordered Clustering for Bounding Volume Hierarchy
+// Construction", IEEE TVCG 2018).  Clusters start as the triangles in
+// Morton order; every round each cluster finds, among the kPlocRadius
+// clusters on either side, the one whose merged box has the smallest
+// surface area; pairs that chose each other merge into a new internal node,
+// and the surviving clusters are compacted in order.  Internal node ids
+// are handed out from n - 2 down, so the last merge, the root, is node 0.
+constexpr int kPlocRadius = 16;
+
+__global__ void k_ploc_init(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *clus,
+                            box *cbox) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) {
+    return;
+  }
+  clus[k] = k | kLeafBit;
+  cbox[k] = tri_box(t9, perm[k]);
+}
+
+// nearest neighbour of every cluster: (merged area, index) smallest
+__global__ void k_ploc_nn(const box *cbox, uint32_t m, uint32_t *nn) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= (int)m) {
+    return;
+  }
+  const box bi = cbox[i];
+  unsigned long long best = ~0ull;
+  const int lo = max(0, i - kPlocRadius), hi = min((int)m - 1, i + kPlocRadius);
+  for (int j = lo; j <= hi; ++j) {
+    if (j == i) {
+      continue;
+    }
+    const float d = area(merge(bi, cbox[j]));
+    const unsigned long long key =
+        ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(uint32_t)j;
+    best = key < best ? key : best;
+  }
+  nn[i] = m > 1 ? (uint32_t)best : (uint32_t)i;
+}
+
+// keep[i]: 1 when cluster i survives the round (merged into its own slot,
+// or not merged); mutual pairs (i < j) merge into slot i
+__global__ void k_ploc_mark(const uint32_t *nn, uint32_t m, uint32_t *keep, uint32_t *merges) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) {
+    return;
+  }
+  const uint32_t j = nn[i];
+  const bool mutual = j != i && nn[j] == i;
+  keep[i] = (!mutual || i < j) ? 1u : 0u;
+  merges[i] = (mutual && i < j) ? 1u : 0u;
+}
+
+// with force (a round that found no mutual pair, possible only at exact
+// ties): neighbours 2t, 2t + 1 merge instead
+__global__ void k_ploc_force(uint32_t m, uint32_t *nn, uint32_t *keep, uint32_t *merges) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) {
+    return;
+  }
+  const uint32_t j = (i & 1u) ? i - 1 : (i + 1 < m ? i + 1 : i);
+  nn[i] = j;
+  keep[i] = (j == i || i < j) ? 1u : 0u;
+  merges[i] = (j != i && i < j) ? 1u : 0u;
+}
+
+// the merges of a round: the pair at rank r of the round (merge_pos[i] =
+// exclusive prefix of merges) becomes internal node id_base - 1 - r; the
+// survivors move to keep_pos[i] (exclusive prefix of keep)
+__global__ void k_ploc_merge(const uint32_t *clus, const box *cbox, const uint32_t *nn,
+                             const uint32_t *keep, const uint32_t *keep_pos,
+                             const uint32_t *merges, const uint32_t *merge_pos, uint32_t m,
+                             uint32_t n, uint32_t id_base, uint32_t *left, uint32_t *right,
+                             uint32_t *parent, uint32_t *clus_out, box *cbox_out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m || !keep[i]) {
+    return;
+  }
+  uint32_t id = clus[i];
+  box b = cbox[i];
+  if (merges[i]) {
+    const uint32_t j = nn[i];
+    const uint32_t a = clus[i], c = clus[j];
+    id = id_base - 1 - merge_pos[i];
+    left[id] = a;
+    right[id] = c;
+    parent[(a & kLeafBit) ? (n - 1) + (a & ~kLeafBit) : a] = id;
+    parent[(c & kLeafBit) ? (n - 1) + (c & ~kLeafBit) : c] = id;
+    b = merge(b, cbox[j]);
+  }
+  clus_out[keep_pos[i]] = id;
+  cbox_out[keep_pos[i]] = b;
 }
 
 __device__ __forceinline__ box load_box_cg(const box *b) {
@@ -129,8 +182,10 @@ __device__ __forceinline__ box load_box_cg(const box *b) {
 // 0.3, per unit area); every leaf of the linear BVH is one triangle
 constexpr float kCostNode = 1.0f;
 constexpr float kCostTri = 0.3f;
-// how the best forest of <= i slots represents a binary subtree
-constexpr uint8_t kFewer = 0, kWide = 1, kOpen = 3; // kOpen + k: k slots left
+// how the best forest of <= i slots represents a binary subtree: fewer
+// slots, a wide node of its own, one leaf slot of all its triangles, or its
+// two children's forests (kOpen + k: k slots to the left child)
+constexpr uint8_t kFewer = 0, kWide = 1, kLeafSlot = 2, kOpen = 3;
 
 // the cost of child c's best forest of <= i slots (i = 1..8)
 __device__ __forceinline__ float child_cost(uint32_t c, const box &cb, const float *cost,
@@ -143,7 +198,8 @@ __device__ __forceinline__ float child_cost(uint32_t c, const box &cb, const flo
 // of a wide node's 8 slots), bottom-up; flags start at zero
 __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const uint32_t *left,
                         const uint32_t *right, const uint32_t *parent, box *boxes,
-                        uint32_t *flags, float *cost, uint8_t *how, uint8_t *wide_k) {
+                        uint32_t *flags, float *cost, uint8_t *how, uint8_t *wide_k,
+                        uint32_t *tri_count) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) {
     return;
@@ -165,6 +221,9 @@ __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const
     const box br = load_box_cg(boxes + ((r & kLeafBit) ? (n - 1) + (r & ~kLeafBit) : r));
     const box bn = merge(bl, br);
     boxes[node] = bn;
+    const uint32_t cnt = ((l & kLeafBit) ? 1u : __ldcg(tri_count + l)) +
+                         ((r & kLeafBit) ? 1u : __ldcg(tri_count + r));
+    tri_count[node] = cnt;
     float cl[9], cr[9];
     for (int i = 1; i <= 8; ++i) {
       cl[i] = child_cost(l, bl, cost, i);
@@ -181,8 +240,14 @@ __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const
     }
     wide_k[node] = bk;
     float c = area(bn) * kCostNode + best;
+    uint8_t h1 = kWide;
+    if (cnt <= kSlotMaxTris && area(bn) * (float)cnt * kCostTri < c) {
+      // every triangle of the subtree in one leaf slot
+      c = area(bn) * (float)cnt * kCostTri;
+      h1 = kLeafSlot;
+    }
     cost[8 * (size_t)node] = c;
-    how[8 * (size_t)node] = kWide;
+    how[8 * (size_t)node] = h1;
     for (int i = 2; i <= 8; ++i) {
       uint8_t h = kFewer;
       for (int k = 1; k < i; ++k) {
@@ -241,7 +306,23 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
   }
   const Entry e = in[q];
   auto box_of = [&](uint32_t id) -> box {
-    return boxes[(id & kLeafBit) ? (n - 1) + (id & ~kLeafBit) : id];
+    return boxes[(id & kLeafBit) ? (n - 1) + (id & ~kLeafBit) : (id & ~kSlotBit)];
+  };
+  // the sorted positions of the triangles under internal node v (at most
+  // kSlotMaxTris), left to right
+  auto slot_tris = [&](uint32_t v, uint32_t *tris) -> uint32_t {
+    uint32_t st[2 * kSlotMaxTris], sp = 0, cnt = 0;
+    st[sp++] = v;
+    while (sp > 0 && cnt < kSlotMaxTris) {
+      const uint32_t u = st[--sp];
+      if (u & kLeafBit) {
+        tris[cnt++] = u & ~kLeafBit;
+      } else if (sp + 2 <= 2 * kSlotMaxTris) {
+        st[sp++] = right[u];
+        st[sp++] = left[u];
+      }
+    }
+    return cnt;
   };
   uint32_t kids[8];
   uint32_t nk = 0;
@@ -268,7 +349,9 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
         --i;
       }
       const uint8_t h = how[8 * (size_t)v + (i - 1)];
-      if (i == 1 || h == kWide) {
+      if (h == kLeafSlot) {
+        kids[nk++] = v | kSlotBit; // one slot of all its triangles
+      } else if (i == 1 || h == kWide) {
         kids[nk++] = v; // a wide node of its own
       } else {
         const uint32_t kk = h - kOpen; // 1 <= kk < i: both children get a slot
@@ -328,6 +411,9 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
   for (uint32_t i = 0; i < nk; ++i) {
     if (kids[i] & kLeafBit) {
       ++n_leaf;
+    } else if (kids[i] & kSlotBit) {
+      uint32_t tmp[kSlotMaxTris];
+      n_leaf += slot_tris(kids[i] & ~kSlotBit, tmp);
     } else {
       ++n_int;
     }
@@ -362,19 +448,29 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
       wn.qlo[a][s] = (uint8_t)fmax(0.0, fmin(255.0, lo));
       wn.qhi[a][s] = (uint8_t)fmax(0.0, fmin(255.0, hi));
     }
-    if (id & kLeafBit) {
-      const uint32_t k = id & ~kLeafBit; // sorted position = BVH-order index
-      const uint32_t o = perm[k];
-      const f3 v0 = vert(t9, o, 0), v1 = vert(t9, o, 1), v2 = vert(t9, o, 2);
-      const f3 e1 = v1 - v0, e2 = v2 - v0;
-      float *dst = wide_tris + 12 * (size_t)(tri_base + tri_off);
-      const float vals[12] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y,
-                              e2.z, __uint_as_float(k), 0.f, 0.f};
-      for (int j = 0; j < 12; ++j) {
-        dst[j] = vals[j];
+    if (id & (kLeafBit | kSlotBit)) {
+      // sorted positions = BVH-order indices of the slot's triangles
+      uint32_t ks[kSlotMaxTris];
+      uint32_t cnt = 1;
+      if (id & kLeafBit) {
+        ks[0] = id & ~kLeafBit;
+      } else {
+        cnt = slot_tris(id & ~kSlotBit, ks);
       }
-      wn.meta[s] = (uint8_t)((1u << 5) | tri_off);
-      ++tri_off;
+      for (uint32_t t = 0; t < cnt; ++t) {
+        const uint32_t k = ks[t];
+        const uint32_t o = perm[k];
+        const f3 v0 = vert(t9, o, 0), v1 = vert(t9, o, 1), v2 = vert(t9, o, 2);
+        const f3 e1 = v1 - v0, e2 = v2 - v0;
+        float *dst = wide_tris + 12 * (size_t)(tri_base + tri_off + t);
+        const float vals[12] = {v0.x, v0.y, v0.z, e1.x, e1.y, e1.z, e2.x, e2.y,
+                                e2.z, __uint_as_float(k), 0.f, 0.f};
+        for (int j = 0; j < 12; ++j) {
+          dst[j] = vals[j];
+        }
+      }
+      wn.meta[s] = (uint8_t)((cnt << 5) | tri_off);
+      tri_off += cnt;
     } else {
       wn.imask |= (uint8_t)(1u << s);
       wn.meta[s] = (uint8_t)rank;
@@ -389,6 +485,94 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
 
 } // namespace
 } // namespace dev
+
+namespace {
+
+// the binary tree over the Morton-sorted triangles by PLOC (left, right:
+// internal nodes 0..n-2, 0 the root; parent of every node)
+Status ploc_tree(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *left,
+                 uint32_t *right, uint32_t *parent, cudaStream_t s) {
+#define PG_PL_TRY(expr, what)                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      return cuda_status(e_, what);                                            \
+    }                                                                          \
+  } while (0)
+  const size_t nn = n;
+  DeviceBuffer clus[2], cbox[2], nbr, keep, keep_pos, merges, merge_pos, tmp, tail;
+  for (int k = 0; k < 2; ++k) {
+    PG_PL_TRY(clus[k].ensure(nn * 4), "ploc");
+    PG_PL_TRY(cbox[k].ensure(nn * sizeof(box)), "ploc");
+  }
+  PG_PL_TRY(nbr.ensure(nn * 4), "ploc");
+  PG_PL_TRY(keep.ensure(nn * 4), "ploc");
+  PG_PL_TRY(keep_pos.ensure(nn * 4), "ploc");
+  PG_PL_TRY(merges.ensure(nn * 4), "ploc");
+  PG_PL_TRY(merge_pos.ensure(nn * 4), "ploc");
+  PG_PL_TRY(tail.ensure(16), "ploc");
+  size_t tmp_bytes = 0;
+  PG_PL_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, keep.as<uint32_t>(),
+                                          keep_pos.as<uint32_t>(), (int)n, s),
+            "ploc scan");
+  PG_PL_TRY(tmp.ensure(std::max<size_t>(tmp_bytes, 16)), "ploc");
+  const uint32_t bs = 256;
+  dev::k_ploc_init<<<(n + bs - 1) / bs, bs, 0, s>>>(t9, perm, n, clus[0].as<uint32_t>(),
+                                                    cbox[0].as<box>());
+  PG_PL_TRY(cudaGetLastError(), "ploc init");
+  uint32_t m = n, id_base = n - 1, cur = 0;
+  // every round merges at least one pair, so n - 1 rounds always suffice
+  for (uint32_t round = 0; m > 1; ++round) {
+    if (round > n) {
+      return Status::err(PATH_ERR_DEVICE_TIMEOUT, "gpu build: clustering did not finish");
+    }
+    const uint32_t nb = (m + bs - 1) / bs;
+    dev::k_ploc_nn<<<nb, bs, 0, s>>>(cbox[cur].as<box>(), m, nbr.as<uint32_t>());
+    dev::k_ploc_mark<<<nb, bs, 0, s>>>(nbr.as<uint32_t>(), m, keep.as<uint32_t>(),
+                                       merges.as<uint32_t>());
+    PG_PL_TRY(cudaGetLastError(), "ploc neighbours");
+    // merges in this round: last exclusive prefix + last flag
+    PG_PL_TRY(cub::DeviceScan::ExclusiveSum(tmp.get(), tmp_bytes, merges.as<uint32_t>(),
+                                            merge_pos.as<uint32_t>(), (int)m, s),
+              "ploc scan");
+    uint32_t h[2];
+    PG_PL_TRY(cudaMemcpyAsync(&h[0], merge_pos.as<uint32_t>() + (m - 1), 4,
+                              cudaMemcpyDeviceToHost, s),
+              "ploc count");
+    PG_PL_TRY(cudaMemcpyAsync(&h[1], merges.as<uint32_t>() + (m - 1), 4, cudaMemcpyDeviceToHost,
+                              s),
+              "ploc count");
+    PG_PL_TRY(cudaStreamSynchronize(s), "ploc count");
+    uint32_t n_merge = h[0] + h[1];
+    if (n_merge == 0) {
+      // no mutual pair (exact ties): merge neighbours pairwise this round
+      dev::k_ploc_force<<<nb, bs, 0, s>>>(m, nbr.as<uint32_t>(), keep.as<uint32_t>(),
+                                          merges.as<uint32_t>());
+      PG_PL_TRY(cub::DeviceScan::ExclusiveSum(tmp.get(), tmp_bytes, merges.as<uint32_t>(),
+                                              merge_pos.as<uint32_t>(), (int)m, s),
+                "ploc scan");
+      n_merge = m / 2;
+    }
+    PG_PL_TRY(cub::DeviceScan::ExclusiveSum(tmp.get(), tmp_bytes, keep.as<uint32_t>(),
+                                            keep_pos.as<uint32_t>(), (int)m, s),
+              "ploc scan");
+    dev::k_ploc_merge<<<nb, bs, 0, s>>>(
+        clus[cur].as<uint32_t>(), cbox[cur].as<box>(), nbr.as<uint32_t>(), keep.as<uint32_t>(),
+        keep_pos.as<uint32_t>(), merges.as<uint32_t>(), merge_pos.as<uint32_t>(), m, n, id_base,
+        left, right, parent, clus[cur ^ 1].as<uint32_t>(), cbox[cur ^ 1].as<box>());
+    PG_PL_TRY(cudaGetLastError(), "ploc merge");
+    id_base -= n_merge;
+    m -= n_merge;
+    cur ^= 1;
+  }
+  if (id_base != 0) {
+    return Status::err(PATH_ERR_DEVICE_TIMEOUT, "gpu build: clustering left nodes unassigned");
+  }
+  return Status::ok();
+#undef PG_PL_TRY
+}
+
+} // namespace
 
 Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float *hi,
                       cudaStream_t s, GpuWideBVH &out) {
@@ -406,7 +590,7 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   } while (0)
   const size_t nn = n;
   DeviceBuffer keys, vals, keys2, tmp, left, right, parent, boxes, flags, qa, qb, counters, cost,
-      how, wide_k;
+      how, wide_k, tri_count;
   PG_GB_TRY(keys.ensure(nn * 4), "gpu build");
   PG_GB_TRY(vals.ensure(nn * 4), "gpu build");
   PG_GB_TRY(keys2.ensure(nn * 4), "gpu build");
@@ -437,16 +621,18 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   PG_GB_TRY(cost.ensure(std::max<size_t>(n_int, 1) * 32), "gpu build");
   PG_GB_TRY(how.ensure(std::max<size_t>(n_int, 1) * 8), "gpu build");
   PG_GB_TRY(wide_k.ensure(std::max<size_t>(n_int, 1)), "gpu build");
+  PG_GB_TRY(tri_count.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
   if (n_int > 0) {
-    dev::k_radix_tree<<<(uint32_t)((n_int + bs - 1) / bs), bs, 0, s>>>(
-        keys2.as<uint32_t>(), n, left.as<uint32_t>(), right.as<uint32_t>(),
-        parent.as<uint32_t>());
-    PG_GB_TRY(cudaGetLastError(), "radix tree");
+    Status sp = ploc_tree(t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(),
+                          right.as<uint32_t>(), parent.as<uint32_t>(), s);
+    if (!sp.good()) {
+      return sp;
+    }
   }
   dev::k_boxes<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(),
                                  right.as<uint32_t>(), parent.as<uint32_t>(), boxes.as<box>(),
                                  flags.as<uint32_t>(), cost.as<float>(), how.as<uint8_t>(),
-                                 wide_k.as<uint8_t>());
+                                 wide_k.as<uint8_t>(), tri_count.as<uint32_t>());
   PG_GB_TRY(cudaGetLastError(), "boxes");
   // collapse: a wide node has at most 8 children and at least 2 binary
   // nodes below it, so n wide nodes and n queue entries always suffice

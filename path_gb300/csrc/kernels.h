@@ -151,9 +151,10 @@ cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
                                  uint32_t n_blocks, cudaStream_t s);
 
 // training records for the radiance cache: n full-length paths from random
-// pixels, one random vertex each ([n][16]: query, radiance, pad)
-cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, float *records,
-                             cudaStream_t s);
+// pixels, each its vertex at `depth` (or its last) ([n][16]: query,
+// radiance, pad)
+cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, uint32_t depth,
+                             float *records, cudaStream_t s);
 // sample_rgb[i] += beta[i] * max(pred[i], 0) for the n samples
 cudaError_t launch_nrc_apply(float *sample_rgb, const float *beta, const float *pred,
                              size_t n, cudaStream_t s);

@@ -1,11 +1,15 @@
 // Training data of the radiance cache: full-length paths traced from random
 // pixels with the integrator of the render (8-wide BVH), each contributing
-// one randomly chosen vertex: its query (position, direction towards the
-// previous vertex, shading normal, albedo) and, as the target, the radiance
-// its path gathered after that vertex's emission divided by the path
-// throughput at the vertex -- a one-sample estimate of the radiance leaving
-// the vertex that the cache has to predict.  Compiled with --fmad=false like
-// the render kernels.
+// its vertex at the depth where the render's paths end into the cache: its
+// query (position, direction towards the previous vertex, shading normal,
+// albedo) and, as the target, the radiance its path gathered after that
+// vertex's emission divided by the path throughput at the vertex -- a
+// one-sample estimate of exactly what the render asks the cache for there,
+// with the bounces a path has left at that depth.  (A vertex at another
+// depth has a different number of bounces left, so its target estimates a
+// different quantity: mixing depths biased the cache low.)  A path that
+// ends before that depth gives its last vertex.  Compiled with --fmad=false
+// like the render kernels.
 #include "integrator.cuh"
 
 namespace pg {
@@ -26,7 +30,8 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 
 template <bool kUniform>
 __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_t n,
-                                                   uint32_t frame, float *records) {
+                                                   uint32_t frame, uint32_t depth,
+                                                   float *records) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) {
     return;
@@ -76,7 +81,7 @@ __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_
     }
     return;
   }
-  const uint32_t k = mix32(h0 ^ 0x7f4a7c15u) % nv;
+  const uint32_t k = depth < nv ? depth : nv - 1;
   const rgb total = s.total;
   const rgb rest = total - gathered[k];
   const float t[3] = {beta[k].r > 1e-12f ? rest.r / beta[k].r : 0.f,
@@ -107,15 +112,16 @@ __global__ void k_nrc_apply(float *sample_rgb, const float *beta, const float *p
 } // namespace
 } // namespace dev
 
-cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, float *records,
+cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, uint32_t depth,
+                             float *records,
                              cudaStream_t s) {
   if (n == 0) {
     return cudaSuccess;
   }
   if (p.rng_uniform) {
-    dev::k_nrc_paths<true><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, records);
+    dev::k_nrc_paths<true><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, depth, records);
   } else {
-    dev::k_nrc_paths<false><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, records);
+    dev::k_nrc_paths<false><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, depth, records);
   }
   return cudaGetLastError();
 }

@@ -770,7 +770,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     RenderParams tp = p;
     tp.cache_depth = 0;
     PG_TRY_CUDA(cache_records_.ensure((size_t)cache_train_paths_ * 64), "cache records");
-    PG_TRY_CUDA(launch_nrc_paths(tp, cache_train_paths_, frame_counter_++,
+    PG_TRY_CUDA(launch_nrc_paths(tp, cache_train_paths_, frame_counter_++, p.cache_depth,
                                  cache_records_.as<float>(), side_stream_),
                 "cache training paths");
     PG_TRY_CUDA(cudaEventRecord(side_done_, side_stream_), "event");
