@@ -522,6 +522,28 @@ def run_cache(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_sobol_draws(args, rank):
+    """Cost of the integrator's Sobol draws read from the table against the
+    same values formed from the direction vectors in registers
+    (path_debug_sobol_draws), on the large-mesh workload's draw count: 67.1 M
+    paths (1024 x 1024 x 64 spp) of 48 draws (six per vertex over the eight
+    vertices of a depth-8 path)."""
+    from path_gb300 import api
+    n_paths, spp, draws = 1024 * 1024 * 64, 64, 48
+    modes = {0: "table (the integrator's)", 1: "direction vectors via L1, XOR in registers",
+             2: "direction vectors in shared memory, XOR in registers"}
+    res, sums = {}, set()
+    for m, name in modes.items():
+        ms, cs = api.debug_sobol_draws(m, n_paths, spp, draws)
+        res[name] = {"ms": ms, "ns_per_draw": ms * 1e6 / (n_paths * draws)}
+        sums.add(cs)
+    line = {"metric": "Sobol draw cost", "unit": "ms per 3.2 G draws", "n_gpus": 1,
+            "config": {"workload": f"{n_paths} paths x {draws} draws, spp {spp}, 256 dims"},
+            "modes": res, "same_values": len(sums) == 1}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -529,7 +551,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mesh",
-                    choices=["large_mesh", "cornell", "batched", "cache"])
+                    choices=["large_mesh", "cornell", "batched", "cache", "sobol_draws"])
     ap.add_argument("--max-frames", type=int, default=400,
                     help="cache workload: frames before giving up on the error target")
     ap.add_argument("--cache-depth", type=int, default=2,
@@ -594,6 +616,9 @@ def main():
         return
     if args.workload == "cache":
         run_cache(args, rank, world, local_rank)
+        return
+    if args.workload == "sobol_draws":
+        run_sobol_draws(args, rank)
         return
     scene, w, h, spp, depth, desc = make_workload(args.workload, args.size, args.spp)
     settings = scenes.path_settings(depth, args.traversal)

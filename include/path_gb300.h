@@ -460,6 +460,17 @@ void path_debug_set_device_alloc_cap(uint64_t bytes);
  *         out [n]. */
 path_status path_debug_bsdf(const path_material *material, uint32_t op, const float *in,
                             uint32_t n, float *out);
+/* The cost of the render's Sobol draws (GB300 addition, a measurement):
+ * n_paths paths of `draws` consecutive dimensions each (sample index p mod
+ * spp, first dimension as a pixel's, 256 dimensions), summed per path;
+ * mode 0 reads the values from the table the integrator uses
+ * (rng_from_sequence_gen.h:45-54), mode 1 forms each from the direction
+ * vectors XOR-ed in a register (vectors read through L1), mode 2 the same
+ * with the vectors in shared memory.  ms receives the kernel time of one
+ * launch (mean of 3 after a warm-up), checksum a hash of the sums, equal
+ * across the modes. */
+path_status path_debug_sobol_draws(uint32_t mode, uint32_t n_paths, uint32_t spp,
+                                   uint32_t draws, float *ms, uint32_t *checksum);
 /* kernel::WorkDivision (src/kernel/work_division.cpp:12-69): out receives
  * [block_size, base_samples_per_thread, n_threads_per_unit_extra,
  *  sample_block_size, x_block_size, y_block_size, num_sample_blocks,

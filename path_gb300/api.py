@@ -498,6 +498,18 @@ def debug_bsdf(material, op, records):
     return out[:, 0] if op == 2 else out
 
 
+def debug_sobol_draws(mode, n_paths, spp, draws):
+    """path_debug_sobol_draws: (ms per launch, checksum) of n_paths paths of
+    `draws` Sobol draws, read from the table (mode 0) or formed from the
+    direction vectors in registers (1: vectors through L1, 2: in shared
+    memory)."""
+    ms = np.zeros(1, np.float32)
+    cs = np.zeros(1, np.uint32)
+    capi.check(capi.load().path_debug_sobol_draws(int(mode), int(n_paths), int(spp), int(draws),
+                                                  _fptr(ms), _uptr(cs)))
+    return float(ms[0]), int(cs[0])
+
+
 def work_division(wd_settings, samples_per, x_dim, y_dim):
     out = (ctypes.c_uint32 * 11)()
     capi.check(capi.load().path_work_division(ctypes.byref(wd_settings), samples_per, x_dim,

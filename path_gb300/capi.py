@@ -129,6 +129,7 @@ SIGNATURES = {
     "path_debug_pmath": (ctypes.c_int, [c_u32, _PF, _PF, _PF, c_u32]),
     "path_debug_bsdf": (ctypes.c_int, [ctypes.POINTER(PathMaterial), c_u32, _PF, c_u32, _PF]),
     "path_debug_set_device_alloc_cap": (None, [ctypes.c_uint64]),
+    "path_debug_sobol_draws": (ctypes.c_int, [c_u32, c_u32, c_u32, c_u32, _PF, _PU]),
     "path_cache_frame_queries": (ctypes.c_int, [_P, c_u32, c_u32, _PF, _PF, _PU]),
     "path_work_division": (ctypes.c_int, [ctypes.POINTER(WorkDivisionSettings), c_u32, c_u32,
                                           c_u32, _PU]),

@@ -17,6 +17,7 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <vector>
 
 struct path_scene {
   pg::Scene s;
@@ -649,6 +650,96 @@ path_status path_sobol_table(uint32_t dimension_bound, uint32_t count, float *ou
 
 path_status path_sobol_table_curand(uint32_t dimension_bound, uint32_t count, float *out) {
   return sobol_common(dimension_bound, count, out, true);
+}
+
+path_status path_debug_sobol_draws(uint32_t mode, uint32_t n_paths, uint32_t spp,
+                                   uint32_t draws, float *ms, uint32_t *checksum) {
+  if (!ms || !checksum || mode > 2 || spp == 0 || spp > (1u << 20) || n_paths == 0 ||
+      n_paths > (1u << 28) || draws == 0 || draws > 4096) {
+    return fail(PATH_ERR_ARGUMENT, "bad Sobol draw arguments");
+  }
+  return guarded([&] {
+    const uint32_t bound = 256;
+    curandDirectionVectors32_t *vecs = nullptr;
+    unsigned *scr = nullptr;
+    if (curandGetDirectionVectors32(&vecs, CURAND_SCRAMBLED_DIRECTION_VECTORS_32_JOEKUO6) !=
+            CURAND_STATUS_SUCCESS ||
+        curandGetScrambleConstants32(&scr) != CURAND_STATUS_SUCCESS) {
+      return fail(PATH_ERR_CUDA, "cuRAND direction vectors unavailable");
+    }
+    pg::DeviceBuffer d_dirs, d_scr, d_table, d_out;
+    pg::Status st = pg::cuda_status(d_dirs.upload(vecs, (size_t)bound * 128, 0), "dirs");
+    if (st.good()) {
+      st = pg::cuda_status(d_scr.upload(scr, (size_t)bound * 4, 0), "scramble");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(d_table.ensure((size_t)bound * spp * 4), "table");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(d_out.ensure((size_t)n_paths * 4), "out");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(pg::launch_sobol_table(d_dirs.as<uint32_t>(), d_scr.as<uint32_t>(),
+                                                  bound, spp, d_table.as<float>(), 0),
+                           "sobol table");
+    }
+    int dev = 0, sms = 0;
+    if (st.good()) {
+      st = pg::cuda_status(cudaGetDevice(&dev), "device");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                           "sm count");
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st.good()) {
+      st = pg::cuda_status(cudaEventCreate(&e0), "event");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(cudaEventCreate(&e1), "event");
+    }
+    const int reps = 3;
+    for (int r = -1; st.good() && r < reps; ++r) {
+      if (r == 0) {
+        st = pg::cuda_status(cudaEventRecord(e0, 0), "event");
+      }
+      if (st.good()) {
+        st = pg::cuda_status(pg::launch_sobol_draws((int)mode, d_table.as<float>(),
+                                                    d_dirs.as<uint32_t>(),
+                                                    d_scr.as<uint32_t>(), bound, spp, n_paths,
+                                                    draws, (uint32_t)sms * 8, d_out.as<float>(),
+                                                    0),
+                             "sobol draws");
+      }
+    }
+    if (st.good()) {
+      st = pg::cuda_status(cudaEventRecord(e1, 0), "event");
+    }
+    if (st.good()) {
+      st = pg::cuda_status(cudaEventSynchronize(e1), "event");
+    }
+    float t = 0.f;
+    if (st.good()) {
+      cudaEventElapsedTime(&t, e0, e1);
+      *ms = t / reps;
+      std::vector<uint32_t> h(n_paths);
+      st = pg::cuda_status(cudaMemcpy(h.data(), d_out.get(), (size_t)n_paths * 4,
+                                      cudaMemcpyDeviceToHost),
+                           "copy");
+      uint32_t c = 0;
+      for (uint32_t v : h) {
+        c = c * 31u + v;
+      }
+      *checksum = c;
+    }
+    if (e0) {
+      cudaEventDestroy(e0);
+    }
+    if (e1) {
+      cudaEventDestroy(e1);
+    }
+    return from(st);
+  });
 }
 
 path_status path_debug_pmath(uint32_t fn, const float *x, const float *y, float *out,

@@ -194,6 +194,13 @@ cudaError_t launch_sobol_curand(const uint32_t *dirs, const uint32_t *scramble,
 
 cudaError_t launch_pmath(uint32_t fn, const float *x, const float *y,
                          float *out, uint32_t n, cudaStream_t s);
+// Sobol draw cost: mode 0 table reads, 1 direction vectors XOR-ed in
+// registers (vectors through L1), 2 the same with the vectors in shared
+// memory; out[p] = the sum of path p's draws
+cudaError_t launch_sobol_draws(int mode, const float *table, const uint32_t *dirs,
+                               const uint32_t *scramble, uint32_t dim_bound, uint32_t spp,
+                               uint32_t n_paths, uint32_t draws, uint32_t grid, float *out,
+                               cudaStream_t s);
 // BSDF probe over n records of 9 floats (ops as path_debug_bsdf)
 cudaError_t launch_bsdf(const DevMaterial *mat, uint32_t op, const float *in, uint32_t n,
                         float *out, cudaStream_t s);
