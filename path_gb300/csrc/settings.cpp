@@ -387,7 +387,8 @@ bool settings_from_yaml_text(const std::string &text, path_settings &s,
         !read_bool(get(g, "count_work"), s.count_work, err) ||
         !read_bool(get(g, "time_kernels"), s.time_kernels, err) ||
         !read_bool(get(g, "gpu_build"), s.gpu_build, err) ||
-        !read_u32(get(g, "wavefront_slots_log2"), s.wavefront_slots_log2, err)) {
+        !read_u32(get(g, "wavefront_slots_log2"), s.wavefront_slots_log2, err) ||
+        !read_u32(get(g, "trace_staged_nodes"), s.trace_staged_nodes, err)) {
       return false;
     }
   }
