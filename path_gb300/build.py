@@ -30,6 +30,13 @@ CPP_SOURCES = ["capi.cpp", "renderer.cpp", "batch.cpp", "cache_host.cpp", "scene
 INCLUDES = ["-I" + CSRC, "-I" + os.path.join(ROOT, "include"),
             "-I" + os.path.join(CUDA_HOME, "include")]
 
+# How the integrator draws its Sobol numbers: "table" reads the [spp][dims]
+# table built once per render (the reference's scheme), "direct" forms each
+# value from the direction vectors XOR-ed in a register.  Both give the same
+# values bit for bit; the choice is a build option (PATH_GB300_SOBOL_DRAW).
+SOBOL_DRAW = os.environ.get("PATH_GB300_SOBOL_DRAW", "table")
+STAMP = os.path.join(OUT_DIR, "build_options.txt")
+
 
 def _sources_newer(target, deps):
     if not os.path.exists(target):
@@ -54,10 +61,22 @@ def _run(cmd):
     return proc.stdout
 
 
+def _options():
+    if SOBOL_DRAW not in ("table", "direct"):
+        raise RuntimeError("PATH_GB300_SOBOL_DRAW must be 'table' or 'direct'")
+    return f"sobol_draw={SOBOL_DRAW}"
+
+
 def build(force=False, verbose=False, ptxas_info=False):
-    """Compile the library if any source is newer than it; return its path."""
+    """Compile the library if any source is newer than it (or the build
+    options changed); return its path."""
     deps = _all_deps()
-    if not force and not _sources_newer(LIB, deps):
+    try:
+        with open(STAMP) as f:
+            same_options = f.read() == _options()
+    except OSError:
+        same_options = False
+    if not force and same_options and not _sources_newer(LIB, deps):
         return LIB
     if shutil.which(NVCC) is None and not os.path.exists(NVCC):
         raise RuntimeError("nvcc not found at " + NVCC)
@@ -68,6 +87,7 @@ def build(force=False, verbose=False, ptxas_info=False):
         obj = os.path.join(obj_dir, src + ".o")
         cmd = [NVCC] + ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                                "-Xcompiler", "-fPIC,-ffp-contract=off",
+                               f"-DPG_SOBOL_DIRECT={1 if SOBOL_DRAW == 'direct' else 0}",
                                "-c", os.path.join(CSRC, src), "-o", obj] + INCLUDES
         if ptxas_info:
             cmd += ["-Xptxas", "-v"]
@@ -89,6 +109,8 @@ def build(force=False, verbose=False, ptxas_info=False):
         "-Xlinker", "-rpath," + os.path.join(CUDA_HOME, "lib64")]
     _run(link)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_options())
     return LIB
 
 

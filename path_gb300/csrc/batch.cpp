@@ -427,6 +427,7 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   p.light_tris = b_lights_.as<const float4>();
   p.light_cdf = b_cdf_.as<const float>();
   p.sobol = sobol_table_.as<const float>();
+  p.sobol_vec = sobol_dirs_.as<const uint32_t>();
   p.dim_bound = st.max_sample_size;
   p.init_dim_bound = std::min(64u, st.max_sample_size);
   p.light_sampler = st.light_sampler;

@@ -609,6 +609,35 @@ __device__ __forceinline__ float uniform_next(uint32_t *w, uint32_t stride) {
 // of the Uniform draw.
 template <bool kUniform> struct RngT;
 
+#if PG_SOBOL_DIRECT
+// Sobel drawn from the direction vectors: x = scramble_d XOR the vectors
+// v_{d,j} of the set bits j of the Gray code of the sample's Sobol index,
+// XOR-ed in a register, mapped to (0, 1] and 1.0 to 0.0 -- the value the
+// table holds (k_sobol), bit for bit.  vec = [bound][32] vectors followed
+// by the [bound] scramble constants.
+template <> struct RngT<false> {
+  const uint32_t *vec;
+  uint32_t gray;
+  uint32_t dim;
+  uint32_t bound;
+  __device__ __forceinline__ float next() {
+    uint32_t x = __ldg(vec + 32 * bound + dim);
+    const uint32_t *v = vec + 32 * dim;
+    for (uint32_t g = gray; g != 0; g &= g - 1) {
+      x ^= __ldg(v + (__ffs(g) - 1));
+    }
+    const float f = __fadd_rn(__fmul_rn(__uint2float_rn(x), 0x1p-32f), 0x1p-33f);
+    ++dim;
+    dim = dim == bound ? 0u : dim;
+    return f == 1.0f ? 0.0f : f;
+  }
+  __device__ __forceinline__ void begin(const RenderParams &P, uint32_t sobol_index) {
+    vec = P.sobol_vec;
+    gray = sobol_index ^ (sobol_index >> 1);
+    bound = P.dim_bound;
+  }
+};
+#else
 template <> struct RngT<false> {
   const float *row;
   uint32_t dim;
@@ -619,7 +648,13 @@ template <> struct RngT<false> {
     dim = dim == bound ? 0u : dim;
     return v;
   }
+  // the table row of Sobol index sobol_index
+  __device__ __forceinline__ void begin(const RenderParams &P, uint32_t sobol_index) {
+    row = P.sobol + (size_t)sobol_index * P.dim_bound;
+    bound = P.dim_bound;
+  }
 };
+#endif
 
 template <> struct RngT<true> {
   uint32_t *w;
@@ -1222,8 +1257,7 @@ __device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Came
     s.rng.w = rng_words;
     s.rng.stride = rng_stride;
   } else {
-    s.rng.row = P.sobol + (size_t)(sample_idx + P.sample_offset) * P.dim_bound;
-    s.rng.bound = P.dim_bound;
+    s.rng.begin(P, sample_idx + P.sample_offset);
     s.rng.dim = fnv_hash(location) % P.init_dim_bound;
   }
   ray r;

@@ -22,8 +22,10 @@ struct RenderParams {
   const float4 *light_tris; // 3 float4 per light triangle: v0, e0, e1
   const float *light_cdf;
   uint32_t n_lights;
-  // rng: Sobol table [spp][dim_bound]
+  // rng: Sobol table [spp][dim_bound], and the direction vectors
+  // [dim_bound][32] followed by the scramble constants [dim_bound]
   const float *sobol;
+  const uint32_t *sobol_vec;
   uint32_t dim_bound, init_dim_bound;
   // integrator settings
   uint32_t light_sampler, dir_sampler, term_prob, term_iters;

@@ -143,6 +143,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
   p.status = status;
   p.counters = counters;
   p.sobol = sobol_table_.as<const float>();
+  p.sobol_vec = sobol_dirs_.as<const uint32_t>();
   p.dim_bound = st.max_sample_size;
   p.init_dim_bound = std::min(64u, st.max_sample_size);
   p.light_sampler = st.light_sampler;

@@ -444,11 +444,18 @@ Status Renderer::prepare_sobol(uint32_t dim_bound, uint32_t count) {
   if (dim_bound > 20000) {
     return Status::err(PATH_ERR_ARGUMENT, "max_sample_size above the 20000 Sobol dimensions");
   }
-  PG_TRY_CUDA(sobol_dirs_.upload(vecs, (size_t)dim_bound * 32 * 4, stream_), "sobol dirs");
-  PG_TRY_CUDA(sobol_scramble_.upload(scr, (size_t)dim_bound * 4, stream_), "sobol scramble");
+  // direction vectors [dim_bound][32], then the scramble constants
+  PG_TRY_CUDA(sobol_dirs_.ensure((size_t)dim_bound * 33 * 4), "sobol dirs");
+  PG_TRY_CUDA(cudaMemcpyAsync(sobol_dirs_.get(), vecs, (size_t)dim_bound * 32 * 4,
+                              cudaMemcpyHostToDevice, stream_),
+              "sobol dirs");
+  PG_TRY_CUDA(cudaMemcpyAsync(sobol_dirs_.as<uint32_t>() + (size_t)dim_bound * 32, scr,
+                              (size_t)dim_bound * 4, cudaMemcpyHostToDevice, stream_),
+              "sobol scramble");
   PG_TRY_CUDA(sobol_table_.ensure((size_t)dim_bound * count * 4), "sobol table");
-  PG_TRY_CUDA(launch_sobol_table(sobol_dirs_.as<uint32_t>(), sobol_scramble_.as<uint32_t>(),
-                                 dim_bound, count, sobol_table_.as<float>(), stream_),
+  PG_TRY_CUDA(launch_sobol_table(sobol_dirs_.as<uint32_t>(),
+                                 sobol_dirs_.as<uint32_t>() + (size_t)dim_bound * 32, dim_bound,
+                                 count, sobol_table_.as<float>(), stream_),
               "sobol kernel");
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "sobol sync");
   sobol_bound_ = dim_bound;
@@ -707,6 +714,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   RenderParams p;
   fill_params(p);
   p.sobol = sobol_table_.as<const float>();
+  p.sobol_vec = sobol_dirs_.as<const uint32_t>();
   p.dim_bound = st.max_sample_size;
   p.init_dim_bound = std::min(64u, st.max_sample_size);
   p.light_sampler = st.light_sampler;

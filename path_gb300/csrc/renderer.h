@@ -182,7 +182,7 @@ private:
   // pinned host copies of the device arrays above, in the same order
   PinnedBuffer st_tris_, st_data_, st_nodes_, st_extra_, st_wnodes_, st_wtris_, st_mats_,
       st_lights_, st_cdf_, st_perm_;
-  DeviceBuffer sobol_dirs_, sobol_scramble_, sobol_table_;
+  DeviceBuffer sobol_dirs_, sobol_table_; // dirs: vectors, then scramble constants
   uint32_t sobol_bound_ = 0, sobol_count_ = 0;
   DeviceBuffer out_a_, out_b_, bgra_, status_, counters_, rays_, idxs_;
   // wavefront state

@@ -138,8 +138,7 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
     s.rng.stride = W.n_slots;
   } else {
     const uint32_t smp = (uint32_t)(local % spp);
-    s.rng.row = P.sobol + (size_t)(smp + P.sample_offset) * P.dim_bound;
-    s.rng.bound = P.dim_bound;
+    s.rng.begin(P, smp + P.sample_offset);
     s.rng.dim = st.z;
   }
   return id;
