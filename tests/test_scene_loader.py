@@ -91,3 +91,62 @@ def test_reference_scenes_load(lib):
         assert z["triangles"] > 0, name
         loaded += 1
     assert loaded >= 5
+
+
+FIXTURES = os.path.join(HERE, "golden", "reference_scenes.npz")
+FIXTURE_SCENES = ["cornell-diffuse", "cornell-glossy-sphere", "cornell-mirror",
+                  "cornell-glass-box"]
+
+
+def _obj_faces(path):
+    """Polygons of an OBJ file (negative indices resolved), in file order."""
+    verts, faces = [], []
+    with open(path) as f:
+        for line in f:
+            tok = line.split()
+            if not tok:
+                continue
+            if tok[0] == "v":
+                verts.append([float(x) for x in tok[1:4]])
+            elif tok[0] == "f":
+                idx = []
+                for t in tok[1:]:
+                    i = int(t.split("/")[0])
+                    idx.append(i - 1 if i > 0 else len(verts) + i)
+                faces.append(np.array([verts[i] for i in idx]))
+    return faces
+
+
+@pytest.mark.skipif(not REFERENCE_SCENES or not os.path.isdir(REFERENCE_SCENES),
+                    reason="PATH_REFERENCE_SCENES does not name the reference's scenes folder")
+@pytest.mark.parametrize("name", FIXTURE_SCENES)
+def test_reference_scene_loads_as_the_fixture_and_covers_every_face(lib, name):
+    # The loader's output for the reference's own scene is what the GPU
+    # tests render (tests/golden/reference_scenes.npz); and every polygon of
+    # the OBJ is cut into triangles of its own vertices covering its area
+    # (tinyobjloader's triangulation, which the reference uses).
+    g = np.load(FIXTURES)
+    sc, f2w = api.Scene.load_xml(os.path.join(REFERENCE_SCENES, name + ".xml"), 1.0)
+    ex = sc.export()
+    for k in ("triangles", "normals", "tri_material"):
+        assert np.array_equal(ex[k], g[f"{name}/{k}"]), k
+    assert np.array_equal(ex["instance_xforms"][0], g[f"{name}/object_to_world"])
+    assert np.array_equal(f2w, g[f"{name}/film_to_world"])
+    n_mat = ex["n_materials"]
+    assert bytes(ex["materials"])[:64 * n_mat] == g[f"{name}/materials"].tobytes()
+    tris = ex["triangles"].reshape(-1, 3, 3).astype(np.float64)
+    faces = _obj_faces(os.path.join(REFERENCE_SCENES, "models", name + ".obj"))
+    assert sum(len(f) - 2 for f in faces) == len(tris)
+    k = 0
+    for face in faces:
+        part = tris[k:k + len(face) - 2]
+        k += len(face) - 2
+        for t in part:
+            for v in t:
+                assert np.min(np.linalg.norm(face - v, axis=1)) < 1e-6
+        area = 0.5 * np.linalg.norm(np.cross(part[:, 1] - part[:, 0], part[:, 2] - part[:, 0]),
+                                    axis=1).sum()
+        # the polygon's area: fan from its first vertex (convex in these files)
+        fan = 0.5 * np.linalg.norm(np.cross(face[1:-1] - face[0], face[2:] - face[0]),
+                                   axis=1).sum()
+        assert abs(area - fan) <= 1e-5 * max(fan, 1e-6)
