@@ -250,7 +250,7 @@ def run_batched(args, rank, world, local_rank):
     batch = scenes.batch_scenes(args.scenes, seed=0)
     gen_s = time.time() - t0
     settings = scenes.path_settings(6, "wide")
-    settings.gpu_build = 1 if args.gpu_build else 0
+    settings.gpu_build = args.gpu_build
     outs = [np.zeros((h, w, 3), np.float32) for _, w, h, _ in batch]
     items = [(sc, api.SquareImage(w, h, scenes.cornell_camera(w, h)), o, spp)
              for (sc, w, h, spp), o in zip(batch, outs)]
@@ -292,7 +292,8 @@ def run_batched(args, rank, world, local_rank):
         "config": {"workload": f"batched: {len(batch)} seeded scenes, {tris} triangles, "
                                f"{samples} samples, depth 6",
                    "tuning": tuning, "l2": "flushed (512 MB write) before every timed step",
-                   "bvh": "GPU linear BVH" if args.gpu_build else "SBVH (host)",
+                   "bvh": ("GPU PLOC BVH" + (" over split references" if args.gpu_build == 2
+                                             else "")) if args.gpu_build else "SBVH (host)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * samples * args.steps / e2e_total / 1e6, "unit": METRIC,
                 "h2d_bytes_per_step": 0,
@@ -586,8 +587,9 @@ def main():
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel override")
     ap.add_argument("--slots-log2", type=int, default=0,
                     help="streaming: paths in flight = 2^this (0 = default 26)")
-    ap.add_argument("--gpu-build", action="store_true",
-                    help="build the 8-wide BVH on the GPU (linear BVH) instead of the SBVH")
+    ap.add_argument("--gpu-build", type=int, nargs="?", const=1, default=0,
+                    help="build the 8-wide BVH on the GPU instead of the SBVH: 1 PLOC, "
+                         "2 PLOC over split triangle references")
     ap.add_argument("--trace-min-blocks", type=int, default=0,
                     help="streaming trace kernel variant (resident blocks per SM, 3..6)")
     ap.add_argument("--staged-nodes", type=int, default=None,
@@ -624,7 +626,7 @@ def main():
     settings = scenes.path_settings(depth, args.traversal)
     settings.kernel_approach = 1 if args.approach == "streaming" else 0
     settings.trace_min_blocks = args.trace_min_blocks
-    settings.gpu_build = 1 if args.gpu_build else 0
+    settings.gpu_build = args.gpu_build
     settings.wavefront_slots_log2 = args.slots_log2
     if args.staged_nodes is not None:
         settings.trace_staged_nodes = args.staged_nodes
@@ -716,7 +718,7 @@ def main():
     launch_s = kern_ms / launches_per_render / 1e3
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     shape = (f"slots_log2={args.slots_log2 or 26} trace_min_blocks={args.trace_min_blocks or 4} "
-             f"bvh={'gpu' if args.gpu_build else 'sbvh'} "
+             f"bvh={'gpu' + str(args.gpu_build) if args.gpu_build else 'sbvh'} "
              f"staged_nodes={settings.trace_staged_nodes}")
     full_size = args.size is None and args.spp is None
     traffic = _profiled_traffic(kernel_name, args, shape) if full_size else None
@@ -765,7 +767,8 @@ def main():
             "trace_min_blocks": args.trace_min_blocks or 4,
             "slots_log2": args.slots_log2 or 26,
             "staged_nodes": int(settings.trace_staged_nodes),
-            "bvh": "GPU linear BVH collapsed to 8-wide" if args.gpu_build else
+            "bvh": ("GPU PLOC BVH" + (" over split references" if args.gpu_build == 2 else "") +
+                    " collapsed to 8-wide") if args.gpu_build else
                    "SBVH (host) collapsed to 8-wide",
             "l2": "flushed (512 MB write) before every timed step",
             "parallelism": f"replicas x{world}"},

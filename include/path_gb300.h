@@ -136,9 +136,13 @@ typedef struct {
                                 default 4); fewer registers per thread above 3 */
   uint32_t time_kernels;     /* 1: time the streaming trace launches with CUDA
                                 events (path_render_stats.trace_ms) */
-  uint32_t gpu_build;        /* 1: build the 8-wide BVH on the GPU (linear BVH
-                                over Morton codes, collapsed to 8-wide); the
-                                wide traversal only, no binary SBVH */
+  uint32_t gpu_build;        /* build the 8-wide BVH on the GPU: 1 = PLOC
+                                clustering of the triangles in Morton order,
+                                collapsed to 8-wide; 2 = the same after
+                                splitting triangles much smaller than their
+                                boxes into clipped references (spatial
+                                splits); the wide traversal only, no binary
+                                SBVH.  0 = the host SBVH */
   uint32_t wavefront_slots_log2; /* streaming: paths in flight = 2^this
                                     (10..26, 0 = default 26) */
   uint32_t trace_staged_nodes; /* streaming trace kernel: the top nodes of the

@@ -119,7 +119,7 @@ Status Renderer::check_batch(const std::vector<BatchItem> &items,
 }
 
 Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb,
-                               bool gpu_build) {
+                               uint32_t gpu_build) {
   std::vector<std::array<uint64_t, 3>> key;
   key.reserve(items.size());
   for (const BatchItem &it : items) {
@@ -186,20 +186,22 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
       DeviceBuffer d9;
       PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, stream_), "gpu build upload");
       GpuWideBVH g;
-      Status sg = gpu_build_wide(d9.as<float>(), (uint32_t)nt, lo, hi, stream_, g);
+      Status sg = gpu_build_wide(d9.as<float>(), (uint32_t)nt, lo, hi, gpu_build == 2, stream_,
+                                 g);
       if (!sg.good()) {
         return sg;
       }
       WideBVH &w = wides[i];
       w.nodes.resize(g.n_nodes);
       w.depth = g.depth;
-      std::vector<float> wt(nt * 12);
+      const size_t nw = g.n_wide_tris;
+      std::vector<float> wt(nw * 12);
       bvhs[i].permutation.resize(nt);
       if (nt > 0) {
         PG_TRY_CUDA(cudaMemcpyAsync(w.nodes.data(), g.nodes.get(), g.n_nodes * sizeof(WideNode),
                                     cudaMemcpyDeviceToHost, stream_),
                     "gpu build download");
-        PG_TRY_CUDA(cudaMemcpyAsync(wt.data(), g.wide_tris.get(), nt * 48,
+        PG_TRY_CUDA(cudaMemcpyAsync(wt.data(), g.wide_tris.get(), nw * 48,
                                     cudaMemcpyDeviceToHost, stream_),
                     "gpu build download");
         PG_TRY_CUDA(cudaMemcpyAsync(bvhs[i].permutation.data(), g.perm.get(), nt * 4,
@@ -207,8 +209,8 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
                     "gpu build download");
       }
       PG_TRY_CUDA(cudaStreamSynchronize(stream_), "gpu build download");
-      w.tri_index.resize(nt);
-      for (size_t k = 0; k < nt; ++k) {
+      w.tri_index.resize(nw);
+      for (size_t k = 0; k < nw; ++k) {
         std::memcpy(&w.tri_index[k], &wt[12 * k + 9], 4);
       }
     }
@@ -664,7 +666,7 @@ Status Renderer::render_batch(const std::vector<BatchItem> &items, const path_se
     return s0;
   }
   auto t0 = std::chrono::steady_clock::now();
-  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build != 0);
+  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build);
   if (!sp.good()) {
     return sp;
   }
@@ -696,7 +698,7 @@ Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_
   if (!s0.good()) {
     return s0;
   }
-  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build != 0);
+  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build);
   if (!sp.good()) {
     return sp;
   }

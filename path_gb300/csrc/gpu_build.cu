@@ -25,7 +25,10 @@
 #include "gpu_build.h"
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
+
+#include <algorithm>
 
 namespace pg {
 namespace dev {
@@ -85,14 +88,196 @@ __device__ __forceinline__ box tri_box(const float *t9, uint32_t i) {
 // are handed out from n - 2 down, so the last merge, the root, is node 0.
 constexpr int kPlocRadius = 16;
 
-__global__ void k_ploc_init(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *clus,
-                            box *cbox) {
+__global__ void k_ploc_init(const box *item_box, uint32_t n, uint32_t *clus, box *cbox) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) {
     return;
   }
   clus[k] = k | kLeafBit;
-  cbox[k] = tri_box(t9, perm[k]);
+  cbox[k] = item_box[k];
+}
+
+// ---- items: the leaves the tree is built over.  Without splitting, item j
+// is the j-th triangle in Morton order; with splitting (Karras and Aila,
+// "Fast Parallel Construction of High-Quality Bounding Volume Hierarchies",
+// HPG 2013, section 4.3), a triangle whose box is much larger than the
+// triangle itself becomes several references, each with the box of the
+// part of the triangle in one piece of its box (the triangle clipped to the
+// piece: a spatial split made before the tree is built).  item_tri[j] is
+// the triangle's position in Morton order, item_box[j] its box.
+
+__global__ void k_items_plain(const float *t9, const uint32_t *perm, uint32_t n,
+                              uint32_t *item_tri, box *item_box) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) {
+    return;
+  }
+  item_tri[k] = k;
+  item_box[k] = tri_box(t9, perm[k]);
+}
+
+// most references of one triangle
+constexpr uint32_t kMaxRefs = 16;
+
+// splitting priority: how much larger than the triangle its box is (the
+// cube root evens out the budget between large and small excesses)
+__global__ void k_split_priority(const float *t9, const uint32_t *perm, uint32_t n,
+                                 float *prio) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) {
+    return;
+  }
+  const uint32_t o = perm[k];
+  const f3 a = vert(t9, o, 0), b = vert(t9, o, 1), c = vert(t9, o, 2);
+  const float tri_area = 0.5f * length(cross(b - a, c - a));
+  const float excess = area(tri_box(t9, o)) - 4.f * tri_area;
+  prio[k] = excess > 0.f ? cbrtf(excess) : 0.f;
+}
+
+// references per triangle: 1 + its share of the split budget
+__global__ void k_split_count(const float *prio, uint32_t n, float scale, uint32_t *count) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) {
+    return;
+  }
+  const float extra = floorf(prio[k] * scale);
+  count[k] = 1u + (uint32_t)fminf(fmaxf(extra, 0.f), (float)(kMaxRefs - 1));
+}
+
+struct Poly {
+  double v[9][3];
+  int n;
+};
+
+// the part of polygon p on one side of the plane x_axis = at
+__device__ void clip_side(const Poly &p, int axis, double at, bool below, Poly &out) {
+  out.n = 0;
+  for (int i = 0; i < p.n; ++i) {
+    const double *a = p.v[i];
+    const double *b = p.v[(i + 1) % p.n];
+    const bool ina = below ? a[axis] <= at : a[axis] >= at;
+    const bool inb = below ? b[axis] <= at : b[axis] >= at;
+    if (ina && out.n < 9) {
+      for (int c = 0; c < 3; ++c) {
+        out.v[out.n][c] = a[c];
+      }
+      ++out.n;
+    }
+    if (ina != inb && out.n < 9) {
+      const double t = (at - a[axis]) / (b[axis] - a[axis]);
+      for (int c = 0; c < 3; ++c) {
+        out.v[out.n][c] = c == axis ? at : a[c] + t * (b[c] - a[c]);
+      }
+      ++out.n;
+    }
+  }
+}
+
+// polygon box rounded outward to float (empty polygon: `fallback`)
+__device__ box poly_box(const Poly &p, const box &fallback) {
+  if (p.n == 0) {
+    return fallback;
+  }
+  double lo[3], hi[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = hi[c] = p.v[0][c];
+  }
+  for (int i = 1; i < p.n; ++i) {
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = fmin(lo[c], p.v[i][c]);
+      hi[c] = fmax(hi[c], p.v[i][c]);
+    }
+  }
+  box b;
+  b.lo = mk(__double2float_rd(lo[0]), __double2float_rd(lo[1]), __double2float_rd(lo[2]));
+  b.hi = mk(__double2float_ru(hi[0]), __double2float_ru(hi[1]), __double2float_ru(hi[2]));
+  return b;
+}
+
+// the count[k] references of triangle k: its polygon split in halves at
+// the middle of the widest axis of the piece's box, recursively
+__global__ void k_split_emit(const float *t9, const uint32_t *perm, uint32_t n,
+                             const uint32_t *count, const uint32_t *offset, uint32_t *ref_tri,
+                             box *ref_box) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) {
+    return;
+  }
+  const uint32_t o = perm[k];
+  uint32_t out = offset[k];
+  const uint32_t end = out + count[k];
+  struct Piece {
+    Poly p;
+    uint32_t refs;
+  };
+  Piece st[6];
+  int sp = 0;
+  Piece &root = st[sp++];
+  root.p.n = 3;
+  for (int i = 0; i < 3; ++i) {
+    const f3 v = vert(t9, o, i);
+    root.p.v[i][0] = v.x;
+    root.p.v[i][1] = v.y;
+    root.p.v[i][2] = v.z;
+  }
+  root.refs = count[k];
+  const box whole = tri_box(t9, o);
+  while (sp > 0 && out < end) {
+    Piece cur = st[--sp];
+    const box pb = poly_box(cur.p, whole);
+    const f3 ext = pb.hi - pb.lo;
+    const int axis = (ext.x >= ext.y && ext.x >= ext.z) ? 0 : (ext.y >= ext.z ? 1 : 2);
+    if (cur.refs <= 1 || ext.get(axis) <= 0.f || sp + 2 > 6) {
+      // one reference per remaining count (copies when it cannot split)
+      for (uint32_t r = 0; r < cur.refs && out < end; ++r) {
+        ref_tri[out] = k;
+        ref_box[out] = pb;
+        ++out;
+      }
+      continue;
+    }
+    const double at = 0.5 * ((double)pb.lo.get(axis) + (double)pb.hi.get(axis));
+    Piece &a = st[sp++];
+    Piece &b = st[sp++];
+    clip_side(cur.p, axis, at, true, a.p);
+    clip_side(cur.p, axis, at, false, b.p);
+    a.refs = cur.refs / 2;
+    b.refs = cur.refs - cur.refs / 2;
+  }
+  // (count[k] references were reserved; every path above writes them all)
+  while (out < end) {
+    ref_tri[out] = k;
+    ref_box[out] = whole;
+    ++out;
+  }
+}
+
+// Morton code of a box's centre
+__global__ void k_morton_box(const box *boxes, uint32_t n, f3 lo, f3 inv_ext, uint32_t *keys,
+                             uint32_t *vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) {
+    return;
+  }
+  const box b = boxes[i];
+  uint32_t q[3];
+  for (int a = 0; a < 3; ++a) {
+    const float c = 0.5f * (b.lo.get(a) + b.hi.get(a));
+    const float u = (c - lo.get(a)) * inv_ext.get(a) * 1024.f;
+    q[a] = (uint32_t)fminf(fmaxf(u, 0.f), 1023.f);
+  }
+  keys[i] = (expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]);
+  vals[i] = i;
+}
+
+__global__ void k_items_refs(const uint32_t *order, const uint32_t *ref_tri, const box *ref_box,
+                             uint32_t m, uint32_t *item_tri, box *item_box) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) {
+    return;
+  }
+  item_tri[j] = ref_tri[order[j]];
+  item_box[j] = ref_box[order[j]];
 }
 
 // nearest neighbour of every cluster: (merged area, index) smallest
@@ -196,7 +381,7 @@ __device__ __forceinline__ float child_cost(uint32_t c, const box &cb, const flo
 // boxes [internal n-1 | leaves n] and the collapse costs of internal nodes
 // ([n-1][8] cost and decision of the forests of 1..8 slots, the left share
 // of a wide node's 8 slots), bottom-up; flags start at zero
-__global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const uint32_t *left,
+__global__ void k_boxes(const box *item_box, uint32_t n, const uint32_t *left,
                         const uint32_t *right, const uint32_t *parent, box *boxes,
                         uint32_t *flags, float *cost, uint8_t *how, uint8_t *wide_k,
                         uint32_t *tri_count) {
@@ -204,7 +389,7 @@ __global__ void k_boxes(const float *t9, const uint32_t *perm, uint32_t n, const
   if (k >= n) {
     return;
   }
-  boxes[(n - 1) + k] = tri_box(t9, perm[k]);
+  boxes[(n - 1) + k] = item_box[k];
   if (n == 1) {
     return;
   }
@@ -296,7 +481,8 @@ struct Entry {
   uint32_t wide; // its wide node
 };
 
-__global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, const uint32_t *left,
+__global__ void k_collapse(const float *t9, const uint32_t *perm, const uint32_t *item_tri,
+                           uint32_t n, const uint32_t *left,
                            const uint32_t *right, const box *boxes, const uint8_t *how,
                            const uint8_t *wide_k, const Entry *in, uint32_t n_in, Entry *out,
                            uint32_t *counters, WideNode *nodes, float *wide_tris) {
@@ -449,7 +635,8 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
       wn.qhi[a][s] = (uint8_t)fmax(0.0, fmin(255.0, hi));
     }
     if (id & (kLeafBit | kSlotBit)) {
-      // sorted positions = BVH-order indices of the slot's triangles
+      // the slot's items; their triangles' Morton positions are the
+      // BVH-order indices
       uint32_t ks[kSlotMaxTris];
       uint32_t cnt = 1;
       if (id & kLeafBit) {
@@ -458,7 +645,7 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, uint32_t n, co
         cnt = slot_tris(id & ~kSlotBit, ks);
       }
       for (uint32_t t = 0; t < cnt; ++t) {
-        const uint32_t k = ks[t];
+        const uint32_t k = item_tri[ks[t]];
         const uint32_t o = perm[k];
         const f3 v0 = vert(t9, o, 0), v1 = vert(t9, o, 1), v2 = vert(t9, o, 2);
         const f3 e1 = v1 - v0, e2 = v2 - v0;
@@ -490,8 +677,8 @@ namespace {
 
 // the binary tree over the Morton-sorted triangles by PLOC (left, right:
 // internal nodes 0..n-2, 0 the root; parent of every node)
-Status ploc_tree(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *left,
-                 uint32_t *right, uint32_t *parent, cudaStream_t s) {
+Status ploc_tree(const box *item_box, uint32_t n, uint32_t *left, uint32_t *right,
+                 uint32_t *parent, cudaStream_t s) {
 #define PG_PL_TRY(expr, what)                                                  \
   do {                                                                         \
     cudaError_t e_ = (expr);                                                   \
@@ -517,7 +704,7 @@ Status ploc_tree(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *le
             "ploc scan");
   PG_PL_TRY(tmp.ensure(std::max<size_t>(tmp_bytes, 16)), "ploc");
   const uint32_t bs = 256;
-  dev::k_ploc_init<<<(n + bs - 1) / bs, bs, 0, s>>>(t9, perm, n, clus[0].as<uint32_t>(),
+  dev::k_ploc_init<<<(n + bs - 1) / bs, bs, 0, s>>>(item_box, n, clus[0].as<uint32_t>(),
                                                     cbox[0].as<box>());
   PG_PL_TRY(cudaGetLastError(), "ploc init");
   uint32_t m = n, id_base = n - 1, cur = 0;
@@ -575,8 +762,9 @@ Status ploc_tree(const float *t9, const uint32_t *perm, uint32_t n, uint32_t *le
 } // namespace
 
 Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float *hi,
-                      cudaStream_t s, GpuWideBVH &out) {
+                      bool split, cudaStream_t s, GpuWideBVH &out) {
   out.n_nodes = 0;
+  out.n_wide_tris = 0;
   out.depth = 0;
   if (n == 0) {
     return Status::ok();
@@ -611,11 +799,95 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
                                             keys2.as<uint32_t>(), vals.as<uint32_t>(),
                                             out.perm.as<uint32_t>(), (int)n, 0, 30, s),
             "radix sort");
-  const size_t n_int = nn > 1 ? nn - 1 : 0;
+  // the items the tree is built over: triangles, or their references
+  DeviceBuffer item_tri, item_box;
+  uint32_t m = n;
+  if (!split) {
+    PG_GB_TRY(item_tri.ensure(nn * 4), "gpu build");
+    PG_GB_TRY(item_box.ensure(nn * sizeof(box)), "gpu build");
+    dev::k_items_plain<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n,
+                                         item_tri.as<uint32_t>(), item_box.as<box>());
+    PG_GB_TRY(cudaGetLastError(), "items");
+  } else {
+    // budget: 30% more references than triangles, shared by priority
+    DeviceBuffer prio, count, offset, sum, ref_tri, ref_box, rkeys, rvals, rkeys2, rorder;
+    PG_GB_TRY(prio.ensure(nn * 4), "gpu build");
+    PG_GB_TRY(count.ensure(nn * 4), "gpu build");
+    PG_GB_TRY(offset.ensure(nn * 4), "gpu build");
+    PG_GB_TRY(sum.ensure(16), "gpu build");
+    dev::k_split_priority<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n, prio.as<float>());
+    PG_GB_TRY(cudaGetLastError(), "split priority");
+    size_t rb = 0;
+    PG_GB_TRY(cub::DeviceReduce::Sum(nullptr, rb, prio.as<float>(), sum.as<float>(), (int)n, s),
+              "split budget");
+    DeviceBuffer rtmp;
+    PG_GB_TRY(rtmp.ensure(std::max<size_t>(rb, 16)), "gpu build");
+    PG_GB_TRY(cub::DeviceReduce::Sum(rtmp.get(), rb, prio.as<float>(), sum.as<float>(), (int)n, s),
+              "split budget");
+    float total = 0.f;
+    PG_GB_TRY(cudaMemcpyAsync(&total, sum.get(), 4, cudaMemcpyDeviceToHost, s), "split budget");
+    PG_GB_TRY(cudaStreamSynchronize(s), "split budget");
+    const float scale = total > 0.f ? 0.3f * (float)n / total : 0.f;
+    dev::k_split_count<<<nb, bs, 0, s>>>(prio.as<float>(), n, scale, count.as<uint32_t>());
+    PG_GB_TRY(cudaGetLastError(), "split count");
+    size_t sb = 0;
+    PG_GB_TRY(cub::DeviceScan::ExclusiveSum(nullptr, sb, count.as<uint32_t>(),
+                                            offset.as<uint32_t>(), (int)n, s),
+              "split offsets");
+    PG_GB_TRY(rtmp.ensure(std::max<size_t>({rb, sb, 16})), "gpu build");
+    PG_GB_TRY(cub::DeviceScan::ExclusiveSum(rtmp.get(), sb, count.as<uint32_t>(),
+                                            offset.as<uint32_t>(), (int)n, s),
+              "split offsets");
+    uint32_t last[2] = {0, 0};
+    PG_GB_TRY(cudaMemcpyAsync(&last[0], offset.as<uint32_t>() + (n - 1), 4,
+                              cudaMemcpyDeviceToHost, s),
+              "split offsets");
+    PG_GB_TRY(cudaMemcpyAsync(&last[1], count.as<uint32_t>() + (n - 1), 4,
+                              cudaMemcpyDeviceToHost, s),
+              "split offsets");
+    PG_GB_TRY(cudaStreamSynchronize(s), "split offsets");
+    m = last[0] + last[1];
+    const size_t mm = m;
+    PG_GB_TRY(ref_tri.ensure(mm * 4), "gpu build");
+    PG_GB_TRY(ref_box.ensure(mm * sizeof(box)), "gpu build");
+    dev::k_split_emit<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n, count.as<uint32_t>(),
+                                        offset.as<uint32_t>(), ref_tri.as<uint32_t>(),
+                                        ref_box.as<box>());
+    PG_GB_TRY(cudaGetLastError(), "split references");
+    // references in Morton order of their boxes' centres
+    PG_GB_TRY(rkeys.ensure(mm * 4), "gpu build");
+    PG_GB_TRY(rvals.ensure(mm * 4), "gpu build");
+    PG_GB_TRY(rkeys2.ensure(mm * 4), "gpu build");
+    PG_GB_TRY(rorder.ensure(mm * 4), "gpu build");
+    const uint32_t mb = (m + bs - 1) / bs;
+    dev::k_morton_box<<<mb, bs, 0, s>>>(ref_box.as<box>(), m, flo, inv, rkeys.as<uint32_t>(),
+                                        rvals.as<uint32_t>());
+    PG_GB_TRY(cudaGetLastError(), "reference codes");
+    size_t ob = 0;
+    PG_GB_TRY(cub::DeviceRadixSort::SortPairs(nullptr, ob, rkeys.as<uint32_t>(),
+                                              rkeys2.as<uint32_t>(), rvals.as<uint32_t>(),
+                                              rorder.as<uint32_t>(), (int)m, 0, 30, s),
+              "reference sort");
+    PG_GB_TRY(rtmp.ensure(std::max<size_t>({rb, sb, ob, 16})), "gpu build");
+    PG_GB_TRY(cub::DeviceRadixSort::SortPairs(rtmp.get(), ob, rkeys.as<uint32_t>(),
+                                              rkeys2.as<uint32_t>(), rvals.as<uint32_t>(),
+                                              rorder.as<uint32_t>(), (int)m, 0, 30, s),
+              "reference sort");
+    PG_GB_TRY(item_tri.ensure(mm * 4), "gpu build");
+    PG_GB_TRY(item_box.ensure(mm * sizeof(box)), "gpu build");
+    dev::k_items_refs<<<mb, bs, 0, s>>>(rorder.as<uint32_t>(), ref_tri.as<uint32_t>(),
+                                        ref_box.as<box>(), m, item_tri.as<uint32_t>(),
+                                        item_box.as<box>());
+    PG_GB_TRY(cudaGetLastError(), "items");
+    PG_GB_TRY(cudaStreamSynchronize(s), "gpu build");
+  }
+  const size_t mm = m;
+  const uint32_t mb = (m + bs - 1) / bs;
+  const size_t n_int = mm > 1 ? mm - 1 : 0;
   PG_GB_TRY(left.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
   PG_GB_TRY(right.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
-  PG_GB_TRY(parent.ensure((n_int + nn) * 4), "gpu build");
-  PG_GB_TRY(boxes.ensure((n_int + nn) * sizeof(box)), "gpu build");
+  PG_GB_TRY(parent.ensure((n_int + mm) * 4), "gpu build");
+  PG_GB_TRY(boxes.ensure((n_int + mm) * sizeof(box)), "gpu build");
   PG_GB_TRY(flags.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
   PG_GB_TRY(cudaMemsetAsync(flags.get(), 0, std::max<size_t>(n_int, 1) * 4, s), "gpu build");
   PG_GB_TRY(cost.ensure(std::max<size_t>(n_int, 1) * 32), "gpu build");
@@ -623,29 +895,29 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   PG_GB_TRY(wide_k.ensure(std::max<size_t>(n_int, 1)), "gpu build");
   PG_GB_TRY(tri_count.ensure(std::max<size_t>(n_int, 1) * 4), "gpu build");
   if (n_int > 0) {
-    Status sp = ploc_tree(t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(),
-                          right.as<uint32_t>(), parent.as<uint32_t>(), s);
+    Status sp = ploc_tree(item_box.as<box>(), m, left.as<uint32_t>(), right.as<uint32_t>(),
+                          parent.as<uint32_t>(), s);
     if (!sp.good()) {
       return sp;
     }
   }
-  dev::k_boxes<<<nb, bs, 0, s>>>(t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(),
+  dev::k_boxes<<<mb, bs, 0, s>>>(item_box.as<box>(), m, left.as<uint32_t>(),
                                  right.as<uint32_t>(), parent.as<uint32_t>(), boxes.as<box>(),
                                  flags.as<uint32_t>(), cost.as<float>(), how.as<uint8_t>(),
                                  wide_k.as<uint8_t>(), tri_count.as<uint32_t>());
   PG_GB_TRY(cudaGetLastError(), "boxes");
   // collapse: a wide node has at most 8 children and at least 2 binary
-  // nodes below it, so n wide nodes and n queue entries always suffice
-  PG_GB_TRY(out.nodes.ensure(nn * sizeof(WideNode)), "gpu build");
-  PG_GB_TRY(out.wide_tris.ensure(nn * 48), "gpu build");
-  PG_GB_TRY(qa.ensure(nn * sizeof(dev::Entry)), "gpu build");
-  PG_GB_TRY(qb.ensure(nn * sizeof(dev::Entry)), "gpu build");
+  // nodes below it, so m wide nodes and m queue entries always suffice
+  PG_GB_TRY(out.nodes.ensure(mm * sizeof(WideNode)), "gpu build");
+  PG_GB_TRY(out.wide_tris.ensure(mm * 48), "gpu build");
+  PG_GB_TRY(qa.ensure(mm * sizeof(dev::Entry)), "gpu build");
+  PG_GB_TRY(qb.ensure(mm * sizeof(dev::Entry)), "gpu build");
   PG_GB_TRY(counters.ensure(16), "gpu build");
   // counters: [0] wide nodes allocated, [1] triangles placed, [2] next queue
   uint32_t h_init[4] = {1, 0, 0, 0};
   PG_GB_TRY(cudaMemcpyAsync(counters.get(), h_init, 16, cudaMemcpyHostToDevice, s),
             "gpu build");
-  dev::Entry root{n > 1 ? 0u : (0u | dev::kLeafBit), 0u};
+  dev::Entry root{m > 1 ? 0u : (0u | dev::kLeafBit), 0u};
   PG_GB_TRY(cudaMemcpyAsync(qa.get(), &root, sizeof(root), cudaMemcpyHostToDevice, s),
             "gpu build");
   uint32_t n_in = 1, depth = 0;
@@ -653,16 +925,17 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   while (n_in > 0) {
     PG_GB_TRY(cudaMemsetAsync(counters.as<uint32_t>() + 2, 0, 4, s), "gpu build");
     dev::k_collapse<<<(n_in + 127) / 128, 128, 0, s>>>(
-        t9, out.perm.as<uint32_t>(), n, left.as<uint32_t>(), right.as<uint32_t>(),
-        boxes.as<box>(), how.as<uint8_t>(), wide_k.as<uint8_t>(), cur->as<dev::Entry>(), n_in,
-        nxt->as<dev::Entry>(),
-        counters.as<uint32_t>(), out.nodes.as<WideNode>(), out.wide_tris.as<float>());
+        t9, out.perm.as<uint32_t>(), item_tri.as<uint32_t>(), m, left.as<uint32_t>(),
+        right.as<uint32_t>(), boxes.as<box>(), how.as<uint8_t>(), wide_k.as<uint8_t>(),
+        cur->as<dev::Entry>(), n_in, nxt->as<dev::Entry>(), counters.as<uint32_t>(),
+        out.nodes.as<WideNode>(), out.wide_tris.as<float>());
     PG_GB_TRY(cudaGetLastError(), "collapse");
     uint32_t h[4];
     PG_GB_TRY(cudaMemcpyAsync(h, counters.get(), 16, cudaMemcpyDeviceToHost, s), "gpu build");
     PG_GB_TRY(cudaStreamSynchronize(s), "gpu build");
     n_in = h[2];
     out.n_nodes = h[0];
+    out.n_wide_tris = h[1];
     ++depth;
     std::swap(cur, nxt);
     if (depth > 4096) {

@@ -96,7 +96,7 @@ Status Renderer::render_noalloc(const path_sample_spec &spec, const path_output 
       prep_.sbvh.use_spatial_splits != (st.use_spatial_splits != 0) ||
       prep_.sbvh.traversal_per_intersect_cost != st.traversal_per_intersect_cost ||
       prep_.sbvh.target_objects != st.target_objects ||
-      prep_.gpu_built != (st.gpu_build != 0)) {
+      prep_.gpu_built != st.gpu_build) {
     return Status::err(PATH_ERR_ARGUMENT,
                        "scene not resident on this renderer: render it once with path_render");
   }

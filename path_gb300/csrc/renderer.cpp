@@ -257,7 +257,7 @@ void scene_box(const FlatScene &flat, float *lo, float *hi) {
 // The 8-wide BVH from the GPU builder; the BVH-order triangle and shading
 // arrays are gathered on the host with its permutation, as for the SBVH.
 Status Renderer::prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t version,
-                                   const std::vector<path_material> &mats) {
+                                   const std::vector<path_material> &mats, uint32_t mode) {
   prep_.valid = false;
   auto t0 = std::chrono::steady_clock::now();
   const size_t n = flat.v0.size();
@@ -274,7 +274,8 @@ Status Renderer::prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t 
   DeviceBuffer d9;
   PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, stream_), "gpu build upload");
   GpuWideBVH g;
-  Status sb = gpu_build_wide(d9.as<float>(), (uint32_t)n, prep_.lo, prep_.hi, stream_, g);
+  Status sb = gpu_build_wide(d9.as<float>(), (uint32_t)n, prep_.lo, prep_.hi, mode == 2, stream_,
+                             g);
   if (!sb.good()) {
     return sb;
   }
@@ -299,7 +300,7 @@ Status Renderer::prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t 
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   prep_.scene_id = id;
   prep_.scene_version = version;
-  prep_.gpu_built = true;
+  prep_.gpu_built = mode;
   // BVH-order triangles and shading data; materials and lights
   PG_TRY_CUDA(st_tris_.ensure(n * 48), "staging");
   PG_TRY_CUDA(st_data_.ensure(n * 48), "staging");
@@ -405,7 +406,7 @@ Status Renderer::prepare_scene(const FlatScene &flat, uint64_t id, uint64_t vers
     return Status::ok();
   }
   prep_.valid = false;
-  prep_.gpu_built = false;
+  prep_.gpu_built = 0;
   auto t0 = std::chrono::steady_clock::now();
   prep_.bvh = build_sbvh(flat.v0.data(), flat.v1.data(), flat.v2.data(), flat.v0.size(), sbvh);
   prep_.wide = build_wide(prep_.bvh);
@@ -537,6 +538,9 @@ Status check_settings(const path_settings &s) {
   if (s.wavefront_slots_log2 != 0 && (s.wavefront_slots_log2 < 10 || s.wavefront_slots_log2 > 26)) {
     return Status::err(PATH_ERR_ARGUMENT, "wavefront_slots_log2 must be 0 or in [10, 26]");
   }
+  if (s.gpu_build > 2) {
+    return Status::err(PATH_ERR_ARGUMENT, "gpu_build must be 0, 1 or 2");
+  }
   if (s.trace_staged_nodes > kMaxStagedNodes) {
     return Status::err(PATH_ERR_ARGUMENT, "trace_staged_nodes must be at most 512");
   }
@@ -606,8 +610,8 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   sb.use_spatial_splits = st.use_spatial_splits != 0;
   sb.traversal_per_intersect_cost = st.traversal_per_intersect_cost;
   sb.target_objects = st.target_objects;
-  const bool gpu_build = st.gpu_build != 0;
-  if (gpu_build && st.traversal != PATH_TRAVERSAL_WIDE8) {
+  const uint32_t gpu_build = st.gpu_build;
+  if (gpu_build != 0 && st.traversal != PATH_TRAVERSAL_WIDE8) {
     return Status::err(PATH_ERR_UNSUPPORTED, "the GPU builder makes the 8-wide BVH only");
   }
   bool rebuilt = !(prep_.valid && prep_.scene_id == scene.id &&
@@ -616,9 +620,9 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
                    prep_.sbvh.use_spatial_splits == sb.use_spatial_splits &&
                    prep_.sbvh.traversal_per_intersect_cost == sb.traversal_per_intersect_cost &&
                    prep_.sbvh.target_objects == sb.target_objects);
-  if (rebuilt && gpu_build) {
+  if (rebuilt && gpu_build != 0) {
     FlatScene flat = flatten(scene);
-    Status sp = prepare_scene_gpu(flat, scene.id, scene.version, scene.materials);
+    Status sp = prepare_scene_gpu(flat, scene.id, scene.version, scene.materials, gpu_build);
     if (!sp.good()) {
       return sp;
     }
@@ -1070,7 +1074,7 @@ Status Renderer::intersect(const float *tris, uint32_t n_tris, const float *rays
     if (st.traversal != PATH_TRAVERSAL_WIDE8) {
       return Status::err(PATH_ERR_UNSUPPORTED, "the GPU builder makes the 8-wide BVH only");
     }
-    Status sp = prepare_scene_gpu(flat, 0, 0, mats);
+    Status sp = prepare_scene_gpu(flat, 0, 0, mats, st.gpu_build);
     if (!sp.good()) {
       return sp;
     }

@@ -83,7 +83,8 @@ struct PreparedScene {
   BinaryBVH bvh;
   WideBVH wide;
   std::vector<uint32_t> orig_to_bvh; // inverse of bvh.permutation
-  bool gpu_built = false;            // wide BVH from the GPU builder (no binary BVH)
+  uint32_t gpu_built = 0;            // wide BVH from the GPU builder (path_settings.gpu_build
+                                     // mode; no binary BVH), 0 = host SBVH
   uint32_t n_wide_nodes = 0;
   float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}; // scene box
   uint32_t n_tris = 0, n_lights = 0;
@@ -114,7 +115,7 @@ struct PreparedBatch {
   bool valid = false;
   std::vector<std::array<uint64_t, 3>> key; // (scene id, version, material version)
   SBVHSettings sbvh;
-  bool gpu_build = false;
+  uint32_t gpu_build = 0;
   std::vector<uint32_t> root, light_off, n_lights, n_tris;
   uint32_t n_wide_nodes = 0;
   uint64_t total_tris = 0;
@@ -166,7 +167,7 @@ private:
   void stage_materials(const FlatScene &flat, const std::vector<path_material> &mats);
   Status refresh_materials(const Scene &scene, uint64_t *bytes);
   Status prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t version,
-                           const std::vector<path_material> &mats);
+                           const std::vector<path_material> &mats, uint32_t mode);
   Status prepare_sobol(uint32_t dim_bound, uint32_t count);
   void fill_params(RenderParams &p) const;
   Status traversal_fits(const path_settings &st) const;
@@ -217,7 +218,7 @@ private:
   // batched render
   Status check_batch(const std::vector<BatchItem> &items, const path_settings &st) const;
   Status prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb,
-                       bool gpu_build);
+                       uint32_t gpu_build);
   Status run_batch(const std::vector<BatchItem> &items, const path_settings &st,
                    const path_batch_tuning &tu, uint64_t sample_limit, bool with_images,
                    float *kernel_ms, uint32_t *launches);

@@ -237,6 +237,15 @@ bool read_u32(const YNode *n, uint32_t &out, std::string &err) {
   return true;
 }
 
+// a boolean (false / true = 0 / 1) or an unsigned number
+bool read_mode(const YNode *n, uint32_t &out, std::string &err) {
+  if (n && (n->scalar == "true" || n->scalar == "True" || n->scalar == "false" ||
+            n->scalar == "False")) {
+    return read_bool(n, out, err);
+  }
+  return read_u32(n, out, err);
+}
+
 bool read_f32(const YNode *n, float &out, std::string &err) {
   if (!n) {
     return true;
@@ -386,7 +395,7 @@ bool settings_from_yaml_text(const std::string &text, path_settings &s,
         !read_u32(get(g, "trace_min_blocks"), s.trace_min_blocks, err) ||
         !read_bool(get(g, "count_work"), s.count_work, err) ||
         !read_bool(get(g, "time_kernels"), s.time_kernels, err) ||
-        !read_bool(get(g, "gpu_build"), s.gpu_build, err) ||
+        !read_mode(get(g, "gpu_build"), s.gpu_build, err) ||
         !read_u32(get(g, "wavefront_slots_log2"), s.wavefront_slots_log2, err) ||
         !read_u32(get(g, "trace_staged_nodes"), s.trace_staged_nodes, err)) {
       return false;

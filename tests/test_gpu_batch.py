@@ -112,7 +112,8 @@ def test_batch_autotune_returns_a_shape_that_renders_the_same(lib):
         assert np.array_equal(bits(out), bits(ref))
 
 
-def test_batch_with_gpu_built_bvhs_renders_the_same_images(lib):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_with_gpu_built_bvhs_renders_the_same_images(lib, mode):
     s = scenes.path_settings(6, "wide")
     items = _small_batch(11, 5)
     batch, outs, refs = [], [], []
@@ -123,7 +124,7 @@ def test_batch_with_gpu_built_bvhs_renders_the_same_images(lib):
         refs.append(_single(sc, s, spp, w, h, f2w))
         batch.append((sc, api.SquareImage(w, h, f2w), out, spp))
     g = s.copy()
-    g.gpu_build = 1
+    g.gpu_build = mode
     api.Renderer().render_batch(batch, g)
     # the same closest hits up to exact-distance ties, which the two BVHs
     # may break with different triangles

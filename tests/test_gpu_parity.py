@@ -515,16 +515,18 @@ def test_edge_cases_match_oracle(lib, oracle, case):
     assert rel_rmse(wave, ref) <= RMSE_TOL if np.linalg.norm(ref) > 0 else not wave.any()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("n", [1, 2, 3, 37, 5000])
-def test_gpu_built_wide_bvh_finds_the_order_independent_closest_hit(lib, oracle, n):
-    """The GPU builder (linear BVH collapsed to 8-wide): the same closest hit
-    as a brute-force search, ties by smallest BVH-order index."""
+def test_gpu_built_wide_bvh_finds_the_order_independent_closest_hit(lib, oracle, n, mode):
+    """The GPU builder (PLOC collapsed to 8-wide; mode 2 after splitting the
+    long thin triangles of this soup into clipped references): the same
+    closest hit as a brute-force search, ties by smallest BVH-order index."""
     rng = np.random.default_rng(n)
     tris = rng.uniform(-1, 1, (n, 9)).astype(np.float32)
     rays = _random_rays(rng, -1, 1, 3000)
     s = api.Settings()
     s.traversal = 1
-    s.gpu_build = 1
+    s.gpu_build = mode
     got, gt = api.Renderer().intersect(tris, rays, s)
     want, wt = ol.loop_all(tris, rays)
     hit = want >= 0
@@ -534,8 +536,9 @@ def test_gpu_built_wide_bvh_finds_the_order_independent_closest_hit(lib, oracle,
     assert np.all((want == got) | (hit & tie))
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("case", ["cornell", "large_mesh"])
-def test_gpu_built_bvh_renders_the_same_image(lib, case):
+def test_gpu_built_bvh_renders_the_same_image(lib, case, mode):
     """Images through the GPU-built BVH equal those through the host SBVH
     (both through the order-independent 8-wide traversal)."""
     if case == "cornell":
@@ -546,12 +549,12 @@ def test_gpu_built_bvh_renders_the_same_image(lib, case):
     s.kernel_approach = 1
     f2w = scenes.cornell_camera(w, h)
     host_built = _render_gpu(sc, s, spp, w, h, f2w)
-    s.gpu_build = 1
+    s.gpu_build = mode
     r = api.Renderer()
     out = np.zeros((h, w, 3), np.float32)
     r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), out, sc, spp, s)
     st = r.stats()
     assert st["device_status"] == 0
-    print(f"{case}: gpu build {1e3 * st['bvh_build_seconds']:.1f} ms, "
+    print(f"{case} mode {mode}: gpu build {1e3 * st['bvh_build_seconds']:.1f} ms, "
           f"{st['num_wide_nodes']} wide nodes, rel RMSE {rel_rmse(out, host_built):.2e}")
     assert rel_rmse(out, host_built) <= RMSE_TOL
