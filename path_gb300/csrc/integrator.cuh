@@ -514,6 +514,83 @@ __device__ __forceinline__ void warp_triangles(const RenderParams &P, WideWalk &
   }
 }
 
+// Per-warp shared-memory scratch of warp_triangles_shared: every lane's ray,
+// written when the lane takes the ray (the w components are not read), and
+// every lane's closest-hit key of the current step.
+struct WarpTriScratch {
+  float4 o[32];
+  float4 d[32];
+  unsigned long long key[32];
+};
+
+// warp_triangles with the rays read from shared memory instead of six
+// shuffles per round, and the per-lane minimum taken by 64-bit shared-memory
+// atomicMin from the items that hit instead of a segmented shuffle
+// reduction over every item.  The keys and the fold are those of
+// warp_triangles, so the result is the same bit for bit.  All 32 lanes call
+// this; sh.o / sh.d hold the ray of every lane with triangles.
+template <bool kCount>
+__device__ __forceinline__ void warp_triangles_shared(const RenderParams &P, WideWalk &w,
+                                                      uint32_t tri_base, uint32_t tmask,
+                                                      uint32_t lane, Counts &cnt,
+                                                      WarpTriScratch &sh) {
+  const uint32_t c = __popc(tmask);
+  uint32_t incl = c;
+#pragma unroll
+  for (uint32_t off = 1; off < 32; off <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, off);
+    if (lane >= off) {
+      incl += v;
+    }
+  }
+  const uint32_t total = __shfl_sync(kFull, incl, 31);
+  if (total == 0) {
+    return;
+  }
+  const uint32_t excl = incl - c;
+  sh.key[lane] = ~0ull;
+  __syncwarp();
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t g = base + lane;
+    // owner: the first lane whose inclusive count exceeds g
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t step = 16; step > 0; step >>= 1) {
+      if (__shfl_sync(kFull, incl, pos + step - 1) <= g) {
+        pos += step;
+      }
+    }
+    const uint32_t o_excl = __shfl_sync(kFull, excl, pos);
+    const uint32_t o_mask = __shfl_sync(kFull, tmask, pos);
+    const uint32_t o_base = __shfl_sync(kFull, tri_base, pos);
+    if (g < total) {
+      const float4 o = sh.o[pos], d = sh.d[pos];
+      ray r;
+      r.o = mk(o.x, o.y, o.z);
+      r.d = mk(d.x, d.y, d.z);
+      const uint32_t k = o_base + nth_set_bit(o_mask, g - o_excl);
+      Hit h = no_hit();
+      wide_tri(P, r, k, h);
+      if (h.ok) {
+        atomicMin(&sh.key[pos], ((unsigned long long)__float_as_uint(h.t) << 32) |
+                                    (unsigned long long)((h.idx << 1) | (h.back ? 1u : 0u)));
+      }
+      if (kCount) {
+        ++cnt.tris;
+      }
+    }
+  }
+  __syncwarp();
+  const unsigned long long mine = sh.key[lane];
+  if (mine != ~0ull) {
+    const uint32_t lo = (uint32_t)mine;
+    fold_min(w.best, __uint_as_float((uint32_t)(mine >> 32)), (lo & 1u) != 0, lo >> 1);
+    if (shadow_settled(w)) {
+      w.done = true;
+    }
+  }
+}
+
 // one traversal step of a lone lane: a node and its triangles
 template <bool kCount>
 __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,

@@ -192,7 +192,9 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
 template <bool kCount, int kMinBlocks, bool kStaged>
 __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W) {
   extern __shared__ uint4 s_top[];
+  __shared__ WarpTriScratch s_tri[8];
   const uint32_t lane = threadIdx.x & 31;
+  WarpTriScratch &sh = s_tri[threadIdx.x >> 5];
   const uint32_t n_top = kStaged ? W.P.n_staged : 0u;
   if constexpr (kStaged) {
     for (uint32_t i = threadIdx.x; i < 5 * n_top; i += blockDim.x) {
@@ -226,6 +228,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
           const bool light = (entry & 1u) != 0;
           const float4 o = W.o[slot];
           const float4 d = light ? W.ld[slot] : W.d[slot];
+          sh.o[lane] = o;
+          sh.d[lane] = d;
           ray r;
           r.o = mk(o.x, o.y, o.z);
           r.d = mk(d.x, d.y, d.z);
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
     if (have && !w.done) {
       wide_node<kCount, kStaged>(W.P, w, st_base, st_bits, cnt, tri_base, tmask, s_top, n_top);
     }
-    warp_triangles<kCount>(W.P, w, tri_base, tmask, lane, cnt);
+    warp_triangles_shared<kCount>(W.P, w, tri_base, tmask, lane, cnt, sh);
     if (have && w.done) {
       const uint32_t slot = entry >> 1;
       ((entry & 1u) ? W.hit_light : W.hit_ext)[slot] = pack_hit(w.best);
@@ -549,6 +553,13 @@ void *trace_kernel(uint32_t min_blocks, bool staged) {
 }
 
 size_t staged_bytes(uint32_t n_staged) { return (size_t)n_staged * sizeof(WideNode); }
+
+// the staged nodes and the static per-warp scratch together can pass the
+// default 48 KB of shared memory per CTA
+cudaError_t allow_staged(void *k, uint32_t n_staged) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)staged_bytes(n_staged));
+}
 } // namespace
 
 int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting, uint32_t n_staged) {
@@ -556,7 +567,8 @@ int wavefront_trace_blocks_per_sm(uint32_t min_blocks, bool counting, uint32_t n
   const bool staged = n_staged > 0 && (min_blocks == 0 || min_blocks == 4);
   void *k = counting ? trace_kernel<true>(min_blocks, staged)
                      : trace_kernel<false>(min_blocks, staged);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256,
+  if ((staged && allow_staged(k, n_staged) != cudaSuccess) ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256,
                                                     staged ? staged_bytes(n_staged) : 0) !=
           cudaSuccess ||
       n < 1) {
@@ -571,6 +583,12 @@ cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
   void *k = counting ? trace_kernel<true>(min_blocks, staged)
                      : trace_kernel<false>(min_blocks, staged);
   void *args[] = {const_cast<WaveParams *>(&w)};
+  if (staged) {
+    const cudaError_t e = allow_staged(k, w.P.n_staged);
+    if (e != cudaSuccess) {
+      return e;
+    }
+  }
   return cudaLaunchKernel(k, dim3(trace_grid), dim3(256), args,
                           staged ? staged_bytes(w.P.n_staged) : 0, s);
 }
