@@ -523,6 +523,105 @@ def run_cache(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def batch_time_to_rmse(r, batch, settings, refs, cfg, max_frames, base, tuning, target=0.02):
+    """time_to_rmse over a batch: frames of 4 new samples of every item (one
+    path_render_batch or path_render_batch_cached call each), accumulated in
+    FP64, until the relative RMSE of the whole batch (all items' pixels)
+    against refs is <= target."""
+    import torch
+    from path_gb300 import api, scenes
+    outs = [torch.zeros((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in batch]
+    accs = [torch.zeros_like(ref) for ref in refs]
+    ref_norm = float(sum(float(torch.sum(ref * ref)) for ref in refs)) ** 0.5
+    cache = api.RadianceCache(seed=1) if cfg is not None else None
+    wall, frames, err, curve = 0.0, 0, None, []
+
+    def frame(offset):
+        items = [(sc, api.SquareImage(w, h, scenes.cornell_camera(w, h), sample_offset=offset),
+                  o, 4) for (sc, w, h, _), o in zip(batch, outs)]
+        if cache is None:
+            r.render_batch(items, settings, tuning)
+        else:
+            r.render_batch_cached(cache, items, settings, tuning,
+                                  cache_depth=cfg["cache_depth"], train_paths=cfg["train_paths"],
+                                  train_steps=cfg["train_steps"])
+
+    while frames < max_frames:
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        frame(base + 4 * frames)
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t
+        frames += 1
+        sq = 0.0
+        for acc, o, ref in zip(accs, outs, refs):
+            acc += o.double()
+            d = acc / frames - ref
+            sq += float(torch.sum(d * d))
+        err = sq ** 0.5 / ref_norm
+        if frames in (1, 2, 4, 8, 16, 32, 64, 128, 256) or err <= target:
+            curve.append((frames, round(wall, 4), round(err, 5)))
+        if err <= target:
+            break
+    res = {"frames": frames, "seconds": wall, "rel_rmse": err,
+           "reached": err is not None and err <= target, "curve": curve}
+    if cfg is not None:
+        res["cache"] = (
+            "one cache for the batch (a cell per item), hash grid 16x2x2^19, MLP 48-64x5-3 "
+            f"BF16 tcgen05, Adam 1e-2, paths end into the cache at vertex {cfg['cache_depth']}, "
+            f"{cfg['train_paths']} records (random items) x {cfg['train_steps']} steps per frame")
+    return res
+
+
+def run_batched_cache(args, rank, world, local_rank):
+    """Time to 0.02 relative RMSE of the batched render, plain against the
+    batched + cache form (path_render_batch_cached): the first
+    args.cache_scenes scenes of the batched workload in frames of 4 spp,
+    against 4096 spp per item of the plain batch accumulated in FP64."""
+    import torch
+    from path_gb300 import api, scenes
+    batch = scenes.batch_scenes(args.cache_scenes, seed=0)
+    settings = scenes.path_settings(6, "wide")
+    tuning = {"slots_log2": 24}
+    r = api.Renderer()
+    t0 = time.time()
+    refs = [torch.zeros((h, w, 3), dtype=torch.float64, device="cuda") for _, w, h, _ in batch]
+    outs = [torch.zeros((h, w, 3), dtype=torch.float32, device="cuda") for _, w, h, _ in batch]
+    n_ref = 64
+    for f in range(n_ref):
+        items = [(sc, api.SquareImage(w, h, scenes.cornell_camera(w, h), sample_offset=64 + 64 * f),
+                  o, 64) for (sc, w, h, _), o in zip(batch, outs)]
+        r.render_batch(items, settings, tuning)
+        for ref, o in zip(refs, outs):
+            ref += o.double()
+    refs = [ref / n_ref for ref in refs]
+    ref_s = time.time() - t0
+    base = 64 + 4096 + 64
+    plain = batch_time_to_rmse(r, batch, settings, refs, None, args.max_frames, base, tuning)
+    cfg = {"cache_depth": args.cache_depth, "train_paths": args.train_paths,
+           "train_steps": args.train_steps}
+    cached = batch_time_to_rmse(r, batch, settings, refs, cfg, args.max_frames, base, tuning)
+    control = batch_time_to_rmse(r, batch, settings, refs, dict(cfg, train_steps=0),
+                                 args.max_frames, base, tuning)
+    pixels = sum(w * h for _, w, h, _ in batch)
+    line = {
+        "metric": "seconds to 0.02 relative RMSE (batch)", "unit": "s",
+        "higher_is_better": False,
+        "value": cached["seconds"] if cached["reached"] else None, "n_gpus": 1,
+        "dtype": "f32 render, bf16 cache MLP", "data": "synthetic",
+        "config": {"workload": f"batched + cache: the first {len(batch)} scenes of the batched "
+                               f"workload ({pixels} pixels), depth 6, 4-spp frames; reference "
+                               "4096 spp per item, FP64 sum",
+                   "tuning": tuning},
+        "ratio_cached_over_plain": (cached["seconds"] / plain["seconds"]
+                                    if plain["reached"] and cached["reached"] else None),
+        "target_ratio": 0.25, "plain": plain, "cached": cached, "cached_untrained": control,
+        "reference_seconds": ref_s,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_sobol_draws(args, rank):
     """Cost of the integrator's Sobol draws read from the table against the
     same values formed from the direction vectors in registers
@@ -552,7 +651,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_mesh",
-                    choices=["large_mesh", "cornell", "batched", "cache", "sobol_draws"])
+                    choices=["large_mesh", "cornell", "batched", "cache", "batched_cache",
+                             "sobol_draws"])
     ap.add_argument("--max-frames", type=int, default=400,
                     help="cache workload: frames before giving up on the error target")
     ap.add_argument("--cache-depth", type=int, default=2,
@@ -566,6 +666,8 @@ def main():
     ap.add_argument("--no-tuned-cache", action="store_true",
                     help="cache workload: skip the tuned cache configuration")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: scene count")
+    ap.add_argument("--cache-scenes", type=int, default=16,
+                    help="batched_cache workload: scene count")
     ap.add_argument("--traversal", default="wide", choices=["wide", "binary"])
     ap.add_argument("--approach", default="streaming", choices=["streaming", "mega"],
                     help="wavefront (streaming) or megakernel integration")
@@ -618,6 +720,9 @@ def main():
         return
     if args.workload == "cache":
         run_cache(args, rank, world, local_rank)
+        return
+    if args.workload == "batched_cache":
+        run_batched_cache(args, rank, world, local_rank)
         return
     if args.workload == "sobol_draws":
         run_sobol_draws(args, rank)

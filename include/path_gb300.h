@@ -326,6 +326,11 @@ path_status path_cache_create(uint32_t seed, float learning_rate, path_cache **o
 void path_cache_destroy(path_cache *cache);
 /* the scene box the hash grid covers */
 path_status path_cache_set_bounds(path_cache *cache, const float *lo, const float *hi);
+/* positions in batch-cell coordinates, as path_render_batch_cached sets them:
+ * a position p of item i is (p - lo_i) / (hi_i - lo_i) (its scene's vertex
+ * box onto [0, 1]^3) plus 2 * (i % 16, i / 16 % 16, i / 256); every cell has
+ * grid vertices of its own.  path_cache_set_bounds returns to one scene box. */
+path_status path_cache_use_batch_cells(path_cache *cache);
 /* radiance [n][3] of n queries (host buffers) */
 path_status path_cache_query(path_cache *cache, const float *queries, uint32_t n, float *out);
 /* one training step on n records (host buffer): with apply_update 0 only the
@@ -364,13 +369,16 @@ path_status path_cache_frame_queries(const path_renderer *renderer, uint32_t max
 /* ---- batched render (GB300 addition; the reference renders one scene per
  * call) ---- */
 /* One image of a batch: a scene, its square-image camera, samples per pixel
- * and where the image goes (FLOAT_RGB or BGRA, host or device memory). */
+ * and where the image goes (FLOAT_RGB or BGRA, host or device memory);
+ * sample_offset: the image takes Sobol samples [sample_offset, sample_offset
+ * + samples_per), as path_sample_spec.sample_offset (progressive frames). */
 typedef struct {
   const path_scene *scene;
   uint32_t x_dim, y_dim;
   float film_to_world[12];
   uint32_t samples_per;
   path_output output;
+  uint32_t sample_offset;
 } path_batch_item;
 
 /* Launch shape of a batched render.  Every choice gives the same images
@@ -395,6 +403,17 @@ typedef struct {
 path_status path_render_batch(path_renderer *renderer, const path_batch_item *items,
                               uint32_t n_items, const path_settings *settings,
                               const path_batch_tuning *tuning, double *seconds);
+/* One frame of every item with one radiance cache for the whole batch (the
+ * cached form of path_render_batch; at most 4096 items): item i's positions
+ * take cell i of the cache (path_cache_use_batch_cells), paths end into the
+ * cache at vertex cache_depth as in path_render_cached, and train_steps Adam
+ * steps follow on train_paths records, each traced from a random item. */
+path_status path_render_batch_cached(path_renderer *renderer, path_cache *cache,
+                                     const path_batch_item *items, uint32_t n_items,
+                                     const path_settings *settings,
+                                     const path_batch_tuning *tuning, uint32_t cache_depth,
+                                     uint32_t train_paths, uint32_t train_steps,
+                                     double *seconds);
 /* Times candidate launch shapes on the batch's first samples (at most
  * sample_budget of them, 0 = 2^27; no image output) and returns the
  * fastest. */

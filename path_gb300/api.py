@@ -362,6 +362,7 @@ class Renderer:
             arr[k].film_to_world[:] = [float(v) for v in spec.film_to_world]
             arr[k].samples_per = int(spp)
             arr[k].output = Renderer._output_c(output)
+            arr[k].sample_offset = int(getattr(spec, "sample_offset", 0))
         return arr
 
     def render_batch(self, items, settings, tuning=None):
@@ -379,6 +380,24 @@ class Renderer:
                                                  ctypes.byref(settings.raw),
                                                  None if t is None else ctypes.byref(t),
                                                  ctypes.byref(secs)))
+        return secs.value
+
+    def render_batch_cached(self, cache, items, settings, tuning=None, cache_depth=2,
+                            train_paths=1 << 16, train_steps=4):
+        """One frame of a batch with one radiance cache for all its items
+        (path_render_batch_cached); items as for render_batch.  Returns
+        seconds."""
+        arr = self._batch_c(items)
+        t = None
+        if tuning is not None:
+            t = capi.BatchTuning()
+            for k, v in tuning.items():
+                setattr(t, k, int(v))
+        secs = ctypes.c_double()
+        capi.check(capi.load().path_render_batch_cached(
+            self._h, cache.handle, arr, len(items), ctypes.byref(settings.raw),
+            None if t is None else ctypes.byref(t), int(cache_depth), int(train_paths),
+            int(train_steps), ctypes.byref(secs)))
         return secs.value
 
     def autotune_batch(self, items, settings, sample_budget=0):
@@ -571,6 +590,10 @@ class RadianceCache:
         lo = np.asarray(lo, np.float32)
         hi = np.asarray(hi, np.float32)
         capi.check(capi.load().path_cache_set_bounds(self._h, _fptr(lo), _fptr(hi)))
+
+    def use_batch_cells(self):
+        """Positions in batch-cell coordinates (path_cache_use_batch_cells)."""
+        capi.check(capi.load().path_cache_use_batch_cells(self._h))
 
     def query(self, queries):
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 12)

@@ -61,7 +61,8 @@ class Output(ctypes.Structure):
 
 class BatchItem(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("x_dim", c_u32), ("y_dim", c_u32),
-                ("film_to_world", c_f32 * 12), ("samples_per", c_u32), ("output", Output)]
+                ("film_to_world", c_f32 * 12), ("samples_per", c_u32), ("output", Output),
+                ("sample_offset", c_u32)]
 
 
 class BatchTuning(ctypes.Structure):
@@ -136,6 +137,7 @@ SIGNATURES = {
     "path_cache_create": (ctypes.c_int, [c_u32, c_f32, ctypes.POINTER(_P)]),
     "path_cache_destroy": (None, [_P]),
     "path_cache_set_bounds": (ctypes.c_int, [_P, _PF, _PF]),
+    "path_cache_use_batch_cells": (ctypes.c_int, [_P]),
     "path_cache_query": (ctypes.c_int, [_P, _PF, c_u32, _PF]),
     "path_cache_train": (ctypes.c_int, [_P, _PF, c_u32, c_u32, _PF]),
     "path_cache_access": (ctypes.c_int, [_P, _PF, _PF, _PF, _PF, c_u32]),
@@ -154,6 +156,10 @@ SIGNATURES = {
                                          ctypes.POINTER(PathSettings),
                                          ctypes.POINTER(BatchTuning),
                                          ctypes.POINTER(ctypes.c_double)]),
+    "path_render_batch_cached": (ctypes.c_int, [_P, _P, ctypes.POINTER(BatchItem), c_u32,
+                                                ctypes.POINTER(PathSettings),
+                                                ctypes.POINTER(BatchTuning), c_u32, c_u32,
+                                                c_u32, ctypes.POINTER(ctypes.c_double)]),
     "path_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(BatchItem), c_u32,
                                            ctypes.POINTER(PathSettings), ctypes.c_uint64,
                                            ctypes.POINTER(BatchTuning)]),

@@ -17,6 +17,7 @@
 // by time alone.
 #include "renderer.h"
 #include "gpu_build.h"
+#include "cache_host.h"
 
 #include <omp.h>
 
@@ -314,8 +315,10 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
   batch_.light_off.assign(n, 0);
   batch_.n_lights.assign(n, 0);
   batch_.n_tris.assign(n, 0);
+  batch_.box.assign(n, {0.f, 0.f, 0.f, 0.f, 0.f, 0.f});
   for (size_t i = 0; i < n; ++i) {
     const size_t f = first_of[i];
+    scene_box(flats[f], batch_.box[i].data(), batch_.box[i].data() + 3);
     batch_.root[i] = node_off[f];
     batch_.light_off[i] = light_off[f];
     batch_.n_lights[i] = (uint32_t)flats[f].light_v0.size();
@@ -364,12 +367,21 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
     b.x_dim = it.x_dim;
     b.y_dim = it.y_dim;
     b.spp = it.spp;
+    b.sample_offset = it.sample_offset;
     b.root = batch_.root[i];
     b.light_off = batch_.light_off[i];
     b.n_lights = st.light_sampler == PATH_LIGHT_RANDOM_TRIANGLE ? batch_.n_lights[i] : 0u;
+    for (int a = 0; a < 3; ++a) {
+      b.cache_lo[a] = batch_.box[i][a];
+      b.cache_inv[a] = 1.f / std::max(batch_.box[i][3 + a] - batch_.box[i][a], 1e-6f);
+    }
+    b.cache_cell = (uint32_t)i;
     b.first_sample = total;
     total += (unsigned long long)it.x_dim * it.y_dim * it.spp;
-    max_spp = std::max(max_spp, it.spp);
+    if ((uint64_t)it.sample_offset + it.spp > 0xffffffffull) {
+      return Status::err(PATH_ERR_ARGUMENT, "sample_offset + samples_per above 2^32 - 1");
+    }
+    max_spp = std::max(max_spp, it.sample_offset + it.spp);
     if (!make_workdiv(st.render_work_division, it.spp, it.x_dim, it.y_dim, wds[i])) {
       return Status::err(PATH_ERR_ARGUMENT, "invalid render work division settings");
     }
@@ -444,6 +456,34 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   p.status = status_.as<uint32_t>();
   p.counters = counters_.as<unsigned long long>();
+  const bool cached = cache_ != nullptr && cache_depth_ != 0;
+  if (cached) {
+    if (limit >= (1ull << 32)) {
+      return Status::err(PATH_ERR_UNSUPPORTED, "more than 2^32 samples with the cache");
+    }
+    PG_TRY_CUDA(cache_q_.ensure((size_t)limit * 48), "cache queries");
+    PG_TRY_CUDA(cache_beta_.ensure((size_t)limit * 12), "cache queries");
+    PG_TRY_CUDA(cudaMemsetAsync(cache_beta_.get(), 0, (size_t)limit * 12, stream_),
+                "cache queries");
+    cached_samples_ = limit;
+    if (cache_train_paths_ > 0) {
+      // the training paths are independent of the frame: traced on a side
+      // stream while the frame renders, once the batch's tables are resident
+      if (side_stream_ == nullptr) {
+        PG_TRY_CUDA(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
+        PG_TRY_CUDA(cudaEventCreateWithFlags(&side_done_, cudaEventDisableTiming), "event");
+      }
+      PG_TRY_CUDA(cudaEventRecord(side_done_, stream_), "event");
+      PG_TRY_CUDA(cudaStreamWaitEvent(side_stream_, side_done_, 0), "event");
+      PG_TRY_CUDA(cache_records_.ensure((size_t)cache_train_paths_ * 64), "cache records");
+      PG_TRY_CUDA(launch_nrc_paths_batch(p, b_scenes_.as<const BatchScene>(), (uint32_t)n,
+                                         cache_train_paths_, frame_counter_++, cache_depth_,
+                                         cache_records_.as<float>(), side_stream_),
+                  "cache training paths");
+      PG_TRY_CUDA(cudaEventRecord(side_done_, side_stream_), "event");
+    }
+    p.cache_depth = cache_depth_;
+  }
 
   unsigned char *base = wf_slots_.as<unsigned char>();
   WaveParams w;
@@ -474,6 +514,10 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
   w.scenes = b_scenes_.as<const BatchScene>();
   w.n_scenes = (uint32_t)n;
   w.feat = work_features(b_mat_types_, p);
+  if (cached) {
+    w.cache_q = cache_q_.as<float>();
+    w.cache_beta = cache_beta_.as<float>();
+  }
 
   uint32_t *h = wf_host_.as<uint32_t>();
   std::memset(h, 0, 64);
@@ -541,6 +585,19 @@ Status Renderer::run_batch(const std::vector<BatchItem> &items, const path_setti
     if ((uint64_t)round * k_iters > 4ull * kMaxPathVertices + limit) {
       return Status::err(PATH_ERR_DEVICE_TIMEOUT, "batch wavefront did not drain");
     }
+  }
+  if (cached) {
+    // the cache's prediction at every path's last vertex
+    PG_TRY_CUDA(cache_pred_.ensure((size_t)limit * 12), "cache predictions");
+    Status sc = cache_->infer(w.cache_q, (uint32_t)limit, cache_pred_.as<float>(), stream_,
+                              w.cache_beta);
+    if (!sc.good()) {
+      return sc;
+    }
+    PG_TRY_CUDA(launch_nrc_apply(w.sample_rgb, w.cache_beta, cache_pred_.as<float>(), limit,
+                                 stream_),
+                "cache apply");
+    nl += 2;
   }
   if (with_images) {
     // per-item sums + ReduceFloatRGB, captured as one graph
@@ -686,6 +743,79 @@ Status Renderer::render_batch(const std::vector<BatchItem> &items, const path_se
     *seconds = stats_.seconds;
   }
   return sr;
+}
+
+Status Renderer::render_batch_cached(const std::vector<BatchItem> &items,
+                                     const path_settings &st, const path_batch_tuning *tuning,
+                                     RadianceCache &cache, uint32_t cache_depth,
+                                     uint32_t train_paths, uint32_t train_steps,
+                                     double *seconds) {
+  if (cache_depth == 0 || cache_depth > 64) {
+    return Status::err(PATH_ERR_ARGUMENT, "cache_depth must be in [1, 64]");
+  }
+  if (items.size() > kMaxCacheCells) {
+    return Status::err(PATH_ERR_UNSUPPORTED, "more than 4096 items in a cached batch");
+  }
+  Status sc = check_batch(items, st);
+  if (!sc.good()) {
+    return sc;
+  }
+  Status s0 = init();
+  if (!s0.good()) {
+    return s0;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  Status sp = prepare_batch(items, sbvh_of(st), st.gpu_build);
+  if (!sp.good()) {
+    return sp;
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  // the batch's cache cells: every item's positions in a cell of its own
+  cache.set_batch_cells();
+  cache_ = &cache;
+  cache_depth_ = cache_depth;
+  cache_train_paths_ = train_steps > 0 ? train_paths : 0u;
+  stats_ = path_render_stats{};
+  float ms = 0.f;
+  uint32_t launches = 0;
+  Status sr = run_batch(items, st, resolved(tuning), ~0ull, true, &ms, &launches);
+  const bool side = cache_train_paths_ > 0;
+  cache_ = nullptr;
+  cache_depth_ = 0;
+  cache_train_paths_ = 0;
+  if (side && side_done_ != nullptr) {
+    PG_TRY_CUDA(cudaEventSynchronize(side_done_), "cache training paths");
+    PG_TRY_CUDA(cudaGetLastError(), "cache training paths");
+  }
+  if (!sr.good()) {
+    return sr;
+  }
+  if (train_paths > 0 && train_steps > 0) {
+    const uint32_t per = std::max<uint32_t>(train_paths / train_steps, 1);
+    for (uint32_t k = 0; k < train_steps; ++k) {
+      const uint32_t first = k * per;
+      if (first >= train_paths) {
+        break;
+      }
+      const uint32_t cnt = std::min<uint32_t>(per, train_paths - first);
+      Status st_train =
+          cache.train(cache_records_.as<float>() + (size_t)first * 16, cnt, nullptr);
+      if (!st_train.good()) {
+        return st_train;
+      }
+    }
+  }
+  auto t2 = std::chrono::steady_clock::now();
+  stats_.seconds = std::chrono::duration<double>(t2 - t1).count();
+  stats_.kernel_ms = ms;
+  stats_.bvh_build_seconds = batch_.build_seconds;
+  stats_.gpu_launches = launches + (side ? 1u : 0u);
+  stats_.num_wide_nodes = batch_.n_wide_nodes;
+  (void)t0;
+  if (seconds) {
+    *seconds = stats_.seconds;
+  }
+  return Status::ok();
 }
 
 Status Renderer::autotune_batch(const std::vector<BatchItem> &items, const path_settings &st,

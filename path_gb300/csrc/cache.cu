@@ -110,6 +110,23 @@ namespace dev {
 
 using tc::smem_offset;
 
+// a query position in [0, 1]^3 of the hash grid and, for a batch's cache,
+// its cell (zero otherwise)
+__device__ __forceinline__ void nrc_position(const NrcParams &C, const float *q, float *p,
+                                             uint32_t *cell) {
+  for (int a = 0; a < 3; ++a) {
+    if (C.batch) {
+      const float c = fminf(fmaxf(floorf(q[a] * 0.5f), 0.f), (float)(kCacheCellsPerAxis - 1));
+      cell[a] = (uint32_t)c;
+      p[a] = q[a] - 2.f * c;
+    } else {
+      cell[a] = 0;
+      p[a] = (q[a] - C.lo[a]) * C.inv_extent[a];
+    }
+    p[a] = fminf(fmaxf(p[a], 0.f), 1.f);
+  }
+}
+
 // hash features of levels [l0, l1) of a query's position (trilinear
 // interpolation of the 8 grid vertices per level) into in[2 (l - l0)] and
 // in[2 (l - l0) + 1]
@@ -119,10 +136,8 @@ template <uint32_t kN>
 __device__ __forceinline__ void nrc_encode_levels(const NrcParams &C, const float *q, uint32_t l0,
                                                   float *in) {
   float p[3];
-  for (int a = 0; a < 3; ++a) {
-    p[a] = (q[a] - C.lo[a]) * C.inv_extent[a];
-    p[a] = fminf(fmaxf(p[a], 0.f), 1.f);
-  }
+  uint32_t cell[3];
+  nrc_position(C, q, p, cell);
 #pragma unroll
   for (uint32_t j = 0; j < kN; ++j) {
     const uint32_t l = l0 + j;
@@ -143,7 +158,8 @@ __device__ __forceinline__ void nrc_encode_levels(const NrcParams &C, const floa
                      gz = c0[2] + ((c >> 2) & 1u);
       const float w = ((c & 1u) ? fr[0] : 1.f - fr[0]) * (((c >> 1) & 1u) ? fr[1] : 1.f - fr[1]) *
                       (((c >> 2) & 1u) ? fr[2] : 1.f - fr[2]);
-      const uint32_t idx = nrc_grid_index(gx, gy, gz, side);
+      const uint32_t idx =
+          C.batch ? nrc_batch_grid_index(gx, gy, gz, side, cell) : nrc_grid_index(gx, gy, gz, side);
       const float2 e = __ldg(C.table + (size_t)l * kNrcTable + idx);
       f0 += w * e.x;
       f1 += w * e.y;
@@ -517,9 +533,8 @@ __global__ void k_nrc_grid_backward(const __grid_constant__ NrcParams C, const f
   const float *q = records + (size_t)i * 16;
   const float *g = d_feat + (size_t)i * 32;
   float p[3];
-  for (int a = 0; a < 3; ++a) {
-    p[a] = fminf(fmaxf((q[a] - C.lo[a]) * C.inv_extent[a], 0.f), 1.f);
-  }
+  uint32_t cell[3];
+  nrc_position(C, q, p, cell);
   for (uint32_t l = 0; l < kNrcLevels; ++l) {
     const float res = C.level_res[l];
     const uint32_t side = (uint32_t)res + 1;
@@ -536,7 +551,9 @@ __global__ void k_nrc_grid_backward(const __grid_constant__ NrcParams C, const f
                      gz = c0[2] + ((c >> 2) & 1u);
       const float w = ((c & 1u) ? fr[0] : 1.f - fr[0]) * (((c >> 1) & 1u) ? fr[1] : 1.f - fr[1]) *
                       (((c >> 2) & 1u) ? fr[2] : 1.f - fr[2]);
-      float2 *e = grad_table + (size_t)l * kNrcTable + nrc_grid_index(gx, gy, gz, side);
+      float2 *e = grad_table + (size_t)l * kNrcTable +
+                  (C.batch ? nrc_batch_grid_index(gx, gy, gz, side, cell)
+                           : nrc_grid_index(gx, gy, gz, side));
       atomicAdd(&e->x, w * g[2 * l]);
       atomicAdd(&e->y, w * g[2 * l + 1]);
     }

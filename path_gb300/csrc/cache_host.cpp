@@ -88,6 +88,7 @@ RadianceCache::~RadianceCache() {
 }
 
 void RadianceCache::set_bounds(const float *lo, const float *hi) {
+  batch_ = false;
   for (int a = 0; a < 3; ++a) {
     const float ext = std::max(hi[a] - lo[a], 1e-6f);
     lo_[a] = lo[a];
@@ -103,6 +104,7 @@ NrcParams RadianceCache::params() const {
     c.lo[a] = lo_[a];
     c.inv_extent[a] = inv_ext_[a];
   }
+  c.batch = batch_ ? 1u : 0u;
   std::memcpy(c.level_res, level_res_, sizeof(level_res_));
   c.w_fwd = wfwd_.as<const unsigned char>();
   c.w_bwd = wbwd_.as<const unsigned char>();

@@ -16,6 +16,10 @@ public:
   Status init(uint32_t seed, float learning_rate);
   // scene box mapped to the unit cube of the hash grid
   void set_bounds(const float *lo, const float *hi);
+  // positions in batch-cell coordinates (a batch's cache, one cell per
+  // scene: BatchScene::cache_cell); set_bounds returns to one scene box
+  void set_batch_cells() { batch_ = true; }
+  bool batch_cells() const { return batch_; }
   NrcParams params() const;
   // out [n][3] = network(queries [n][12]) on stream s (device pointers);
   // with live ([n][3]), queries whose three live values are zero are skipped
@@ -40,6 +44,7 @@ private:
   uint64_t step_ = 0;
   float level_res_[kNrcLevels] = {};
   float lo_[3] = {}, inv_ext_[3] = {};
+  bool batch_ = false;
   DeviceBuffer table_, w_, gw_, mw_, vw_, gt_, mt_, vt_, wfwd_, wbwd_, dfeat_, scratch_, err_,
       loss_;
 };

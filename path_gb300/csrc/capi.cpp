@@ -333,6 +333,14 @@ path_status path_cache_set_bounds(path_cache *cache, const float *lo, const floa
   return PATH_OK;
 }
 
+path_status path_cache_use_batch_cells(path_cache *cache) {
+  if (!cache) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  cache->c.set_batch_cells();
+  return PATH_OK;
+}
+
 path_status path_cache_query(path_cache *cache, const float *queries, uint32_t n, float *out) {
   if (!cache || (n > 0 && (!queries || !out))) {
     return fail(PATH_ERR_ARGUMENT, "null argument");
@@ -469,6 +477,7 @@ static path_status batch_items(const path_batch_item *items, uint32_t n,
     b.x_dim = items[i].x_dim;
     b.y_dim = items[i].y_dim;
     b.spp = items[i].samples_per;
+    b.sample_offset = items[i].sample_offset;
     std::memcpy(b.f2w, items[i].film_to_world, sizeof(b.f2w));
     b.output = items[i].output;
   }
@@ -488,6 +497,26 @@ path_status path_render_batch(path_renderer *renderer, const path_batch_item *it
       return s;
     }
     return from(renderer->r.render_batch(v, *settings, tuning, seconds));
+  });
+}
+
+path_status path_render_batch_cached(path_renderer *renderer, path_cache *cache,
+                                     const path_batch_item *items, uint32_t n_items,
+                                     const path_settings *settings,
+                                     const path_batch_tuning *tuning, uint32_t cache_depth,
+                                     uint32_t train_paths, uint32_t train_steps,
+                                     double *seconds) {
+  if (!renderer || !cache || (n_items > 0 && !items) || !settings) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] {
+    std::vector<pg::BatchItem> v;
+    path_status s = batch_items(items, n_items, v);
+    if (s != PATH_OK) {
+      return s;
+    }
+    return from(renderer->r.render_batch_cached(v, *settings, tuning, cache->c, cache_depth,
+                                                train_paths, train_steps, seconds));
   });
 }
 

@@ -612,9 +612,9 @@ __device__ __forceinline__ void wide_step(const RenderParams &P, WideWalk &w,
 
 template <bool kCount>
 __device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, float tlimit,
-                          float light_target) {
+                          float light_target, uint32_t root = 0) {
   WideWalk w;
-  wide_begin(P, w, r, tlimit, light_target);
+  wide_begin(P, w, r, tlimit, light_target, root);
   uint32_t st_base[kWideStack];
   uint32_t st_bits[kWideStack];
   while (!w.done) {
@@ -624,15 +624,16 @@ __device__ Hit trace_wide(const RenderParams &P, const ray &r, Counts &cnt, floa
 }
 
 // closest hit; the binary traversal keeps the reference's order and
-// pruning exactly and ignores tlimit
+// pruning exactly and ignores tlimit; root: the wide root node (a batch
+// scene's)
 template <uint32_t kTrav, bool kCount>
 __device__ __forceinline__ Hit trace(const RenderParams &P, const ray &r, Counts &cnt,
-                                     float tlimit, float light_target) {
+                                     float tlimit, float light_target, uint32_t root = 0) {
   if (kCount) {
     ++cnt.rays;
   }
   if (kTrav == kTravWide) {
-    return trace_wide<kCount>(P, r, cnt, tlimit, light_target);
+    return trace_wide<kCount>(P, r, cnt, tlimit, light_target, root);
   }
   return trace_binary<kCount>(P, r, cnt);
 }
@@ -1185,6 +1186,28 @@ __device__ __forceinline__ LightSet lights_of(const RenderParams &P) {
   return l;
 }
 
+// the lights of one scene of a batch
+__device__ __forceinline__ LightSet lights_of(const RenderParams &P, const BatchScene &b) {
+  LightSet l;
+  l.tris = P.light_tris + 3 * (size_t)b.light_off;
+  l.cdf = P.light_cdf + b.light_off;
+  l.n = b.n_lights;
+  return l;
+}
+
+// a position of a batch scene in the coordinates of the batch's radiance
+// cache (BatchScene::cache_cell); clamped to the scene's box first, so that
+// a hit point rounded just outside it stays in the scene's own cell
+__device__ __forceinline__ f3 batch_cache_position(const BatchScene &b, f3 p) {
+  const uint32_t c = b.cache_cell;
+  const auto unit = [](float v) { return fminf(fmaxf(v, 0.f), 1.f); };
+  return mk(unit((p.x - b.cache_lo[0]) * b.cache_inv[0]) + 2.f * (float)(c % kCacheCellsPerAxis),
+            unit((p.y - b.cache_lo[1]) * b.cache_inv[1]) +
+                2.f * (float)(c / kCacheCellsPerAxis % kCacheCellsPerAxis),
+            unit((p.z - b.cache_lo[2]) * b.cache_inv[2]) +
+                2.f * (float)(c / (kCacheCellsPerAxis * kCacheCellsPerAxis)));
+}
+
 template <class R>
 __device__ bool sample_light(const LightSet &L, f3 pos, const Mat &m, f3 normal, R &rng,
                              LightSample &out) {
@@ -1264,6 +1287,7 @@ __device__ __forceinline__ float term_prob(const RenderParams &P, uint32_t iters
 struct Camera {
   const float *f2w;
   uint32_t x_dim, y_dim, spp;
+  uint32_t sample_offset; // Sobol row of sample s: s + sample_offset
 };
 
 __device__ __forceinline__ Camera camera_of(const RenderParams &P) {
@@ -1272,6 +1296,7 @@ __device__ __forceinline__ Camera camera_of(const RenderParams &P) {
   c.x_dim = P.x_dim;
   c.y_dim = P.y_dim;
   c.spp = P.spp;
+  c.sample_offset = P.sample_offset;
   return c;
 }
 
@@ -1329,12 +1354,12 @@ __device__ __forceinline__ void path_begin_cam(const RenderParams &P, const Came
                                                uint32_t rng_stride) {
   const uint32_t location = x + y * cam.x_dim;
   if constexpr (kUniform) {
-    uniform_seed(sample_idx + location * cam.spp + P.sample_offset * (cam.x_dim * cam.y_dim),
+    uniform_seed(sample_idx + location * cam.spp + cam.sample_offset * (cam.x_dim * cam.y_dim),
                  rng_words, rng_stride);
     s.rng.w = rng_words;
     s.rng.stride = rng_stride;
   } else {
-    s.rng.begin(P, sample_idx + P.sample_offset);
+    s.rng.begin(P, sample_idx + cam.sample_offset);
     s.rng.dim = fnv_hash(location) % P.init_dim_bound;
   }
   ray r;
@@ -1521,14 +1546,14 @@ __device__ __forceinline__ bool path_continues(const RenderParams &P, S &s, bool
 template <uint32_t kTrav, bool kCount, class S>
 __device__ __forceinline__ void step_hits(const RenderParams &P, const S &s,
                                           bool first, uint32_t x, Counts &cnt, Hit &lh,
-                                          Hit &nh) {
+                                          Hit &nh, uint32_t root = 0) {
   lh = no_hit();
   nh = no_hit();
   if (s.has_light) {
     ray lr;
     lr.o = s.o;
     lr.d = s.ld;
-    lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target), s.light_target);
+    lh = trace<kTrav, kCount>(P, lr, cnt, light_bound(s.light_target), s.light_target, root);
   }
   if (first && P.initial_idx != nullptr) {
     nh.t = 1.f;
@@ -1539,7 +1564,7 @@ __device__ __forceinline__ void step_hits(const RenderParams &P, const S &s,
     ray r;
     r.o = s.o;
     r.d = s.d;
-    nh = trace<kTrav, kCount>(P, r, cnt, PG_INF, -PG_INF);
+    nh = trace<kTrav, kCount>(P, r, cnt, PG_INF, -PG_INF, root);
   }
 }
 

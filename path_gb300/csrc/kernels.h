@@ -84,9 +84,18 @@ struct BatchScene {
   uint32_t x_dim, y_dim, spp;
   uint32_t root;               // wide-node index of the scene's root
   uint32_t light_off, n_lights; // its emissive triangles in the light table
-  uint32_t pad[2];
+  // radiance-cache coordinates of a batch with one cache: a position p of
+  // this scene is (p - cache_lo) * cache_inv (its box onto [0, 1]^3) plus
+  // twice the cell (cache_cell % 16, cache_cell / 16 % 16, cache_cell / 256)
+  float cache_lo[3], cache_inv[3];
+  uint32_t cache_cell;
+  uint32_t sample_offset;          // Sobol row of its sample s: s + sample_offset
   unsigned long long first_sample; // global id of its first sample
 };
+
+// a batch item's radiance-cache cell: up to 16^3
+constexpr uint32_t kCacheCellsPerAxis = 16;
+constexpr uint32_t kMaxCacheCells = kCacheCellsPerAxis * kCacheCellsPerAxis * kCacheCellsPerAxis;
 
 // wavefront render state (device pointers); slot arrays hold PathState
 struct WaveParams {
@@ -157,6 +166,12 @@ cudaError_t launch_wavefront_sum(const RenderParams &p, const float *sample_rgb,
 // radiance, pad)
 cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, uint32_t depth,
                              float *records, cudaStream_t s);
+// the same over a batch: each path takes a random scene of scenes[0..n_scenes)
+// (its camera, root and lights) and records its position in the scene's
+// cache cell
+cudaError_t launch_nrc_paths_batch(const RenderParams &p, const BatchScene *scenes,
+                                   uint32_t n_scenes, uint32_t n, uint32_t frame,
+                                   uint32_t depth, float *records, cudaStream_t s);
 // sample_rgb[i] += beta[i] * max(pred[i], 0) for the n samples
 cudaError_t launch_nrc_apply(float *sample_rgb, const float *beta, const float *pred,
                              size_t n, cudaStream_t s);

@@ -51,9 +51,20 @@ __host__ __device__ inline uint32_t nrc_grid_index(uint32_t x, uint32_t y, uint3
   return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (kNrcTable - 1);
 }
 
+// A batch's cache: positions arrive as x in [0, 1]^3 plus twice an integer
+// cell (one cell per scene of the batch); the cell offsets the grid vertex
+// coordinates so that every scene has vertices of its own, all hashed.
+__host__ __device__ inline uint32_t nrc_batch_grid_index(uint32_t x, uint32_t y, uint32_t z,
+                                                         uint32_t side, const uint32_t *cell) {
+  return ((x + side * cell[0]) ^ ((y + side * cell[1]) * 2654435761u) ^
+          ((z + side * cell[2]) * 805459861u)) &
+         (kNrcTable - 1);
+}
+
 struct NrcParams {
   const float2 *table;        // [levels][kNrcTable] feature pairs
   float lo[3], inv_extent[3]; // scene box: position -> [0, 1]^3
+  uint32_t batch;             // positions in batch-cell coordinates (lo, inv_extent unused)
   float level_res[kNrcLevels];
   const unsigned char *w_fwd; // BF16 [out][in] K-major tiles (tc.cuh layout)
   const unsigned char *w_bwd; // BF16 [in][out] K-major tiles

@@ -28,8 +28,11 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   return x;
 }
 
+// scenes != nullptr: a batch; each path takes a random scene of it and
+// records its positions in that scene's cell of the cache
 template <bool kUniform>
-__global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_t n,
+__global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, const BatchScene *scenes,
+                                                   uint32_t n_scenes, uint32_t n,
                                                    uint32_t frame, uint32_t depth,
                                                    float *records) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -37,27 +40,41 @@ __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_
     return;
   }
   const uint32_t h0 = mix32(i * 0x9e3779b9u ^ mix32(frame + 0x632be5abu));
-  const uint32_t n_pix = P.x_dim * P.y_dim;
+  Camera cam = camera_of(P);
+  LightSet lights = lights_of(P);
+  uint32_t root = 0;
+  const BatchScene *scene = nullptr;
+  if (scenes != nullptr) {
+    scene = scenes + mix32(h0 ^ 0x5bd1e995u) % n_scenes;
+    cam.f2w = scene->f2w;
+    cam.x_dim = scene->x_dim;
+    cam.y_dim = scene->y_dim;
+    cam.spp = scene->spp;
+    cam.sample_offset = scene->sample_offset;
+    lights = lights_of(P, *scene);
+    root = scene->root;
+  }
+  const uint32_t n_pix = cam.x_dim * cam.y_dim;
   const uint32_t pixel = h0 % n_pix;
-  const uint32_t x = pixel % P.x_dim, y = pixel / P.x_dim;
-  const uint32_t smp = mix32(h0) % P.spp;
+  const uint32_t x = pixel % cam.x_dim, y = pixel / cam.x_dim;
+  const uint32_t smp = mix32(h0) % cam.spp;
   PathStateT<kUniform> s;
   uint32_t xw[kUniform ? kXorwowWords : 1];
-  path_begin(P, smp, x, y, s, xw, 1);
+  path_begin_cam(P, cam, smp, x, y, s, xw, 1);
   float q[kMaxRecordVertices][12];
   rgb gathered[kMaxRecordVertices], beta[kMaxRecordVertices];
   uint32_t nv = 0;
   Counts cnt = {0, 0, 0};
-  const LightSet lights = lights_of(P);
   while (true) {
     Hit lh, nh;
-    step_hits<kTravWide, false>(P, s, false, x, cnt, lh, nh);
+    step_hits<kTravWide, false>(P, s, false, x, cnt, lh, nh, root);
     const rgb b = s.multiplier;
     StepTrace tr;
     const bool cont = path_continues(P, s, path_step(P, lights, s, lh, nh, &tr));
     if (tr.hit && nv < kMaxRecordVertices) {
       const f3 wo = -tr.in;
-      const float v[12] = {tr.point.x, tr.point.y, tr.point.z, wo.x, wo.y, wo.z,
+      const f3 cp = scene != nullptr ? batch_cache_position(*scene, tr.point) : tr.point;
+      const float v[12] = {cp.x, cp.y, cp.z, wo.x, wo.y, wo.z,
                            tr.normal.x, tr.normal.y, tr.normal.z, tr.albedo.r,
                            tr.albedo.g, tr.albedo.b};
       for (int j = 0; j < 12; ++j) {
@@ -74,7 +91,8 @@ __global__ void __launch_bounds__(128) k_nrc_paths(const RenderParams P, uint32_
   float *r = records + (size_t)i * 16;
   if (nv == 0) {
     // the camera ray left the scene: a zero-radiance record at its origin
-    const float v[16] = {s.o.x, s.o.y, s.o.z, 0.f, 0.f, 1.f, 0.f, 0.f, 1.f,
+    const f3 cp = scene != nullptr ? batch_cache_position(*scene, s.o) : s.o;
+    const float v[16] = {cp.x, cp.y, cp.z, 0.f, 0.f, 1.f, 0.f, 0.f, 1.f,
                          0.f,   0.f,   0.f,   0.f, 0.f, 0.f, 0.f};
     for (int j = 0; j < 16; ++j) {
       r[j] = v[j];
@@ -119,9 +137,27 @@ cudaError_t launch_nrc_paths(const RenderParams &p, uint32_t n, uint32_t frame, 
     return cudaSuccess;
   }
   if (p.rng_uniform) {
-    dev::k_nrc_paths<true><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, depth, records);
+    dev::k_nrc_paths<true>
+        <<<(n + 127) / 128, 128, 0, s>>>(p, nullptr, 0, n, frame, depth, records);
   } else {
-    dev::k_nrc_paths<false><<<(n + 127) / 128, 128, 0, s>>>(p, n, frame, depth, records);
+    dev::k_nrc_paths<false>
+        <<<(n + 127) / 128, 128, 0, s>>>(p, nullptr, 0, n, frame, depth, records);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_paths_batch(const RenderParams &p, const BatchScene *scenes,
+                                   uint32_t n_scenes, uint32_t n, uint32_t frame,
+                                   uint32_t depth, float *records, cudaStream_t s) {
+  if (n == 0 || n_scenes == 0) {
+    return cudaSuccess;
+  }
+  if (p.rng_uniform) {
+    dev::k_nrc_paths<true>
+        <<<(n + 127) / 128, 128, 0, s>>>(p, scenes, n_scenes, n, frame, depth, records);
+  } else {
+    dev::k_nrc_paths<false>
+        <<<(n + 127) / 128, 128, 0, s>>>(p, scenes, n_scenes, n, frame, depth, records);
   }
   return cudaGetLastError();
 }

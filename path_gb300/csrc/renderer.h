@@ -106,6 +106,7 @@ void scene_box(const FlatScene &flat, float *lo, float *hi);
 struct BatchItem {
   const Scene *scene;
   uint32_t x_dim, y_dim, spp;
+  uint32_t sample_offset = 0; // Sobol samples [sample_offset, sample_offset + spp)
   float f2w[12];
   path_output output;
 };
@@ -117,6 +118,7 @@ struct PreparedBatch {
   SBVHSettings sbvh;
   uint32_t gpu_build = 0;
   std::vector<uint32_t> root, light_off, n_lights, n_tris;
+  std::vector<std::array<float, 6>> box; // per item: its scene's vertex box (lo, hi)
   uint32_t n_wide_nodes = 0;
   uint64_t total_tris = 0;
   double build_seconds = 0.0;
@@ -152,6 +154,13 @@ public:
                       const path_batch_tuning *tuning, double *seconds);
   Status autotune_batch(const std::vector<BatchItem> &items, const path_settings &settings,
                         uint64_t sample_budget, path_batch_tuning *out);
+  // one frame of every item with one radiance cache for the whole batch
+  // (item i in cell i of it), then train_steps Adam steps on train_paths
+  // records traced from random items
+  Status render_batch_cached(const std::vector<BatchItem> &items, const path_settings &settings,
+                             const path_batch_tuning *tuning, class RadianceCache &cache,
+                             uint32_t cache_depth, uint32_t train_paths, uint32_t train_steps,
+                             double *seconds);
   // render that allocates nothing; scratch is device memory the caller owns
   // (defined in noalloc.cu)
   Status render_noalloc(const path_sample_spec &spec, const path_output &output,

@@ -96,12 +96,7 @@ __device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t s
   if (W.scenes == nullptr) {
     return lights_of(W.P);
   }
-  const BatchScene &b = W.scenes[scene];
-  LightSet l;
-  l.tris = W.P.light_tris + 3 * (size_t)b.light_off;
-  l.cdf = W.P.light_cdf + b.light_off;
-  l.n = b.n_lights;
-  return l;
+  return lights_of(W.P, W.scenes[scene]);
 }
 
 template <bool kUniform>
@@ -128,17 +123,18 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
   s.has_light = (flags & kFlagLight) != 0;
   s.count_emission = (flags & kFlagEmission) != 0;
   unsigned long long local = id;
-  uint32_t spp = P.spp;
+  uint32_t spp = P.spp, offset = P.sample_offset;
   if (W.scenes != nullptr) {
     local = id - W.scenes[scene].first_sample;
     spp = W.scenes[scene].spp;
+    offset = W.scenes[scene].sample_offset;
   }
   if constexpr (kUniform) {
     s.rng.w = W.rng_state + slot;
     s.rng.stride = W.n_slots;
   } else {
     const uint32_t smp = (uint32_t)(local % spp);
-    s.rng.begin(P, smp + P.sample_offset);
+    s.rng.begin(P, smp + offset);
     s.rng.dim = st.z;
   }
   return id;
@@ -161,6 +157,7 @@ __device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
     cam.x_dim = b.x_dim;
     cam.y_dim = b.y_dim;
     cam.spp = b.spp;
+    cam.sample_offset = b.sample_offset;
     path_begin_cam(W.P, cam, smp, x, y, s, W.rng_state + slot, W.n_slots);
     root = b.root;
   }
@@ -365,7 +362,10 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
           const size_t k = (size_t)(id - W.first_sample);
           float *q = W.cache_q + 12 * k;
           const f3 wo = -tr.in;
-          const float vals[12] = {tr.point.x, tr.point.y, tr.point.z, wo.x, wo.y, wo.z,
+          // a batch shares one cache: the scene's cell of it
+          const f3 cp = W.scenes != nullptr ? batch_cache_position(W.scenes[scene], tr.point)
+                                            : tr.point;
+          const float vals[12] = {cp.x, cp.y, cp.z, wo.x, wo.y, wo.z,
                                   tr.normal.x, tr.normal.y, tr.normal.z, tr.albedo.r,
                                   tr.albedo.g, tr.albedo.b};
           for (int j = 0; j < 12; ++j) {

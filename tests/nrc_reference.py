@@ -26,11 +26,29 @@ def grid_index(x, y, z, side):
     return (h & np.uint64(TABLE - 1)).astype(np.int64)
 
 
+def batch_grid_index(x, y, z, side, cell):
+    """A batch cache's vertex: coordinates offset by side x the cell, hashed."""
+    xs = (x + side * cell[:, 0]).astype(np.uint64)
+    ys = (y + side * cell[:, 1]).astype(np.uint64)
+    zs = (z + side * cell[:, 2]).astype(np.uint64)
+    h = xs ^ ((ys * np.uint64(2654435761)) & np.uint64(0xFFFFFFFF)) ^ \
+        ((zs * np.uint64(805459861)) & np.uint64(0xFFFFFFFF))
+    return (h & np.uint64(TABLE - 1)).astype(np.int64)
+
+
 def corners(q, lo, hi):
-    """Per level: (indices [n, 8], weights [n, 8])."""
-    lo = np.asarray(lo, np.float32)
-    inv = (np.float32(1) / np.maximum(np.asarray(hi, np.float32) - lo, np.float32(1e-6)))
-    p = np.clip((q[:, :3].astype(np.float32) - lo) * inv, 0, 1).astype(np.float32)
+    """Per level: (indices [n, 8], weights [n, 8]).  lo None: positions in
+    batch-cell coordinates (x in [0, 1]^3 plus twice an integer cell)."""
+    pos = q[:, :3].astype(np.float32)
+    if lo is None:
+        cell = np.clip(np.floor(pos * np.float32(0.5)), 0, 15).astype(np.float32)
+        p = np.clip(pos - np.float32(2) * cell, 0, 1).astype(np.float32)
+        cell = cell.astype(np.int64)
+    else:
+        lo = np.asarray(lo, np.float32)
+        inv = (np.float32(1) / np.maximum(np.asarray(hi, np.float32) - lo, np.float32(1e-6)))
+        p = np.clip((pos - lo) * inv, 0, 1).astype(np.float32)
+        cell = None
     out = []
     for res in level_res():
         side = int(res) + 1
@@ -42,7 +60,10 @@ def corners(q, lo, hi):
         for c in range(8):
             o = np.array([c & 1, (c >> 1) & 1, (c >> 2) & 1])
             g = c0 + o
-            idx.append(grid_index(g[:, 0], g[:, 1], g[:, 2], side))
+            if cell is None:
+                idx.append(grid_index(g[:, 0], g[:, 1], g[:, 2], side))
+            else:
+                idx.append(batch_grid_index(g[:, 0], g[:, 1], g[:, 2], side, cell))
             w.append(np.prod(np.where(o == 1, fr, 1 - fr), axis=1))
         out.append((np.stack(idx, 1), np.stack(w, 1)))
     return out

@@ -131,3 +131,26 @@ def test_batch_with_gpu_built_bvhs_renders_the_same_images(lib, mode):
     for out, ref in zip(outs, refs):
         err = np.linalg.norm(out.astype(np.float64) - ref) / np.linalg.norm(ref)
         assert err <= 1e-4
+
+
+def test_batch_sample_offsets_equal_single_renders(lib):
+    """An item's sample_offset picks the same Sobol samples as the
+    single-scene render's (progressive frames of a batch)."""
+    s = scenes.path_settings(6, "wide")
+    items = _small_batch(13, 3)
+    batch, outs, refs = [], [], []
+    for k, (sc, w, h, spp) in enumerate(items):
+        f2w = scenes.cornell_camera(w, h)
+        off = 7 + 100 * k
+        out = np.zeros((h, w, 3), np.float32)
+        outs.append(out)
+        ref = np.zeros((h, w, 3), np.float32)
+        s1 = s.copy()
+        s1.kernel_approach = 1
+        api.Renderer().render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w, sample_offset=off),
+                              ref, sc, spp, s1)
+        refs.append(ref)
+        batch.append((sc, api.SquareImage(w, h, f2w, sample_offset=off), out, spp))
+    api.Renderer().render_batch(batch, s)
+    for out, ref in zip(outs, refs):
+        assert np.array_equal(bits(out), bits(ref))
