@@ -148,28 +148,17 @@ __device__ Hit trace_binary(const RenderParams &P, const ray &r, Counts &cnt) {
 // ---------------------------------------------------------------------------
 // compressed 8-wide BVH.  A node is five 128-bit loads.  Its eight child
 // boxes are tested with one fused multiply-add per plane,
-//   t = q * (2^e / d) + (p - o) / d,
-// widened by a rounding margin of 2^-20 (|(p - o) / d| + 255 |2^e / d|),
-// which covers the error of the fused form against the exact plane
-// p + q 2^e (an exactly representable float, see wide.cpp) several times
-// over.  Decoded boxes contain the binary SBVH's boxes, so every box the
-// reference's slab test accepts is accepted here too.
-__device__ __forceinline__ uint32_t byte_of(uint32_t lo, uint32_t hi, int i) {
-  uint32_t w = i < 4 ? lo : hi;
-  return (w >> (8 * (i & 3))) & 0xffu;
-}
-
+//   t = q a + b,  a = 2^e / d,  b = (p - o) / d,
+// evaluated as m A + C with m = 1 + q 2^-15 (the byte placed in the float
+// 1.0 by one byte permute), A = 2^15 a and C = b - A, and widened by a
+// rounding margin of 2^-20 (|b| + 255 |a|), which covers the error of the
+// fused form against the exact plane p + q 2^e (an exactly representable
+// float, see wide.cpp) several times over, plus 2^-8 |a| + 2^-23 |b|, which
+// covers the rounding of C (at most 2^-9 |a| + 2^-24 |b|).  Decoded boxes
+// contain the binary SBVH's boxes, so every box the reference's slab test
+// accepts is accepted here too.
 __device__ __forceinline__ float exp2_byte(uint32_t e) {
   return __uint_as_float(e << 23);
-}
-
-// byte i (0..3) of w as a float: (2^23 + byte) - 2^23, exact
-__device__ __forceinline__ float byte_float(uint32_t w, int i) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | (uint32_t)i)) - 8388608.0f;
-}
-
-__device__ __forceinline__ float byte8_float(uint32_t lo, uint32_t hi, int i) {
-  return byte_float(i < 4 ? lo : hi, i & 3);
 }
 
 // two-lane FP32 (one instruction on sm_100 and later; each lane rounds like
@@ -192,14 +181,16 @@ __device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
   return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
 }
 
-// bytes i of (n, f) as the pair of plane distances q * a + (bn, bf)
-__device__ __forceinline__ float2 plane_pair(uint32_t nl, uint32_t nh, uint32_t fl, uint32_t fh,
-                                             int i, float2 aa, float2 bb) {
+// bytes i of (n, f) as the pair of plane distances m * A + (Cn, Cf) with
+// m = 1 + q 2^-15 (the byte in the second byte of the float 1.0) and
+// A = 2^15 a, C = b - A: q a + b in one fused multiply-add per plane
+__device__ __forceinline__ float2 plane_pair(uint32_t nl, uint32_t nh, uint32_t fl,
+                                               uint32_t fh, int i, float2 aa, float2 cc) {
   const uint32_t wn = i < 4 ? nl : nh, wf = i < 4 ? fl : fh;
-  const float2 m = make_float2(__uint_as_float(__byte_perm(wn, 0x4B000000u, 0x7650u | (uint32_t)(i & 3))),
-                               __uint_as_float(__byte_perm(wf, 0x4B000000u, 0x7650u | (uint32_t)(i & 3))));
-  const float2 q = add2_rn(m, make_float2(-8388608.0f, -8388608.0f));
-  return fma2_rn(q, aa, bb);
+  const uint32_t sel = 0x7604u | ((uint32_t)(i & 3) << 4);
+  const float2 m = make_float2(__uint_as_float(__byte_perm(wn, 0x3F800000u, sel)),
+                               __uint_as_float(__byte_perm(wf, 0x3F800000u, sel)));
+  return fma2_rn(m, aa, cc);
 }
 
 constexpr int kWideStack = (int)kWideStackDepth;
@@ -334,9 +325,11 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
   const float bx = (__uint_as_float(n0.x) - w.r.o.x) * inv.x;
   const float by = (__uint_as_float(n0.y) - w.r.o.y) * inv.y;
   const float bz = (__uint_as_float(n0.z) - w.r.o.z) * inv.z;
-  const float ex = __fmul_rn(__fmaf_rn(255.f, fabsf(ax), fabsf(bx)), 0x1p-20f);
-  const float ey = __fmul_rn(__fmaf_rn(255.f, fabsf(ay), fabsf(by)), 0x1p-20f);
-  const float ez = __fmul_rn(__fmaf_rn(255.f, fabsf(az), fabsf(bz)), 0x1p-20f);
+  // 2^-20 (255 |a| + |b|), plus 2^-8 |a| + 2^-23 |b| for the rounding of
+  // C = b - 2^15 a (at most 2^-9 |a| + 2^-24 |b|)
+  const float ex = __fmul_rn(__fmaf_rn(4352.f, fabsf(ax), __fmul_rn(1.125f, fabsf(bx))), 0x1p-20f);
+  const float ey = __fmul_rn(__fmaf_rn(4352.f, fabsf(ay), __fmul_rn(1.125f, fabsf(by))), 0x1p-20f);
+  const float ez = __fmul_rn(__fmaf_rn(4352.f, fabsf(az), __fmul_rn(1.125f, fabsf(bz))), 0x1p-20f);
   const float bnx = bx - ex, bfx = bx + ex;
   const float bny = by - ey, bfy = by + ey;
   const float bnz = bz - ez, bfz = bz + ez;
@@ -350,22 +343,30 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
   const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
   const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
   const float tcull = w.best.t;
-  // slot i's box test into bit i (empty slots never pass: lo > hi)
-  uint32_t hm = 0;
-  const float2 aax = make_float2(ax, ax), aay = make_float2(ay, ay), aaz = make_float2(az, az);
-  const float2 bbx = make_float2(bnx, bfx), bby = make_float2(bny, bfy),
-               bbz = make_float2(bnz, bfz);
+  const float Ax = __fmul_rn(ax, 32768.f), Ay = __fmul_rn(ay, 32768.f),
+              Az = __fmul_rn(az, 32768.f);
+  const float2 aax = make_float2(Ax, Ax), aay = make_float2(Ay, Ay), aaz = make_float2(Az, Az);
+  const float2 ccx = add2_rn(make_float2(bnx, bfx), make_float2(-Ax, -Ax));
+  const float2 ccy = add2_rn(make_float2(bny, bfy), make_float2(-Ay, -Ay));
+  const float2 ccz = add2_rn(make_float2(bnz, bfz), make_float2(-Az, -Az));
+  // slot i's box test, a miss as the sign of tmax - tmin, tcull - tmin or
+  // tmax (tmin <= tmax && tmin <= tcull && tmax >= 0; tcull >= 0; a box
+  // holding a hit at t > 1e-5 has tmax > 0), shifted in from slot 7 down so
+  // that slot i lands in bit i (empty slots never pass: lo > hi)
+  uint32_t miss = 0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
+  for (int i = 7; i >= 0; --i) {
     // (near, far) plane distance per axis
-    const float2 tx = plane_pair(nxl, nxh, fxl, fxh, i, aax, bbx);
-    const float2 ty = plane_pair(nyl, nyh, fyl, fyh, i, aay, bby);
-    const float2 tz = plane_pair(nzl, nzh, fzl, fzh, i, aaz, bbz);
-    // tmin <= tmax && tmax >= 0 && tmin <= tcull, as one comparison (tcull >= 0)
-    const float tmin = fmax3(tx.x, ty.x, fmaxf(tz.x, 0.f));
-    const float tmax = fmin3(tx.y, ty.y, fminf(tz.y, tcull));
-    hm |= (tmin <= tmax ? 1u : 0u) << i;
+    const float2 tx = plane_pair(nxl, nxh, fxl, fxh, i, aax, ccx);
+    const float2 ty = plane_pair(nyl, nyh, fyl, fyh, i, aay, ccy);
+    const float2 tz = plane_pair(nzl, nzh, fzl, fzh, i, aaz, ccz);
+    const float tmin = fmax3(tx.x, ty.x, tz.x);
+    const float tmax = fmin3(tx.y, ty.y, tz.y);
+    const uint32_t neg = __float_as_uint(__fsub_rn(tmax, tmin)) |
+                         __float_as_uint(__fsub_rn(tcull, tmin)) | __float_as_uint(tmax);
+    miss = __funnelshift_l(neg, miss, 1);
   }
+  const uint32_t hm = ~miss & 0xffu;
   // internal children: slot i -> bit i ^ oct (ray order), by three swaps
   uint32_t hits = hm & imask;
   const uint32_t h1 = ((hits & 0x55u) << 1) | ((hits >> 1) & 0x55u);
