@@ -529,8 +529,9 @@ struct WarpTriScratch {
 // atomicMin from the items that hit instead of a segmented shuffle
 // reduction over every item.  The keys and the fold are those of
 // warp_triangles, so the result is the same bit for bit.  All 32 lanes call
-// this; sh.o / sh.d hold the ray of every lane with triangles.
-template <bool kCount>
+// this; sh.o / sh.d hold the ray of every lane with triangles, or, with
+// kStoreRay, each such lane writes its ray there first.
+template <bool kCount, bool kStoreRay = false>
 __device__ __forceinline__ void warp_triangles_shared(const RenderParams &P, WideWalk &w,
                                                       uint32_t tri_base, uint32_t tmask,
                                                       uint32_t lane, Counts &cnt,
@@ -550,6 +551,10 @@ __device__ __forceinline__ void warp_triangles_shared(const RenderParams &P, Wid
   }
   const uint32_t excl = incl - c;
   sh.key[lane] = ~0ull;
+  if (kStoreRay && c > 0) {
+    sh.o[lane] = make_float4(w.r.o.x, w.r.o.y, w.r.o.z, 0.f);
+    sh.d[lane] = make_float4(w.r.d.x, w.r.d.y, w.r.d.z, 0.f);
+  }
   __syncwarp();
   for (uint32_t base = 0; base < total; base += 32) {
     const uint32_t g = base + lane;

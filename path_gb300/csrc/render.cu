@@ -60,6 +60,8 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
   const uint32_t block = blockIdx.x + P.start_block;
   const uint32_t tid = threadIdx.x;
   const uint32_t lane = tid & 31;
+  __shared__ WarpTriScratch s_tri[8];
+  WarpTriScratch &sh = s_tri[tid >> 5];
   const ThreadWork tw = band_work(P, block, tid);
   Counts cnt = {0, 0, 0};
   rgb total = zero_rgb();
@@ -130,7 +132,7 @@ __global__ void __launch_bounds__(256, 2) k_render_coop(const RenderParams P) {
     if (tracing && !w.done) {
       wide_node<kCount>(P, w, st_base, st_bits, cnt, tri_base, tmask);
     }
-    warp_triangles<kCount>(P, w, tri_base, tmask, lane, cnt);
+    warp_triangles_shared<kCount, true>(P, w, tri_base, tmask, lane, cnt, sh);
     if (tracing && w.done) {
       if (phase == 1) {
         lh = w.best;

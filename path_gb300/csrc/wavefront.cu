@@ -99,14 +99,57 @@ __device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t s
   return lights_of(W.P, W.scenes[scene]);
 }
 
+// A lane's slot state (and both hits) copied into shared memory by
+// asynchronous copies: the shade kernel stages a warp's next batch of slots
+// while it shades the current one.
+struct SlotStage {
+  float4 o, d, ld, mult, lmult, total;
+  uint4 state;
+  uint2 hit_light, hit_ext;
+};
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+__device__ __forceinline__ void stage_slot(const WaveParams &W, uint32_t slot, SlotStage &g) {
+  cp_async16(&g.o, W.o + slot);
+  cp_async16(&g.d, W.d + slot);
+  cp_async16(&g.ld, W.ld + slot);
+  cp_async16(&g.mult, W.mult + slot);
+  cp_async16(&g.lmult, W.lmult + slot);
+  cp_async16(&g.total, W.total + slot);
+  cp_async16(&g.state, W.state + slot);
+  cp_async8(&g.hit_light, W.hit_light + slot);
+  cp_async8(&g.hit_ext, W.hit_ext + slot);
+}
+
+// a slot's path state from its seven words (global or staged)
 template <bool kUniform>
-__device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
-                                                        PathStateT<kUniform> &s,
-                                                        uint32_t &scene, uint32_t &root) {
+__device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, uint32_t slot,
+                                                          float4 o, float4 d, float4 ld,
+                                                          float4 m, float4 lm, float4 t,
+                                                          uint4 st, PathStateT<kUniform> &s,
+                                                          uint32_t &scene, uint32_t &root) {
   const RenderParams &P = W.P;
-  float4 o = W.o[slot], d = W.d[slot], ld = W.ld[slot];
-  float4 m = W.mult[slot], lm = W.lmult[slot], t = W.total[slot];
-  uint4 st = W.state[slot];
   unsigned long long id = (unsigned long long)st.x | ((unsigned long long)(st.y & 0xffu) << 32);
   scene = st.y >> 8;
   root = __float_as_uint(d.w);
@@ -138,6 +181,14 @@ __device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uin
     s.rng.dim = st.z;
   }
   return id;
+}
+
+template <bool kUniform>
+__device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
+                                                        PathStateT<kUniform> &s,
+                                                        uint32_t &scene, uint32_t &root) {
+  return unpack_path(W, slot, W.o[slot], W.d[slot], W.ld[slot], W.mult[slot], W.lmult[slot],
+                     W.total[slot], W.state[slot], s, scene, root);
 }
 
 template <bool kUniform>
@@ -323,35 +374,51 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // which measured faster than fewer warps without register spills.  kCache
 // (paths end into the radiance cache) is a template parameter so that the
 // plain kernel carries none of the cache-query code.
+// Each warp takes batches of 32 live slots; the state of its next batch is
+// copied into shared memory (cp.async) while it shades the current one, so
+// the slot loads of a batch overlap the previous batch's work.
 template <bool kGrad, bool kUniform, bool kCache, uint32_t kFeat = kFeatAll>
 __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_t parity) {
+  __shared__ SlotStage s_stage[256];
   const uint32_t lane = threadIdx.x & 31;
+  SlotStage &g = s_stage[threadIdx.x];
   const uint32_t count = W.q->active[parity];
   const uint32_t *in = W.active[parity];
   uint32_t *out = W.active[parity ^ 1u];
-  while (true) {
-    uint32_t base = 0;
+  auto take = [&]() {
+    uint32_t b = 0;
     if (lane == 0) {
-      base = atomicAdd(&W.q->shade_cursor, 32u);
+      b = atomicAdd(&W.q->shade_cursor, 32u);
     }
-    base = __shfl_sync(kFull, base, 0);
-    if (base >= count) {
-      break;
-    }
-    const uint32_t i = base + lane;
-    const bool valid = i < count;
-    uint32_t slot = 0;
+    return __shfl_sync(kFull, b, 0);
+  };
+  uint32_t base = take();
+  if (base >= count) {
+    return;
+  }
+  bool valid = base + lane < count;
+  uint32_t slot = valid ? in[base + lane] : 0u;
+  if (valid) {
+    stage_slot(W, slot, g);
+  }
+  cp_async_commit();
+  while (true) {
+    // the next batch's slots, read now and staged after this batch
+    const uint32_t next_base = take();
+    const bool next_valid = next_base + lane < count;
+    const uint32_t next_slot = next_valid ? in[next_base + lane] : 0u;
+    cp_async_wait_all();
     bool live = false, finished = false, want_next = false, want_light = false;
     uint32_t gm_vertex = kNoMaterial, gm_light = kNoMaterial, gm_emit = kNoMaterial;
     float gv_vertex[4] = {0.f, 0.f, 0.f, 0.f};
     float gv_light[3] = {0.f, 0.f, 0.f}, gv_emit[3] = {0.f, 0.f, 0.f};
     if (valid) {
-      slot = in[i];
       PathStateT<kUniform> s;
       uint32_t scene, root;
-      unsigned long long id = load_path(W, slot, s, scene, root);
-      Hit lh = s.has_light ? unpack_hit(W.hit_light[slot]) : no_hit();
-      Hit nh = s.has_next ? unpack_hit(W.hit_ext[slot]) : no_hit();
+      unsigned long long id = unpack_path(W, slot, g.o, g.d, g.ld, g.mult, g.lmult, g.total,
+                                          g.state, s, scene, root);
+      Hit lh = s.has_light ? unpack_hit(g.hit_light) : no_hit();
+      Hit nh = s.has_next ? unpack_hit(g.hit_ext) : no_hit();
       if (!kGrad) {
         StepTrace tr;
         StepTrace *trp = kCache ? &tr : nullptr;
@@ -496,6 +563,15 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
     if (want_light) {
       W.rays[pl] = (slot << 1) | 1u;
     }
+    if (next_base >= count) {
+      break;
+    }
+    if (next_valid) {
+      stage_slot(W, next_slot, g);
+    }
+    cp_async_commit();
+    slot = next_slot;
+    valid = next_valid;
   }
 }
 
