@@ -153,7 +153,8 @@ __device__ Hit trace_binary(const RenderParams &P, const ray &r, Counts &cnt) {
 // 1.0 by one byte permute), A = 2^15 a and C = b - A, and widened by a
 // rounding margin of 2^-20 (|b| + 255 |a|), which covers the error of the
 // fused form against the exact plane p + q 2^e (an exactly representable
-// float, see wide.cpp) several times over, plus 2^-8 |a| + 2^-23 |b|, which
+// float, see wide.cpp), with 1 / d one ulp off (the hardware reciprocal),
+// more than twice over, plus 2^-8 |a| + 2^-23 |b|, which
 // covers the rounding of C (at most 2^-9 |a| + 2^-24 |b|).  Decoded boxes
 // contain the binary SBVH's boxes, so every box the reference's slab test
 // accepts is accepted here too.
@@ -240,6 +241,22 @@ struct WideWalk {
   bool done;
 };
 
+// The inverse direction of the 8-wide walk: the reference's zero rule
+// (aabb.h:16-28) with the hardware reciprocal (rcp.approx.f32, at most one
+// ulp from 1 / x).  It only feeds the 8-wide box tests, whose rounding margin
+// (2^-20 of the plane distance) covers an inverse one ulp off several times
+// over; the triangle test and the binary traversal keep the exact division.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ f3 inv_dir_wide(f3 d) {
+  return mk(rcp_approx(d.x == 0.f ? 1e-20f : d.x), rcp_approx(d.y == 0.f ? 1e-20f : d.y),
+            rcp_approx(d.z == 0.f ? 1e-20f : d.z));
+}
+
 // tlimit: hits beyond it are not wanted (shadow rays only need hits up to
 // just past the light); INF for extension rays.  Within the limit the
 // closest hit is the same as without it.
@@ -247,7 +264,7 @@ __device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, c
                                            float tlimit, float light_target,
                                            uint32_t root = 0) {
   w.r = r;
-  w.inv = inv_dir(r.d);
+  w.inv = inv_dir_wide(r.d);
   w.best = no_hit();
   w.best.t = tlimit;
   w.light_target = light_target;
