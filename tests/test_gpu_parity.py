@@ -558,3 +558,74 @@ def test_gpu_built_bvh_renders_the_same_image(lib, case, mode):
     print(f"{case} mode {mode}: gpu build {1e3 * st['bvh_build_seconds']:.1f} ms, "
           f"{st['num_wide_nodes']} wide nodes, rel RMSE {rel_rmse(out, host_built):.2e}")
     assert rel_rmse(out, host_built) <= RMSE_TOL
+
+
+def _adversarial_rays(rng, tris):
+    """Rays that stress the 8-wide box test's margin: axis-parallel rays
+    (zero direction components, the 1e-20 rule) with origins on the
+    triangles' own vertex coordinates (on node planes), directions with
+    components of 1e-30 and 1e-40 (a subnormal), rays grazing the axis
+    planes of the room's walls, and rays from vertices towards vertices."""
+    v = tris.reshape(-1, 3)
+    rays = []
+    axes = np.eye(3)
+    for k in range(600):
+        o = v[rng.integers(len(v))].astype(np.float64).copy()
+        a = rng.integers(3)
+        o[(a + 1) % 3] += rng.choice([0.0, 1e-7, -1e-7, 0.01])
+        d = axes[a] * rng.choice([-1.0, 1.0])
+        rays.append(np.concatenate([o - 3 * d, d]))
+    for tiny in (1e-30, -1e-30, 1e-40, -1e-40):
+        for k in range(200):
+            o = rng.uniform(-0.9, 0.9, 3)
+            d = np.zeros(3)
+            a = rng.integers(3)
+            d[a] = rng.choice([-1.0, 1.0])
+            d[(a + 1) % 3] = tiny
+            d[(a + 2) % 3] = rng.choice([0.0, tiny, 0.3])
+            rays.append(np.concatenate([o, d]))
+    for k in range(400):
+        # grazing the walls: origin on a wall plane, direction in it
+        o = rng.uniform(-1, 1, 3)
+        a = rng.integers(3)
+        o[a] = rng.choice([-1.0, 1.0])
+        d = rng.normal(size=3)
+        d[a] = rng.choice([0.0, 1e-7, -1e-7])
+        rays.append(np.concatenate([o, d / np.linalg.norm(d)]))
+    for k in range(800):
+        p, q = v[rng.integers(len(v))], v[rng.integers(len(v))]
+        d = q.astype(np.float64) - p
+        n = np.linalg.norm(d)
+        if n == 0:
+            continue
+        rays.append(np.concatenate([p, d / n]))
+    return np.array(rays, np.float32)
+
+
+def test_wide_traversal_on_adversarial_rays(lib, oracle):
+    """The 8-wide walk (quantised boxes, rounding margin, hardware
+    reciprocal) finds every closest hit that testing every triangle finds,
+    on rays built to sit on its box planes and to have zero, tiny and
+    subnormal direction components."""
+    rng = np.random.default_rng(33)
+    walls, light = scenes.room_triangles()
+    room = [t for ts in walls.values() for t in ts] + list(light)
+    for k in range(12):
+        room.extend(scenes._box(rng.uniform(0.05, 0.6), rng.uniform(0.05, 1.2),
+                                rng.uniform(0.05, 0.6),
+                                float(rng.choice([0.0, 90.0, rng.uniform(0, 90)])),
+                                tuple(rng.uniform(-0.7, 0.7, 2))))
+    room = np.stack(room).reshape(-1, 9).astype(np.float32)
+    ico, _ = scenes.displaced_icosphere(4)
+    s = api.Settings()
+    s.traversal = 1
+    r = api.Renderer()
+    for tris in (room, np.concatenate([room, ico]).astype(np.float32)):
+        rays = _adversarial_rays(rng, tris)
+        want, wt = ol.loop_all(tris, rays)
+        got, gt = r.intersect(tris, rays, s)
+        hit = want >= 0
+        assert np.array_equal(hit, got >= 0)
+        assert np.array_equal(bits(wt[hit]), bits(gt[hit]))
+        # equal distances may name another triangle (the tie rules differ)
+        assert np.all((want == got) | hit)
