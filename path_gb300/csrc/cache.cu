@@ -250,102 +250,197 @@ __device__ __forceinline__ void tc_wait(TcSync &s, uint32_t tid, uint32_t *err) 
   tc::fence_after_sync();
 }
 
-// Inference: out[i] = MLP(encode(queries[i])) for i < n; persistent CTAs of
-// 512 threads over tiles of 128 queries.  The encoding is split four ways
-// (thread t: row t % 128, levels 4 (t / 128) ...), and each layer's
-// epilogue too: warp w reads tensor-memory lanes 32 (w % 4) ... (its lane
-// quarter) and columns 16 (w / 4) ... 16 (w / 4) + 15.
-constexpr uint32_t kInferThreads = 512;
+// The network's first-layer input of every query as BF16 tiles of 128 rows
+// in the tensor core's K-major layout (kNrcTileBytes per tile, rows past n
+// zero), written by k_nrc_encode and copied whole into shared memory by
+// k_nrc_infer.  Four threads per row: thread g encodes hash levels 4 g ...
+// 4 g + 3 (one 16-byte core-matrix row of eight features); threads 0 and 1
+// also write the direction, normal and albedo columns and the zero padding.
+constexpr uint32_t kNrcTileBytes = 128 * kNrcIn * 2;
+
+__device__ __forceinline__ uint4 pack_bf16x8(const float (&v)[8]) {
+  uint4 r;
+  uint32_t *w = &r.x;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    w[k] = *reinterpret_cast<const uint32_t *>(&h);
+  }
+  return r;
+}
 
 // live (optional): per query 3 floats, all zero for a query no path uses
-// (its encoding is skipped and its output is not meaningful)
-__global__ void __launch_bounds__(kInferThreads) k_nrc_infer(const __grid_constant__ NrcParams C,
-                                                             const float *queries, uint32_t n,
-                                                             const float *live, float *out,
-                                                             uint32_t *err) {
+// (its encoding is skipped: zeros)
+__global__ void __launch_bounds__(256) k_nrc_encode(const __grid_constant__ NrcParams C,
+                                                    const float *queries, uint32_t n,
+                                                    uint32_t n_rows, const float *live,
+                                                    unsigned char *x0) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t qi = t >> 2, g = t & 3u;
+  if (qi >= n_rows) {
+    return;
+  }
+  const float *q = queries + (size_t)qi * 12;
+  const bool used = qi < n && (live == nullptr || live[3 * (size_t)qi] != 0.f ||
+                               live[3 * (size_t)qi + 1] != 0.f ||
+                               live[3 * (size_t)qi + 2] != 0.f);
+  float in[8];
+  if (used) {
+    nrc_encode_levels<4>(C, q, 4 * g, in);
+  } else {
+    for (int k = 0; k < 8; ++k) {
+      in[k] = 0.f;
+    }
+  }
+  unsigned char *tile = x0 + (size_t)(qi >> 7) * kNrcTileBytes;
+  const uint32_t row = qi & 127u;
+  *reinterpret_cast<uint4 *>(tile + smem_offset(row, 8 * g, kNrcIn)) = pack_bf16x8(in);
+  if (g < 2) {
+    // columns 32 ... 39: direction, normal, albedo r g; 40 ... 47: albedo b, zeros
+    float e[8];
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t c = 8 * g + (uint32_t)k; // 0 ... 15 past the hash features
+      e[k] = used && c < 9 ? q[3 + c] : 0.f;
+    }
+    *reinterpret_cast<uint4 *>(tile + smem_offset(row, 32 + 8 * g, kNrcIn)) = pack_bf16x8(e);
+  }
+}
+
+// Inference: out[i] = MLP(x0 row i) for i < n.  One CTA per SM of four
+// independent teams (warpgroups) that share the weights in shared memory;
+// each team takes every fourth tile of the CTA's share, with its own 64
+// tensor-memory columns, mbarriers and 44 KB of tile buffers: its tile's
+// input is copied in by one bulk copy (the next tile's copy starts as soon
+// as the first layer has consumed the buffer), its leader issues the six
+// layers' MMAs, and its four warps read the accumulator lanes of their
+// rows (warp q of the team: lanes 32 q ... 32 q + 31) for the ReLU / BF16
+// epilogue.  The four teams' MMAs, epilogues and copies overlap.
+constexpr uint32_t kInferTeams = 4;
+constexpr uint32_t kInferThreads = 128 * kInferTeams;
+constexpr uint32_t kInferTeamBytes = kNrcTileBytes + 2 * 128 * kNrcHid * 2;
+
+__global__ void __launch_bounds__(kInferThreads, 1) k_nrc_infer(const __grid_constant__ NrcParams C,
+                                                                const unsigned char *x0g,
+                                                                uint32_t n, float *out,
+                                                                uint32_t *err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar_mma[kInferTeams];
+  __shared__ __align__(8) uint64_t mbar_x[kInferTeams];
   __shared__ uint32_t tmem_base;
   const uint32_t tid = threadIdx.x;
-  unsigned char *w = smem;                    // forward weights, kNrcWeightBytes
-  unsigned char *x0 = w + kNrcWeightBytes;    // [128][kNrcIn]
-  unsigned char *ha = x0 + 128 * kNrcIn * 2;  // [128][64]
-  unsigned char *hb = ha + 128 * kNrcHid * 2; // [128][64]
+  const uint32_t team = tid / 128, ttid = tid % 128;
+  const uint32_t bar_id = 1 + team; // named barrier of the team (0 is __syncthreads)
+  unsigned char *w = smem;          // forward weights, kNrcWeightBytes
+  unsigned char *x0 = smem + kNrcWeightBytes + team * kInferTeamBytes; // [128][kNrcIn]
+  unsigned char *ha = x0 + kNrcTileBytes;                               // [128][64]
+  unsigned char *hb = ha + 128 * kNrcHid * 2;                           // [128][64]
   copy16(w, C.w_fwd, kNrcWeightBytes, tid, kInferThreads);
   if (tid < 32) {
-    tc::tmem_alloc(tc::smem_addr(&tmem_base), 64);
+    tc::tmem_alloc(tc::smem_addr(&tmem_base), 64 * kInferTeams);
   }
-  if (tid == 0) {
-    tc::mbar_init(tc::smem_addr(&mbar), 1);
+  if (tid < kInferTeams) {
+    tc::mbar_init(tc::smem_addr(&mbar_mma[tid]), 1);
+    tc::mbar_init(tc::smem_addr(&mbar_x[tid]), 1);
   }
   tc_barrier();
-  TcSync sync{tc::smem_addr(&mbar), 0, true};
-  const uint32_t tmem = tmem_base;
-  const uint32_t warp = tid / 32;
-  const uint32_t quarter = warp % 4, cgroup = warp / 4;
-  const uint32_t erow = quarter * 32 + (tid & 31); // epilogue row
-  const uint32_t qrow = tid % 128, lgroup = tid / 128; // encoding row, level group
-  for (uint32_t tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
-    const uint32_t qi = tile * 128 + qrow;
-    float in[8];
-    const uint32_t l0 = lgroup * 4;
-    const bool used = qi < n && (live == nullptr || live[3 * (size_t)qi] != 0.f ||
-                                 live[3 * (size_t)qi + 1] != 0.f ||
-                                 live[3 * (size_t)qi + 2] != 0.f);
-    if (used) {
-      nrc_encode_levels<4>(C, queries + (size_t)qi * 12, l0, in);
-    } else {
-      for (int k = 0; k < 8; ++k) {
-        in[k] = 0.f;
-      }
+  const uint32_t tmem = tmem_base + 64 * team;
+  const uint32_t mm = tc::smem_addr(&mbar_mma[team]), mx = tc::smem_addr(&mbar_x[team]);
+  const uint32_t quarter = ttid / 32;
+  const uint32_t erow = ttid; // epilogue row: warp quarter's lanes
+  const uint32_t n_tiles = (n + 127) / 128;
+  const uint32_t stride = gridDim.x * kInferTeams;
+  uint32_t tile = blockIdx.x * kInferTeams + team;
+  uint32_t phase_m = 0, phase_x = 0;
+  bool copying = false; // the leader's bulk copy into x0 not yet waited for
+  bool ok = true;
+  if (ttid == 0 && tile < n_tiles) {
+    tc::mbar_arrive_expect_tx(mx, kNrcTileBytes);
+    tc::bulk_g2s(tc::smem_addr(x0), x0g + (size_t)tile * kNrcTileBytes, kNrcTileBytes, mx);
+    copying = true;
+  }
+  for (; tile < n_tiles && ok; tile += stride) {
+    ok = tc::bar_and(bar_id, 128, tc::mbar_wait(mx, phase_x, kTcWaitLimit));
+    phase_x ^= 1u;
+    copying = false;
+    if (!ok) {
+      break;
     }
-    for (uint32_t k = 0; k < 8; ++k) {
-      store_bf16(x0, qrow, 2 * l0 + k, kNrcIn, in[k]);
-    }
-    if (lgroup == 0) {
-      for (uint32_t k = 0; k < 9; ++k) {
-        store_bf16(x0, qrow, 32 + k, kNrcIn, used ? queries[(size_t)qi * 12 + 3 + k] : 0.f);
-      }
-      for (uint32_t k = 41; k < kNrcIn; ++k) {
-        store_bf16(x0, qrow, k, kNrcIn, 0.f);
-      }
-    }
-    tc_barrier();
+    tc::fence_after_sync();
     const unsigned char *a = x0;
-    const uint32_t oi = tile * 128 + erow;
     for (uint32_t l = 0; l < kNrcLayers; ++l) {
       const uint32_t k_dim = nrc_in_dim(l), n_dim = nrc_out_dim(l);
-      tc_layer(sync, tid, tmem, a, w + nrc_weight_offset(l) * 2, k_dim, n_dim, 0);
-      tc_wait(sync, tid, err);
-      if (!sync.ok) {
+      if (ttid == 0) {
+        const uint32_t idesc = tc::idesc_bf16(128, n_dim);
+        const unsigned char *b = w + nrc_weight_offset(l) * 2;
+        for (uint32_t k0 = 0; k0 < k_dim; k0 += 16) {
+          tc::mma_bf16(tmem, tc::smem_desc(tc::smem_addr(a) + k0 * 16, k_dim),
+                       tc::smem_desc(tc::smem_addr(b) + k0 * 16, k_dim), idesc,
+                       k0 > 0 ? 1u : 0u);
+        }
+        tc::commit(mm);
+      }
+      ok = tc::bar_and(bar_id, 128, tc::mbar_wait(mm, phase_m, kTcWaitLimit));
+      phase_m ^= 1u;
+      if (!ok) {
         break;
       }
+      tc::fence_after_sync();
+      if (l == 0 && ttid == 0 && tile + stride < n_tiles) {
+        // the first layer has read x0: copy the team's next tile in
+        tc::mbar_arrive_expect_tx(mx, kNrcTileBytes);
+        tc::bulk_g2s(tc::smem_addr(x0), x0g + (size_t)(tile + stride) * kNrcTileBytes,
+                     kNrcTileBytes, mx);
+        copying = true;
+      }
       unsigned char *dst = (l & 1) ? hb : ha;
-      const uint32_t c0 = 16 * cgroup;
-      if (c0 < n_dim) {
-        float v[16];
-        tc::tmem_ld16(tmem + ((quarter * 32) << 16) + c0, v);
-        if (l + 1 < kNrcLayers) {
-          for (int j = 0; j < 16; ++j) {
-            store_bf16(dst, erow, c0 + j, kNrcHid, fmaxf(v[j], 0.f));
+      const uint32_t lane_base = (quarter * 32) << 16;
+      if (l + 1 < kNrcLayers) {
+#pragma unroll
+        for (uint32_t c0 = 0; c0 < kNrcHid; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(tmem + lane_base + c0, v);
+          float lo[8], hi[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            lo[j] = fmaxf(v[j], 0.f);
+            hi[j] = fmaxf(v[8 + j], 0.f);
           }
-        } else if (oi < n) {
+          *reinterpret_cast<uint4 *>(dst + smem_offset(erow, c0, kNrcHid)) = pack_bf16x8(lo);
+          *reinterpret_cast<uint4 *>(dst + smem_offset(erow, c0 + 8, kNrcHid)) =
+              pack_bf16x8(hi);
+        }
+      } else {
+        float v[16];
+        tc::tmem_ld16(tmem + lane_base, v);
+        const uint32_t oi = tile * 128 + erow;
+        if (oi < n) {
           out[(size_t)oi * 3 + 0] = v[0];
           out[(size_t)oi * 3 + 1] = v[1];
           out[(size_t)oi * 3 + 2] = v[2];
         }
       }
-      tc_barrier();
+      // epilogue writes visible to the tensor core, tensor-memory reads
+      // ordered before the next MMA
+      tc::fence_async_smem();
+      tc::fence_before_sync();
+      tc::bar_sync(bar_id, 128);
+      tc::fence_after_sync();
       a = dst;
     }
-    if (!sync.ok) {
-      break;
+  }
+  if (!ok) {
+    if (ttid == 0) {
+      atomicExch(err, 1u);
+    }
+    if (copying) {
+      // a bulk copy still in flight lands before the CTA may exit
+      tc::mbar_wait(mx, phase_x, kTcWaitLimit);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   if (tid < 32) {
-    tc::tmem_dealloc(tmem, 64);
+    tc::tmem_dealloc(tmem_base, 64 * kInferTeams);
   }
 }
 
@@ -602,7 +697,11 @@ __global__ void k_adam(float *param, float *grad, float *m, float *v, size_t n, 
 } // namespace dev
 
 size_t nrc_infer_smem_bytes() {
-  return kNrcWeightBytes + 128 * kNrcIn * 2 + 2 * 128 * kNrcHid * 2;
+  return kNrcWeightBytes + dev::kInferTeams * dev::kInferTeamBytes;
+}
+
+size_t nrc_encoded_bytes(uint32_t n) {
+  return (size_t)((n + 127) / 128) * dev::kNrcTileBytes;
 }
 
 size_t nrc_train_smem_bytes() {
@@ -615,15 +714,21 @@ size_t nrc_train_scratch_bytes(int grid) {
 }
 
 cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n,
-                             const float *live, float *out, uint32_t *err, int grid,
-                             cudaStream_t s) {
+                             const float *live, float *out, unsigned char *encoded,
+                             uint32_t *err, int grid, cudaStream_t s) {
   const size_t smem = nrc_infer_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(dev::k_nrc_infer,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess || n == 0) {
     return e;
   }
-  dev::k_nrc_infer<<<grid, dev::kInferThreads, smem, s>>>(c, queries, n, live, out, err);
+  const uint32_t n_rows = (n + 127) / 128 * 128;
+  dev::k_nrc_encode<<<(n_rows * 4 + 255) / 256, 256, 0, s>>>(c, queries, n, n_rows, live,
+                                                             encoded);
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    return e;
+  }
+  dev::k_nrc_infer<<<grid, dev::kInferThreads, smem, s>>>(c, encoded, n, out, err);
   return cudaGetLastError();
 }
 

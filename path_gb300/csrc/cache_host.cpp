@@ -16,16 +16,18 @@ namespace pg {
     }                                                                          \
   } while (0)
 
-namespace {
-constexpr int kTrainGrid = 148; // one 128-thread CTA per SM (512 tensor-memory columns)
-constexpr int kInferGrid = 304;
-} // namespace
+// grids: one training CTA per SM (each holds all 512 tensor-memory
+// columns) and one inference CTA per SM (its four teams take 221 KB of
+// shared memory)
 
 Status RadianceCache::init(uint32_t seed, float lr) {
   if (ready_) {
     return Status::ok();
   }
   PG_TRY_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  int dev = 0;
+  PG_TRY_CUDA(cudaGetDevice(&dev), "device");
+  PG_TRY_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev), "sm count");
   lr_ = lr;
   const size_t nt = (size_t)kNrcLevels * kNrcTable * 2;
   // Xavier-uniform weights (rows 3.. of the output layer stay zero), small
@@ -60,7 +62,7 @@ Status RadianceCache::init(uint32_t seed, float lr) {
   }
   PG_TRY_CUDA(wfwd_.ensure(kNrcWeightBytes), "cache images");
   PG_TRY_CUDA(wbwd_.ensure(kNrcWeightBytes), "cache images");
-  PG_TRY_CUDA(scratch_.ensure(nrc_train_scratch_bytes(kTrainGrid)), "cache scratch");
+  PG_TRY_CUDA(scratch_.ensure(nrc_train_scratch_bytes(sms_)), "cache scratch");
   PG_TRY_CUDA(err_.ensure(4), "cache flags");
   PG_TRY_CUDA(loss_.ensure(4), "cache flags");
   PG_TRY_CUDA(launch_nrc_pack_weights(w_.as<float>(), wfwd_.as<unsigned char>(),
@@ -125,8 +127,9 @@ Status RadianceCache::check_err(const char *what) {
 Status RadianceCache::infer(const float *queries, uint32_t n, float *out, cudaStream_t s,
                             const float *live) {
   PG_TRY_CUDA(cudaMemsetAsync(err_.get(), 0, 4, s), "cache query");
-  PG_TRY_CUDA(launch_nrc_infer(params(), queries, n, live, out, err_.as<uint32_t>(), kInferGrid,
-                               s),
+  PG_TRY_CUDA(encoded_.ensure(std::max<size_t>(nrc_encoded_bytes(n), 16)), "cache query");
+  PG_TRY_CUDA(launch_nrc_infer(params(), queries, n, live, out, encoded_.as<unsigned char>(),
+                               err_.as<uint32_t>(), sms_, s),
               "cache query");
   return Status::ok();
 }
@@ -142,7 +145,7 @@ Status RadianceCache::gradients(const float *records, uint32_t n, float *loss) {
   PG_TRY_CUDA(launch_nrc_train(c, records, n, 1.f / (float)std::max<uint32_t>(n, 1),
                                gw_.as<float>(), dfeat_.as<float>(),
                                scratch_.as<unsigned char>(), loss_.as<float>(),
-                               err_.as<uint32_t>(), kTrainGrid, stream_),
+                               err_.as<uint32_t>(), sms_, stream_),
               "cache train");
   PG_TRY_CUDA(launch_nrc_grid_backward(c, records, n, dfeat_.as<float>(), gt_.as<float2>(),
                                        stream_),

@@ -45,8 +45,9 @@ private:
   float level_res_[kNrcLevels] = {};
   float lo_[3] = {}, inv_ext_[3] = {};
   bool batch_ = false;
+  int sms_ = 0;
   DeviceBuffer table_, w_, gw_, mw_, vw_, gt_, mt_, vt_, wfwd_, wbwd_, dfeat_, scratch_, err_,
-      loss_;
+      loss_, encoded_;
 };
 
 } // namespace pg

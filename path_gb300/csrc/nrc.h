@@ -70,10 +70,12 @@ struct NrcParams {
   const unsigned char *w_bwd; // BF16 [in][out] K-major tiles
 };
 
-// live: optional [n][3], a query whose three values are zero is skipped
+// live: optional [n][3], a query whose three values are zero is skipped;
+// encoded: nrc_encoded_bytes(n) of scratch for the encoded input tiles
 cudaError_t launch_nrc_infer(const NrcParams &c, const float *queries, uint32_t n,
-                             const float *live, float *out, uint32_t *err, int grid,
-                             cudaStream_t s);
+                             const float *live, float *out, unsigned char *encoded,
+                             uint32_t *err, int grid, cudaStream_t s);
+size_t nrc_encoded_bytes(uint32_t n);
 cudaError_t launch_nrc_train(const NrcParams &c, const float *records, uint32_t n,
                              float inv_batch, float *grad_w, float *d_feat,
                              unsigned char *scratch, float *loss, uint32_t *err, int grid,

@@ -88,6 +88,44 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, uint32_
   return false;
 }
 
+// arrive on the mbarrier and expect `bytes` of asynchronous copies to
+// complete on it in this phase
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar),
+               "r"(bytes)
+               : "memory");
+}
+
+// bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to this CTA's shared memory, completing on the mbarrier
+__device__ __forceinline__ void bulk_g2s(uint32_t dst_smem, const void *src, uint32_t bytes,
+                                         uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];\n" ::"r"(dst_smem),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
+// barrier `id` (1..15) over `count` threads (a multiple of 32), returning
+// whether `pred` held in every one of them
+__device__ __forceinline__ bool bar_and(uint32_t id, uint32_t count, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.and.pred p, %2, %3, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"(pred ? 1u : 0u), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t count) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+
 // tensor-memory allocation of ncols columns (a power of two >= 32) by one
 // whole warp; the base address is written to *dst (shared memory)
 __device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
