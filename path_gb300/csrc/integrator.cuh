@@ -447,91 +447,6 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t r) {
   return pos;
 }
 
-// The leaf triangles the warp's lanes took from their last nodes, tested by
-// the whole warp: the work items (lane, triangle) are numbered lane-major
-// and dealt out 32 per round, each item's ray fetched from its lane by
-// shuffle.  The closest hit per lane is a minimum of 64-bit keys (distance
-// bits, then BVH index, then the back flag; distances are positive, so the
-// bit order is the numeric order), reduced over each lane's run of items
-// and folded into the lane's walk: the same order-independent result the
-// lane's own loop gives.  All 32 lanes call this.
-template <bool kCount>
-__device__ __forceinline__ void warp_triangles(const RenderParams &P, WideWalk &w,
-                                               uint32_t tri_base, uint32_t tmask,
-                                               uint32_t lane, Counts &cnt) {
-  const uint32_t c = __popc(tmask);
-  uint32_t incl = c;
-#pragma unroll
-  for (uint32_t off = 1; off < 32; off <<= 1) {
-    const uint32_t v = __shfl_up_sync(kFull, incl, off);
-    if (lane >= off) {
-      incl += v;
-    }
-  }
-  const uint32_t total = __shfl_sync(kFull, incl, 31);
-  if (total == 0) {
-    return;
-  }
-  const uint32_t excl = incl - c;
-  unsigned long long mine = ~0ull;
-  for (uint32_t base = 0; base < total; base += 32) {
-    const uint32_t g = base + lane;
-    const bool valid = g < total;
-    // owner: the first lane whose inclusive count exceeds g
-    uint32_t pos = 0;
-#pragma unroll
-    for (uint32_t step = 16; step > 0; step >>= 1) {
-      if (__shfl_sync(kFull, incl, pos + step - 1) <= g) {
-        pos += step;
-      }
-    }
-    const uint32_t owner = valid ? pos : 32u;
-    const uint32_t src = pos;
-    const uint32_t o_excl = __shfl_sync(kFull, excl, src);
-    const uint32_t o_mask = __shfl_sync(kFull, tmask, src);
-    const uint32_t o_base = __shfl_sync(kFull, tri_base, src);
-    ray r;
-    r.o = mk(__shfl_sync(kFull, w.r.o.x, src), __shfl_sync(kFull, w.r.o.y, src),
-             __shfl_sync(kFull, w.r.o.z, src));
-    r.d = mk(__shfl_sync(kFull, w.r.d.x, src), __shfl_sync(kFull, w.r.d.y, src),
-             __shfl_sync(kFull, w.r.d.z, src));
-    unsigned long long key = ~0ull;
-    if (valid) {
-      const uint32_t k = o_base + nth_set_bit(o_mask, g - o_excl);
-      Hit h = no_hit();
-      wide_tri(P, r, k, h);
-      if (h.ok) {
-        key = ((unsigned long long)__float_as_uint(h.t) << 32) |
-              (unsigned long long)((h.idx << 1) | (h.back ? 1u : 0u));
-      }
-      if (kCount) {
-        ++cnt.tris;
-      }
-    }
-    // minimum over each owner's contiguous run of lanes, held by its first lane
-#pragma unroll
-    for (uint32_t off = 1; off < 32; off <<= 1) {
-      const unsigned long long ok = __shfl_down_sync(kFull, key, off);
-      const uint32_t oo = __shfl_down_sync(kFull, owner, off);
-      if (lane + off < 32 && oo == owner && ok < key) {
-        key = ok;
-      }
-    }
-    const uint32_t head = (excl > base ? excl : base) - base;
-    const unsigned long long seg = __shfl_sync(kFull, key, head & 31u);
-    if (c > 0 && excl < base + 32 && incl > base && seg < mine) {
-      mine = seg;
-    }
-  }
-  if (mine != ~0ull) {
-    const uint32_t lo = (uint32_t)mine;
-    fold_min(w.best, __uint_as_float((uint32_t)(mine >> 32)), (lo & 1u) != 0, lo >> 1);
-    if (shadow_settled(w)) {
-      w.done = true;
-    }
-  }
-}
-
 // Per-warp shared-memory scratch of warp_triangles_shared: every lane's ray,
 // written when the lane takes the ray (the w components are not read), and
 // every lane's closest-hit key of the current step.
@@ -541,13 +456,18 @@ struct WarpTriScratch {
   unsigned long long key[32];
 };
 
-// warp_triangles with the rays read from shared memory instead of six
-// shuffles per round, and the per-lane minimum taken by 64-bit shared-memory
-// atomicMin from the items that hit instead of a segmented shuffle
-// reduction over every item.  The keys and the fold are those of
-// warp_triangles, so the result is the same bit for bit.  All 32 lanes call
-// this; sh.o / sh.d hold the ray of every lane with triangles, or, with
-// kStoreRay, each such lane writes its ray there first.
+// The leaf triangles the warp's lanes took from their last nodes, tested by
+// the whole warp: the work items (lane, triangle) are numbered lane-major
+// (a shuffle scan) and dealt out 32 per round; an item finds its owner lane
+// by a binary search over the lanes' inclusive counts, reads the owner's ray
+// from shared memory and runs Moller-Trumbore.  The closest hit per lane is
+// the minimum of 64-bit keys (distance bits, then BVH index, then the back
+// flag; distances are positive, so the bit order is the numeric order),
+// lowered by 64-bit shared-memory atomicMin from the items that hit and
+// folded into the lane's walk: the same order-independent result the lane's
+// own loop gives.  All 32 lanes call this; sh.o / sh.d hold the ray of every
+// lane with triangles, or, with kStoreRay, each such lane writes its ray
+// there first.
 template <bool kCount, bool kStoreRay = false>
 __device__ __forceinline__ void warp_triangles_shared(const RenderParams &P, WideWalk &w,
                                                       uint32_t tri_base, uint32_t tmask,
