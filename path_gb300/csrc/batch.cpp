@@ -26,6 +26,7 @@
 #include <chrono>
 #include <cstring>
 #include <exception>
+#include <mutex>
 
 namespace pg {
 
@@ -119,6 +120,56 @@ Status Renderer::check_batch(const std::vector<BatchItem> &items,
   return Status::ok();
 }
 
+namespace {
+
+// One scene's 8-wide BVH built on the GPU on stream s (d9 and g: the calling
+// thread's buffers, reused from scene to scene), downloaded into w (nodes,
+// leaf references) and b (the permutation).
+Status build_one_gpu(const FlatScene &f, bool split, cudaStream_t s, DeviceBuffer &d9,
+                     GpuWideBVH &g, WideBVH &w, BinaryBVH &b) {
+  const size_t nt = f.v0.size();
+  std::vector<float> t9(nt * 9);
+  for (size_t k = 0; k < nt; ++k) {
+    const f3 v[3] = {f.v0[k], f.v1[k], f.v2[k]};
+    for (int c = 0; c < 3; ++c) {
+      t9[9 * k + 3 * c] = v[c].x;
+      t9[9 * k + 3 * c + 1] = v[c].y;
+      t9[9 * k + 3 * c + 2] = v[c].z;
+    }
+  }
+  float lo[3], hi[3];
+  scene_box(f, lo, hi);
+  PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, s), "gpu build upload");
+  Status sg = gpu_build_wide(d9.as<float>(), (uint32_t)nt, lo, hi, split, s, g);
+  if (!sg.good()) {
+    return sg;
+  }
+  w.nodes.resize(g.n_nodes);
+  w.depth = g.depth;
+  const size_t nw = g.n_wide_tris;
+  std::vector<float> wt(nw * 12);
+  b.permutation.resize(nt);
+  if (nt > 0) {
+    PG_TRY_CUDA(cudaMemcpyAsync(w.nodes.data(), g.nodes.get(), g.n_nodes * sizeof(WideNode),
+                                cudaMemcpyDeviceToHost, s),
+                "gpu build download");
+    PG_TRY_CUDA(cudaMemcpyAsync(wt.data(), g.wide_tris.get(), nw * 48, cudaMemcpyDeviceToHost,
+                                s),
+                "gpu build download");
+    PG_TRY_CUDA(cudaMemcpyAsync(b.permutation.data(), g.perm.get(), nt * 4,
+                                cudaMemcpyDeviceToHost, s),
+                "gpu build download");
+  }
+  PG_TRY_CUDA(cudaStreamSynchronize(s), "gpu build download");
+  w.tri_index.resize(nw);
+  for (size_t k = 0; k < nw; ++k) {
+    std::memcpy(&w.tri_index[k], &wt[12 * k + 9], 4);
+  }
+  return Status::ok();
+}
+
+} // namespace
+
 Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSettings &sb,
                                uint32_t gpu_build) {
   std::vector<std::array<uint64_t, 3>> key;
@@ -165,54 +216,61 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
     }
   }
   if (gpu_build) {
-    // one GPU build per distinct scene; its wide nodes, leaf references and
+    // one GPU build per distinct scene, several at once: host threads with
+    // a stream each (the builder's scratch memory is stream-ordered, so the
+    // builds overlap); each scene's wide nodes, leaf references and
     // permutation come back for the arena assembly below
+    std::vector<size_t> todo;
+    size_t max_n = 0;
     for (size_t i = 0; i < n; ++i) {
-      if (first_of[i] != i || !errors[i].empty()) {
-        continue;
+      if (first_of[i] == i && errors[i].empty()) {
+        todo.push_back(i);
+        max_n = std::max(max_n, flats[i].v0.size());
       }
-      const FlatScene &f = flats[i];
-      const size_t nt = f.v0.size();
-      std::vector<float> t9(nt * 9);
-      for (size_t k = 0; k < nt; ++k) {
-        const f3 v[3] = {f.v0[k], f.v1[k], f.v2[k]};
-        for (int c = 0; c < 3; ++c) {
-          t9[9 * k + 3 * c] = v[c].x;
-          t9[9 * k + 3 * c + 1] = v[c].y;
-          t9[9 * k + 3 * c + 2] = v[c].z;
-        }
+    }
+    // largest first, so that the threads' buffers are sized by their first scene
+    std::sort(todo.begin(), todo.end(),
+              [&](size_t a, size_t b) { return flats[a].v0.size() > flats[b].v0.size(); });
+    int dev = 0;
+    PG_TRY_CUDA(cudaGetDevice(&dev), "device");
+    PG_TRY_CUDA(cudaStreamSynchronize(stream_), "gpu build");
+    const int n_threads = (int)std::min<size_t>(8, std::max<size_t>(todo.size(), 1));
+    std::vector<Status> build_status(n);
+    size_t next = 0;
+    std::mutex next_mutex;
+#pragma omp parallel num_threads(n_threads)
+    {
+      cudaStream_t bs = nullptr;
+      cudaError_t se = cudaSetDevice(dev);
+      if (se == cudaSuccess) {
+        se = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
       }
-      float lo[3], hi[3];
-      scene_box(f, lo, hi);
       DeviceBuffer d9;
-      PG_TRY_CUDA(d9.upload(t9.data(), t9.size() * 4, stream_), "gpu build upload");
       GpuWideBVH g;
-      Status sg = gpu_build_wide(d9.as<float>(), (uint32_t)nt, lo, hi, gpu_build == 2, stream_,
-                                 g);
-      if (!sg.good()) {
-        return sg;
+      while (true) {
+        size_t k;
+        {
+          std::lock_guard<std::mutex> lock(next_mutex);
+          k = next++;
+        }
+        if (k >= todo.size()) {
+          break;
+        }
+        const size_t i = todo[k];
+        if (se != cudaSuccess) {
+          build_status[i] = cuda_status(se, "gpu build stream");
+          continue;
+        }
+        build_status[i] = build_one_gpu(flats[i], gpu_build == 2, bs, d9, g, wides[i], bvhs[i]);
       }
-      WideBVH &w = wides[i];
-      w.nodes.resize(g.n_nodes);
-      w.depth = g.depth;
-      const size_t nw = g.n_wide_tris;
-      std::vector<float> wt(nw * 12);
-      bvhs[i].permutation.resize(nt);
-      if (nt > 0) {
-        PG_TRY_CUDA(cudaMemcpyAsync(w.nodes.data(), g.nodes.get(), g.n_nodes * sizeof(WideNode),
-                                    cudaMemcpyDeviceToHost, stream_),
-                    "gpu build download");
-        PG_TRY_CUDA(cudaMemcpyAsync(wt.data(), g.wide_tris.get(), nw * 48,
-                                    cudaMemcpyDeviceToHost, stream_),
-                    "gpu build download");
-        PG_TRY_CUDA(cudaMemcpyAsync(bvhs[i].permutation.data(), g.perm.get(), nt * 4,
-                                    cudaMemcpyDeviceToHost, stream_),
-                    "gpu build download");
+      if (bs != nullptr) {
+        cudaStreamSynchronize(bs);
+        cudaStreamDestroy(bs);
       }
-      PG_TRY_CUDA(cudaStreamSynchronize(stream_), "gpu build download");
-      w.tri_index.resize(nw);
-      for (size_t k = 0; k < nw; ++k) {
-        std::memcpy(&w.tri_index[k], &wt[12 * k + 9], 4);
+    }
+    for (size_t i : todo) {
+      if (!build_status[i].good()) {
+        return build_status[i];
       }
     }
   }

@@ -675,6 +675,52 @@ __global__ void k_collapse(const float *t9, const uint32_t *perm, const uint32_t
 
 namespace {
 
+// the stream of the build this host thread is running (its scratch buffers
+// are allocated and freed in that stream's order)
+thread_local cudaStream_t t_build_stream = nullptr;
+
+// Scratch device memory of one build: cudaMallocAsync / cudaFreeAsync in the
+// build's stream, which, unlike cudaFree, do not synchronise the device, so
+// builds run from several host threads on their own streams overlap.
+class ScratchBuffer {
+public:
+  ScratchBuffer() = default;
+  ScratchBuffer(const ScratchBuffer &) = delete;
+  ScratchBuffer &operator=(const ScratchBuffer &) = delete;
+  ~ScratchBuffer() { release(); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= size_ && ptr_ != nullptr) {
+      return cudaSuccess;
+    }
+    release();
+    if (bytes == 0) {
+      return cudaSuccess;
+    }
+    stream_ = t_build_stream;
+    cudaError_t e = cudaMallocAsync(&ptr_, bytes, stream_);
+    if (e != cudaSuccess) {
+      ptr_ = nullptr;
+      return e;
+    }
+    size_ = bytes;
+    return cudaSuccess;
+  }
+  void release() {
+    if (ptr_ != nullptr) {
+      cudaFreeAsync(ptr_, stream_);
+      ptr_ = nullptr;
+      size_ = 0;
+    }
+  }
+  void *get() const { return ptr_; }
+  template <typename T> T *as() const { return static_cast<T *>(ptr_); }
+
+private:
+  void *ptr_ = nullptr;
+  size_t size_ = 0;
+  cudaStream_t stream_ = nullptr;
+};
+
 // the binary tree over the Morton-sorted triangles by PLOC (left, right:
 // internal nodes 0..n-2, 0 the root; parent of every node)
 Status ploc_tree(const box *item_box, uint32_t n, uint32_t *left, uint32_t *right,
@@ -687,7 +733,8 @@ Status ploc_tree(const box *item_box, uint32_t n, uint32_t *left, uint32_t *righ
     }                                                                          \
   } while (0)
   const size_t nn = n;
-  DeviceBuffer clus[2], cbox[2], nbr, keep, keep_pos, merges, merge_pos, tmp, tail;
+  t_build_stream = s;
+  ScratchBuffer clus[2], cbox[2], nbr, keep, keep_pos, merges, merge_pos, tmp, tail;
   for (int k = 0; k < 2; ++k) {
     PG_PL_TRY(clus[k].ensure(nn * 4), "ploc");
     PG_PL_TRY(cbox[k].ensure(nn * sizeof(box)), "ploc");
@@ -777,7 +824,8 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
     }                                                                          \
   } while (0)
   const size_t nn = n;
-  DeviceBuffer keys, vals, keys2, tmp, left, right, parent, boxes, flags, qa, qb, counters, cost,
+  t_build_stream = s;
+  ScratchBuffer keys, vals, keys2, tmp, left, right, parent, boxes, flags, qa, qb, counters, cost,
       how, wide_k, tri_count;
   PG_GB_TRY(keys.ensure(nn * 4), "gpu build");
   PG_GB_TRY(vals.ensure(nn * 4), "gpu build");
@@ -800,7 +848,7 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
                                             out.perm.as<uint32_t>(), (int)n, 0, 30, s),
             "radix sort");
   // the items the tree is built over: triangles, or their references
-  DeviceBuffer item_tri, item_box;
+  ScratchBuffer item_tri, item_box;
   uint32_t m = n;
   if (!split) {
     PG_GB_TRY(item_tri.ensure(nn * 4), "gpu build");
@@ -810,7 +858,7 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
     PG_GB_TRY(cudaGetLastError(), "items");
   } else {
     // budget: 30% more references than triangles, shared by priority
-    DeviceBuffer prio, count, offset, sum, ref_tri, ref_box, rkeys, rvals, rkeys2, rorder;
+    ScratchBuffer prio, count, offset, sum, ref_tri, ref_box, rkeys, rvals, rkeys2, rorder;
     PG_GB_TRY(prio.ensure(nn * 4), "gpu build");
     PG_GB_TRY(count.ensure(nn * 4), "gpu build");
     PG_GB_TRY(offset.ensure(nn * 4), "gpu build");
@@ -820,7 +868,7 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
     size_t rb = 0;
     PG_GB_TRY(cub::DeviceReduce::Sum(nullptr, rb, prio.as<float>(), sum.as<float>(), (int)n, s),
               "split budget");
-    DeviceBuffer rtmp;
+    ScratchBuffer rtmp;
     PG_GB_TRY(rtmp.ensure(std::max<size_t>(rb, 16)), "gpu build");
     PG_GB_TRY(cub::DeviceReduce::Sum(rtmp.get(), rb, prio.as<float>(), sum.as<float>(), (int)n, s),
               "split budget");
@@ -921,7 +969,7 @@ Status gpu_build_wide(const float *t9, uint32_t n, const float *lo, const float 
   PG_GB_TRY(cudaMemcpyAsync(qa.get(), &root, sizeof(root), cudaMemcpyHostToDevice, s),
             "gpu build");
   uint32_t n_in = 1, depth = 0;
-  DeviceBuffer *cur = &qa, *nxt = &qb;
+  ScratchBuffer *cur = &qa, *nxt = &qb;
   while (n_in > 0) {
     PG_GB_TRY(cudaMemsetAsync(counters.as<uint32_t>() + 2, 0, 4, s), "gpu build");
     dev::k_collapse<<<(n_in + 127) / 128, 128, 0, s>>>(
