@@ -130,7 +130,10 @@ typedef struct {
   uint32_t persistent_ctas_per_sm; /* 0 = one launch over all blocks */
   uint32_t count_work;       /* 1: count rays / nodes / triangles (slower) */
   uint32_t upload_scene_every_render; /* 1: re-copy the cached scene arrays
-                                         host -> device on every render */
+                                         the render reads (triangles, shading
+                                         data, its traversal's BVH, materials,
+                                         lights) host -> device on every
+                                         render */
   uint32_t trace_min_blocks; /* streaming trace kernel: resident 256-thread
                                 blocks per SM it is compiled for (3..6, 0 =
                                 default 4); fewer registers per thread above 3 */

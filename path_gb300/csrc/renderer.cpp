@@ -226,7 +226,7 @@ Status Renderer::upload_geometry(const FlatScene &flat,
     std::memcpy(st_perm_.get(), bvh.permutation.data(), bvh.permutation.size() * 4);
   }
   uint64_t bytes = 0;
-  Status sc = copy_staged(&bytes);
+  Status sc = copy_staged(&bytes, true, PATH_TRAVERSAL_WIDE8);
   if (!sc.good()) {
     return sc;
   }
@@ -377,18 +377,26 @@ Status Renderer::refresh_materials(const Scene &scene, uint64_t *bytes) {
 }
 
 // host -> device copies of every staged scene array (asynchronous)
-Status Renderer::copy_staged(uint64_t *bytes) {
+// The resident scene copied from its pinned staging copies: every array
+// (all), or only those a render with this traversal reads (the binary or
+// the 8-wide BVH, not both; the permutation serves path_intersect only).
+Status Renderer::copy_staged(uint64_t *bytes, bool all, uint32_t traversal) {
   struct Pair {
     DeviceBuffer *dev;
     PinnedBuffer *host;
+    bool used;
   };
-  Pair pairs[] = {{&tris_, &st_tris_},       {&tri_data_, &st_data_},
-                  {&bin_nodes_, &st_nodes_}, {&extra_, &st_extra_},
-                  {&wide_nodes_, &st_wnodes_}, {&wide_tris_, &st_wtris_},
-                  {&materials_, &st_mats_},  {&light_tris_, &st_lights_},
-                  {&light_cdf_, &st_cdf_},   {&perm_, &st_perm_}};
+  const bool wide = traversal == PATH_TRAVERSAL_WIDE8;
+  const Pair pairs[] = {{&tris_, &st_tris_, true},          {&tri_data_, &st_data_, true},
+                        {&bin_nodes_, &st_nodes_, !wide},    {&extra_, &st_extra_, !wide},
+                        {&wide_nodes_, &st_wnodes_, wide},   {&wide_tris_, &st_wtris_, wide},
+                        {&materials_, &st_mats_, true},      {&light_tris_, &st_lights_, true},
+                        {&light_cdf_, &st_cdf_, true},       {&perm_, &st_perm_, false}};
   uint64_t total = 0;
   for (const Pair &p : pairs) {
+    if (!all && !p.used) {
+      continue;
+    }
     PG_TRY_CUDA(p.dev->upload(p.host->get(), p.host->bytes, stream_), "scene upload");
     total += p.host->bytes;
   }
@@ -657,7 +665,7 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
     return sf;
   }
   if (!rebuilt && st.upload_scene_every_render) {
-    Status sr = copy_staged(&h2d);
+    Status sr = copy_staged(&h2d, false, st.traversal);
     if (!sr.good()) {
       return sr;
     }

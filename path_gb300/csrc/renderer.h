@@ -172,7 +172,7 @@ private:
   Status prepare_scene(const FlatScene &flat, uint64_t id, uint64_t version,
                        const SBVHSettings &sbvh, bool force);
   Status upload_geometry(const FlatScene &flat, const std::vector<path_material> &mats);
-  Status copy_staged(uint64_t *bytes);
+  Status copy_staged(uint64_t *bytes, bool all, uint32_t traversal);
   void stage_materials(const FlatScene &flat, const std::vector<path_material> &mats);
   Status refresh_materials(const Scene &scene, uint64_t *bytes);
   Status prepare_scene_gpu(const FlatScene &flat, uint64_t id, uint64_t version,
