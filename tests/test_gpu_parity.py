@@ -629,3 +629,22 @@ def test_wide_traversal_on_adversarial_rays(lib, oracle):
         assert np.array_equal(bits(wt[hit]), bits(gt[hit]))
         # equal distances may name another triangle (the tie rules differ)
         assert np.all((want == got) | hit)
+
+
+@pytest.mark.parametrize("traversal", ["binary", "wide"])
+def test_scene_reupload_renders_the_same_image(lib, traversal):
+    """upload_scene_every_render (the bench's end-to-end leg) re-copies the
+    arrays the traversal reads and renders the same image bit for bit."""
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(5, traversal)
+    w = h = 24
+    f2w = scenes.cornell_camera(w, h)
+    r = api.Renderer()
+    a = np.zeros((h, w, 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), a, sc, 8, s)
+    e = s.copy()
+    e.upload_scene_every_render = 1
+    b = np.zeros((h, w, 3), np.float32)
+    r.render(api.ExecutionModel.GPU, api.SquareImage(w, h, f2w), b, sc, 8, e)
+    assert r.stats()["h2d_bytes"] > 0
+    assert np.array_equal(bits(a), bits(b))
