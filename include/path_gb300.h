@@ -298,6 +298,12 @@ path_status path_renderer_stats(const path_renderer *renderer,
  * one tcgen05 MMA tile; k, n multiples of 16 in [16, 128]; host buffers */
 path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k, uint32_t n,
                                float *d);
+/* The bounded wait of the tensor-core kernels, made to run out: the
+ * self-test kernel issues no MMA, so nothing arrives on its mbarrier and
+ * its wait gives up after `polls` polls; returns PATH_ERR_DEVICE_TIMEOUT
+ * (the status a render or cache call returns when a wait gives up), after
+ * which the device is usable as before. */
+path_status path_debug_tc_wait_timeout(uint32_t polls);
 
 /* ---- adjoint (GB300 addition; the reference has no derivatives) ---- */
 /* Gradients of a loss of the rendered image with respect to each material's

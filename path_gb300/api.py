@@ -563,6 +563,12 @@ def debug_tc_gemm(a, b):
     return d, bf16_value(ab), bf16_value(bb)
 
 
+def debug_tc_wait_timeout(polls=1 << 16):
+    """path_debug_tc_wait_timeout: the status of a tensor-core wait made to
+    run out (PATH_ERR_DEVICE_TIMEOUT expected)."""
+    return int(capi.load().path_debug_tc_wait_timeout(int(polls)))
+
+
 class RadianceCache:
     """Neural radiance cache (path_cache_*): hash-grid encoding + BF16 MLP on
     the tensor cores, trained online with Adam."""

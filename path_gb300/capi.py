@@ -145,6 +145,7 @@ SIGNATURES = {
                                           ctypes.POINTER(Output), _P, c_u32,
                                           ctypes.POINTER(PathSettings), c_u32, c_u32, c_u32,
                                           ctypes.POINTER(ctypes.c_double)]),
+    "path_debug_tc_wait_timeout": (ctypes.c_int, [c_u32]),
     "path_debug_tc_gemm": (ctypes.c_int, [ctypes.POINTER(ctypes.c_uint16),
                                           ctypes.POINTER(ctypes.c_uint16), c_u32, c_u32, _PF]),
     "path_render_adjoint": (ctypes.c_int, [_P, ctypes.POINTER(SampleSpec), _P, c_u32,

@@ -16,11 +16,15 @@ namespace dev {
 constexpr uint32_t kTcWaitLimit = 1u << 24; // polls before a wait gives up
 
 // D [128][n] = A [128][k] . B [n][k]^T, BF16 in, FP32 out, one CTA of 128
-// threads.  err: set to 1 when the tensor core did not signal completion.
+// threads.  err: set to 1 when the tensor core did not signal completion
+// within wait_limit polls of the mbarrier.  With issue 0 no MMA is issued
+// and nothing arrives on the mbarrier: the wait runs out, which is how the
+// tests exercise the bounded waits without faulting anything.
 __global__ void __launch_bounds__(128) k_tc_gemm(const __nv_bfloat16 *a,
                                                  const __nv_bfloat16 *b, float *d,
                                                  uint32_t k_dim, uint32_t n_dim,
-                                                 uint32_t *err) {
+                                                 uint32_t *err, uint32_t wait_limit,
+                                                 uint32_t issue) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
@@ -51,7 +55,7 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const __nv_bfloat16 *a,
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
-  if (tid == 0) {
+  if (tid == 0 && issue != 0) {
     const uint32_t idesc = tc::idesc_bf16(128, n_dim);
     for (uint32_t k0 = 0; k0 < k_dim; k0 += 16) {
       const uint64_t ad = tc::smem_desc(tc::smem_addr(sa) + k0 * 16, k_dim);
@@ -60,7 +64,7 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const __nv_bfloat16 *a,
     }
     tc::commit(tc::smem_addr(&mbar));
   }
-  const bool ok = tc::mbar_wait(tc::smem_addr(&mbar), 0, kTcWaitLimit);
+  const bool ok = __syncthreads_and(tc::mbar_wait(tc::smem_addr(&mbar), 0, wait_limit)) != 0;
   tc::fence_after_sync();
   if (!ok) {
     if (tid == 0) {
@@ -87,7 +91,8 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const __nv_bfloat16 *a,
 } // namespace dev
 
 cudaError_t launch_tc_gemm(const void *a, const void *b, float *d, uint32_t k_dim,
-                           uint32_t n_dim, uint32_t *err, cudaStream_t s) {
+                           uint32_t n_dim, uint32_t *err, cudaStream_t s, uint32_t wait_limit,
+                           bool issue) {
   const size_t smem = (size_t)(128 + n_dim) * k_dim * 2;
   cudaError_t e = cudaFuncSetAttribute(dev::k_tc_gemm,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -96,7 +101,8 @@ cudaError_t launch_tc_gemm(const void *a, const void *b, float *d, uint32_t k_di
   }
   dev::k_tc_gemm<<<1, 128, smem, s>>>(static_cast<const __nv_bfloat16 *>(a),
                                       static_cast<const __nv_bfloat16 *>(b), d, k_dim, n_dim,
-                                      err);
+                                      err, wait_limit == 0 ? dev::kTcWaitLimit : wait_limit,
+                                      issue ? 1u : 0u);
   return cudaGetLastError();
 }
 

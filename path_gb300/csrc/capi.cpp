@@ -450,6 +450,33 @@ path_status path_debug_tc_gemm(const uint16_t *a, const uint16_t *b, uint32_t k,
   });
 }
 
+path_status path_debug_tc_wait_timeout(uint32_t polls) {
+  if (polls == 0) {
+    return fail(PATH_ERR_ARGUMENT, "polls must be positive");
+  }
+  return guarded([&]() -> path_status {
+    pg::DeviceBuffer da, db, dd, derr;
+    cudaStream_t s = nullptr;
+    cudaError_t e = cudaSuccess;
+    uint32_t err = 0;
+    if ((e = da.ensure((size_t)128 * 16 * 2)) != cudaSuccess ||
+        (e = db.ensure((size_t)16 * 16 * 2)) != cudaSuccess ||
+        (e = cudaMemset(da.get(), 0, (size_t)128 * 16 * 2)) != cudaSuccess ||
+        (e = cudaMemset(db.get(), 0, (size_t)16 * 16 * 2)) != cudaSuccess ||
+        (e = dd.ensure((size_t)128 * 16 * 4)) != cudaSuccess ||
+        (e = derr.upload(&err, 4, s)) != cudaSuccess ||
+        (e = pg::launch_tc_gemm(da.get(), db.get(), dd.as<float>(), 16, 16,
+                                derr.as<uint32_t>(), s, polls, false)) != cudaSuccess ||
+        (e = cudaMemcpy(&err, derr.get(), 4, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+      return from(pg::cuda_status(e, "tensor-core wait test"));
+    }
+    if (err != 0) {
+      return fail(PATH_ERR_DEVICE_TIMEOUT, "tensor-core wait gave up");
+    }
+    return PATH_OK;
+  });
+}
+
 path_status path_render_adjoint(path_renderer *renderer, const path_sample_spec *sample_spec,
                                 const path_scene *scene, uint32_t samples_per,
                                 const path_settings *settings, const float *d_image,

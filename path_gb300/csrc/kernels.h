@@ -223,8 +223,11 @@ cudaError_t launch_bsdf(const DevMaterial *mat, uint32_t op, const float *in, ui
                         float *out, cudaStream_t s);
 
 // tensor-core self-test: D [128][n] = A [128][k] . B [n][k]^T (BF16 in, FP32
-// out), one CTA; err set when the MMA did not complete
+// out), one CTA; err set when the MMA did not complete within wait_limit
+// polls (0: the kernels' limit); issue false: no MMA is issued, so the wait
+// runs out
 cudaError_t launch_tc_gemm(const void *a, const void *b, float *d, uint32_t k_dim,
-                           uint32_t n_dim, uint32_t *err, cudaStream_t s);
+                           uint32_t n_dim, uint32_t *err, cudaStream_t s,
+                           uint32_t wait_limit = 0, bool issue = true);
 
 } // namespace pg

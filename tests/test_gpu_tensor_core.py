@@ -20,3 +20,16 @@ def test_tc_gemm_matches_numpy(lib, k, n):
     err = np.abs(d - ref).max() / np.abs(ref).max()
     print(f"k={k} n={n} max rel err {err:.2e}")
     assert err < 1e-5
+
+
+def test_tensor_core_wait_that_runs_out_is_reported(lib):
+    """The tensor-core kernels' mbarrier waits are bounded: with no MMA
+    issued nothing arrives, the wait gives up, the call returns
+    PATH_ERR_DEVICE_TIMEOUT (4), and the device computes correctly after."""
+    assert api.debug_tc_wait_timeout(1 << 12) == 4
+    rng = np.random.default_rng(5)
+    a = rng.normal(size=(128, 32)).astype(np.float32)
+    b = rng.normal(size=(32, 32)).astype(np.float32)
+    d, ar, br = api.debug_tc_gemm(a, b)
+    ref = ar.astype(np.float64) @ br.astype(np.float64).T
+    assert np.abs(d - ref).max() / np.abs(ref).max() < 1e-5
