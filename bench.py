@@ -120,24 +120,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _profiled_traffic(kernel, args, shape):
-    """DRAM bytes per launch of the dominant kernel, from the committed ncu
-    summary of this workload (a line 'dram_bytes_per_launch: N' in
-    profiles/<kernel>_dram_<workload>.txt), or None when the summary is
-    missing or was taken at another launch shape (its 'launch_shape:'
-    line)."""
+def _profiled_traffic(kernel, args, shape, alg_bytes_per_launch):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary of this workload (profiles/<kernel>_dram_<workload>.txt): its
+    measured DRAM bytes per algorithmic byte ('dram_per_algorithmic_byte:')
+    times this run's algorithmic bytes per launch, or its
+    'dram_bytes_per_launch:' line; None when the summary is missing or was
+    taken at another launch shape (its 'launch_shape:' line)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_dram_{args.workload}.txt")
-    traffic, profiled_shape = None, None
+    traffic, ratio, profiled_shape = None, None, None
     try:
         with open(path) as f:
             for ln in f:
                 if ln.startswith("dram_bytes_per_launch:"):
                     traffic = float(ln.split(":", 1)[1])
+                elif ln.startswith("dram_per_algorithmic_byte:"):
+                    ratio = float(ln.split(":", 1)[1])
                 elif ln.startswith("launch_shape:"):
                     profiled_shape = ln.split(":", 1)[1].strip()
     except OSError:
         pass
-    return traffic if profiled_shape == shape else None
+    if profiled_shape != shape:
+        return None
+    return ratio * alg_bytes_per_launch if ratio is not None else traffic
 
 
 def _profiled_issue(kernel, args, shape):
@@ -826,7 +831,8 @@ def main():
              f"bvh={'gpu' + str(args.gpu_build) if args.gpu_build else 'sbvh'} "
              f"staged_nodes={settings.trace_staged_nodes}")
     full_size = args.size is None and args.spp is None
-    traffic = _profiled_traffic(kernel_name, args, shape) if full_size else None
+    traffic = (_profiled_traffic(kernel_name, args, shape, alg_bytes / launches_per_render)
+               if full_size else None)
     issue = _profiled_issue(kernel_name, args, shape) if full_size and streaming else None
     # the other side of the roofline: FP32 work (22 operations per box test,
     # 8 box tests per wide node, 45 per Moller-Trumbore test) against the

@@ -1002,8 +1002,15 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
   const uint32_t shade_grid = (uint32_t)num_sms_ * 4;
   uint32_t parity = 0;
   volatile uint32_t *live = h + 12;
+  // Iterations before the first live-count check: under NIters{N} a path
+  // that starts in the first iteration is shaded at most N + 1 times and its
+  // last light ray traced once more, so when every sample is in flight the
+  // first check after N + 2 iterations finds no live path; then 4 a round.
+  const uint32_t first_round =
+      p.term_prob == 1 ? std::min<uint32_t>(std::max<uint32_t>(p.term_iters + 2, 4), 64) : 4;
   for (uint32_t round = 0;; ++round) {
-    for (int k = 0; k < 4; ++k) {
+    const uint32_t iters = round == 0 ? first_round : 4;
+    for (uint32_t k = 0; k < iters; ++k) {
       if (time_trace) {
         PG_TRY_CUDA(cudaEventRecord(trace_event(2 * trace_timed_), stream_), "event");
       }
