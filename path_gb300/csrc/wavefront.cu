@@ -71,16 +71,21 @@ __device__ __forceinline__ uint32_t scene_of(const WaveParams &W, unsigned long 
 // Slot state: o (xyz, light target), d and ld (xyz, scene root node bits in
 // w, read by the trace kernel), multipliers, radiance so far, and
 // (id low word, id bits 32-39 | scene << 8, RNG dimension, iters | flags << 24).
+// A fresh path (iters 0: no vertex shaded yet) stores only o, d and the
+// state word: its light direction, multipliers and radiance are the start
+// values (path_begin_cam), which unpack_path restores.
 template <class S>
 __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
                                            const S &s, unsigned long long id,
-                                           uint32_t scene, uint32_t root) {
+                                           uint32_t scene, uint32_t root, bool fresh = false) {
   W.o[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.light_target);
   W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, __uint_as_float(root));
-  W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, __uint_as_float(root));
-  W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
-  W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
-  W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
+  if (!fresh) {
+    W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, __uint_as_float(root));
+    W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
+    W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
+    W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
+  }
   uint32_t flags = (s.has_next ? kFlagNext : 0u) | (s.has_light ? kFlagLight : 0u) |
                    (s.count_emission ? kFlagEmission : 0u);
   uint32_t dim = 0; // a Uniform path's generator state is in W.rng_state
@@ -165,6 +170,13 @@ __device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, u
   s.has_next = (flags & kFlagNext) != 0;
   s.has_light = (flags & kFlagLight) != 0;
   s.count_emission = (flags & kFlagEmission) != 0;
+  if (s.iters == 0) {
+    // a fresh path: only o, d and this word were stored
+    s.ld = mk(0.f, 0.f, 0.f);
+    s.multiplier = mkrgb(1.f, 1.f, 1.f);
+    s.light_mult = zero_rgb();
+    s.total = zero_rgb();
+  }
   unsigned long long local = id;
   uint32_t spp = P.spp, offset = P.sample_offset;
   if (W.scenes != nullptr) {
@@ -212,7 +224,7 @@ __device__ __forceinline__ void begin_sample(const WaveParams &W, uint32_t slot,
     path_begin_cam(W.P, cam, smp, x, y, s, W.rng_state + slot, W.n_slots);
     root = b.root;
   }
-  store_path(W, slot, s, id, scene, root);
+  store_path(W, slot, s, id, scene, root, true);
 }
 
 // slot i takes sample i; the first ray of each is queued
