@@ -324,6 +324,8 @@ def time_to_rmse(r, scene, w, h, f2w, settings, ref, cfg, max_frames, base, targ
     ref_norm = float(torch.linalg.norm(ref))
     out = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
     cache = api.RadianceCache(seed=1) if cfg is not None else None
+    if cache is not None and cfg.get("ema", 0.0) > 0.0:
+        cache.set_ema(cfg["ema"])
     acc = torch.zeros_like(ref)
     wall, frames, err, curve = 0.0, 0, None, []
 
@@ -364,7 +366,9 @@ def time_to_rmse(r, scene, w, h, f2w, settings, ref, cfg, max_frames, base, targ
             "hash grid 16x2x2^19, MLP 48-64x5-3 BF16 tcgen05, Adam 1e-2, "
             f"paths end into the cache at vertex {cfg['cache_depth']}, "
             f"{cfg['train_paths']} records x {cfg['train_steps']} steps per frame, "
-            f"{cfg['pretrain_frames']} training-only frames first")
+            f"{cfg['pretrain_frames']} training-only frames first"
+            + (f", inference on a moving average of the parameters (decay {cfg['ema']} "
+               "per Adam step)" if cfg.get("ema", 0.0) > 0.0 else ""))
     return res
 
 
@@ -435,13 +439,17 @@ def cache_study(r, scene, w, h, f2w, settings, ref, args, ref_note):
     spec_cfg = {"cache_depth": args.cache_depth, "train_paths": args.train_paths,
                 "train_steps": args.train_steps, "pretrain_frames": args.pretrain_frames}
     runs = {"cached": time_to_rmse(r, scene, w, h, f2w, settings, ref, spec_cfg,
-                                   args.max_frames, base)}
+                                   args.max_frames, base),
+            "cached_ema": time_to_rmse(r, scene, w, h, f2w, settings, ref,
+                                       dict(spec_cfg, ema=0.99), args.max_frames, base)}
     controls = {}
     if not args.no_tuned_cache:
         tuned = {"cache_depth": 3, "train_paths": 1 << 14, "train_steps": 2,
                  "pretrain_frames": 0}
         runs["cached_tuned"] = time_to_rmse(r, scene, w, h, f2w, settings, ref, tuned,
                                             args.max_frames, base)
+        runs["cached_tuned_ema"] = time_to_rmse(r, scene, w, h, f2w, settings, ref,
+                                                dict(tuned, ema=0.9), args.max_frames, base)
         controls["cached_tuned_untrained"] = time_to_rmse(
             r, scene, w, h, f2w, settings, ref, dict(tuned, train_steps=0), args.max_frames,
             base)

@@ -340,6 +340,11 @@ path_status path_cache_set_bounds(path_cache *cache, const float *lo, const floa
  * box onto [0, 1]^3) plus 2 * (i % 16, i / 16 % 16, i / 256); every cell has
  * grid vertices of its own.  path_cache_set_bounds returns to one scene box. */
 path_status path_cache_use_batch_cells(path_cache *cache);
+/* Inference (queries, cached renders) on an exponential moving average of
+ * the weights and table, avg = decay avg + (1 - decay) param after every
+ * Adam step, starting from the current parameters; decay in [0, 1), 0 (the
+ * default) uses the parameters themselves. */
+path_status path_cache_set_ema(path_cache *cache, float decay);
 /* radiance [n][3] of n queries (host buffers) */
 path_status path_cache_query(path_cache *cache, const float *queries, uint32_t n, float *out);
 /* one training step on n records (host buffer): with apply_update 0 only the

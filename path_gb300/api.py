@@ -597,6 +597,10 @@ class RadianceCache:
         hi = np.asarray(hi, np.float32)
         capi.check(capi.load().path_cache_set_bounds(self._h, _fptr(lo), _fptr(hi)))
 
+    def set_ema(self, decay):
+        """Inference on a moving average of the parameters (path_cache_set_ema)."""
+        capi.check(capi.load().path_cache_set_ema(self._h, float(decay)))
+
     def use_batch_cells(self):
         """Positions in batch-cell coordinates (path_cache_use_batch_cells)."""
         capi.check(capi.load().path_cache_use_batch_cells(self._h))

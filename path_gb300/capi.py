@@ -138,6 +138,7 @@ SIGNATURES = {
     "path_cache_destroy": (None, [_P]),
     "path_cache_set_bounds": (ctypes.c_int, [_P, _PF, _PF]),
     "path_cache_use_batch_cells": (ctypes.c_int, [_P]),
+    "path_cache_set_ema": (ctypes.c_int, [_P, c_f32]),
     "path_cache_query": (ctypes.c_int, [_P, _PF, c_u32, _PF]),
     "path_cache_train": (ctypes.c_int, [_P, _PF, c_u32, c_u32, _PF]),
     "path_cache_access": (ctypes.c_int, [_P, _PF, _PF, _PF, _PF, c_u32]),

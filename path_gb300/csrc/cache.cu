@@ -682,6 +682,15 @@ __global__ void k_nrc_pack(const float *w, unsigned char *w_fwd, unsigned char *
   *reinterpret_cast<__nv_bfloat16 *>(b + smem_offset(i, o, out_l)) = v;
 }
 
+// avg = decay avg + (1 - decay) param: the exponential moving average of the
+// parameters that inference may use instead of the parameters themselves
+__global__ void k_ema(float *avg, const float *param, size_t n, float decay) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    avg[i] = decay * avg[i] + (1.f - decay) * param[i];
+  }
+}
+
 // Adam (Kingma and Ba 2015) with bias correction; clears the gradient
 __global__ void k_adam(float *param, float *grad, float *m, float *v, size_t n, float lr,
                        float beta1, float beta2, float eps, float step) {
@@ -765,6 +774,14 @@ cudaError_t launch_nrc_grid_backward(const NrcParams &c, const float *records, u
 cudaError_t launch_nrc_pack_weights(const float *w, unsigned char *w_fwd, unsigned char *w_bwd,
                                     cudaStream_t s) {
   dev::k_nrc_pack<<<(kNrcWeights + 255) / 256, 256, 0, s>>>(w, w_fwd, w_bwd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ema(float *avg, const float *param, size_t n, float decay, cudaStream_t s) {
+  if (n == 0) {
+    return cudaSuccess;
+  }
+  dev::k_ema<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(avg, param, n, decay);
   return cudaGetLastError();
 }
 

@@ -128,7 +128,7 @@ Status RadianceCache::infer(const float *queries, uint32_t n, float *out, cudaSt
                             const float *live) {
   PG_TRY_CUDA(cudaMemsetAsync(err_.get(), 0, 4, s), "cache query");
   PG_TRY_CUDA(encoded_.ensure(std::max<size_t>(nrc_encoded_bytes(n), 16)), "cache query");
-  PG_TRY_CUDA(launch_nrc_infer(params(), queries, n, live, out, encoded_.as<unsigned char>(),
+  PG_TRY_CUDA(launch_nrc_infer(infer_params(), queries, n, live, out, encoded_.as<unsigned char>(),
                                err_.as<uint32_t>(), sms_, s),
               "cache query");
   return Status::ok();
@@ -174,8 +174,54 @@ Status RadianceCache::train(const float *records, uint32_t n, float *loss) {
   PG_TRY_CUDA(launch_nrc_pack_weights(w_.as<float>(), wfwd_.as<unsigned char>(),
                                       wbwd_.as<unsigned char>(), stream_),
               "cache pack");
+  if (ema_decay_ > 0.f) {
+    PG_TRY_CUDA(launch_ema(ema_w_.as<float>(), w_.as<float>(), kNrcWeights, ema_decay_, stream_),
+                "cache average");
+    PG_TRY_CUDA(launch_ema(ema_t_.as<float>(), table_.as<float>(),
+                           (size_t)kNrcLevels * kNrcTable * 2, ema_decay_, stream_),
+                "cache average");
+    PG_TRY_CUDA(launch_nrc_pack_weights(ema_w_.as<float>(), ema_fwd_.as<unsigned char>(),
+                                        ema_bwd_.as<unsigned char>(), stream_),
+                "cache average");
+  }
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "cache train");
   return Status::ok();
+}
+
+Status RadianceCache::reset_ema() {
+  const size_t nt = (size_t)kNrcLevels * kNrcTable * 2 * 4;
+  PG_TRY_CUDA(ema_w_.ensure(kNrcWeights * 4), "cache average");
+  PG_TRY_CUDA(ema_t_.ensure(nt), "cache average");
+  PG_TRY_CUDA(ema_fwd_.ensure(kNrcWeightBytes), "cache average");
+  PG_TRY_CUDA(ema_bwd_.ensure(kNrcWeightBytes), "cache average");
+  PG_TRY_CUDA(cudaMemcpyAsync(ema_w_.get(), w_.get(), kNrcWeights * 4, cudaMemcpyDeviceToDevice,
+                              stream_),
+              "cache average");
+  PG_TRY_CUDA(cudaMemcpyAsync(ema_t_.get(), table_.get(), nt, cudaMemcpyDeviceToDevice, stream_),
+              "cache average");
+  PG_TRY_CUDA(launch_nrc_pack_weights(ema_w_.as<float>(), ema_fwd_.as<unsigned char>(),
+                                      ema_bwd_.as<unsigned char>(), stream_),
+              "cache average");
+  PG_TRY_CUDA(cudaStreamSynchronize(stream_), "cache average");
+  return Status::ok();
+}
+
+Status RadianceCache::set_ema(float decay) {
+  if (!(decay >= 0.f && decay < 1.f)) {
+    return Status::err(PATH_ERR_ARGUMENT, "the average's decay must be in [0, 1)");
+  }
+  ema_decay_ = decay;
+  return decay > 0.f ? reset_ema() : Status::ok();
+}
+
+NrcParams RadianceCache::infer_params() const {
+  NrcParams c = params();
+  if (ema_decay_ > 0.f) {
+    c.table = ema_t_.as<const float2>();
+    c.w_fwd = ema_fwd_.as<const unsigned char>();
+    c.w_bwd = ema_bwd_.as<const unsigned char>();
+  }
+  return c;
 }
 
 Status RadianceCache::access(float *weights, float *table, float *grad_w, float *grad_t,
@@ -203,6 +249,10 @@ Status RadianceCache::access(float *weights, float *table, float *grad_w, float 
                 "cache pack");
   }
   PG_TRY_CUDA(cudaStreamSynchronize(stream_), "cache parameters");
+  if (set && ema_decay_ > 0.f) {
+    // new parameters: the average starts again from them
+    return reset_ema();
+  }
   return Status::ok();
 }
 

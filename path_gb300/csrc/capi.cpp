@@ -333,6 +333,13 @@ path_status path_cache_set_bounds(path_cache *cache, const float *lo, const floa
   return PATH_OK;
 }
 
+path_status path_cache_set_ema(path_cache *cache, float decay) {
+  if (!cache) {
+    return fail(PATH_ERR_ARGUMENT, "null argument");
+  }
+  return guarded([&] { return from(cache->c.set_ema(decay)); });
+}
+
 path_status path_cache_use_batch_cells(path_cache *cache) {
   if (!cache) {
     return fail(PATH_ERR_ARGUMENT, "null argument");

@@ -84,6 +84,8 @@ cudaError_t launch_nrc_grid_backward(const NrcParams &c, const float *records, u
                                      const float *d_feat, float2 *grad_table, cudaStream_t s);
 cudaError_t launch_nrc_pack_weights(const float *w, unsigned char *w_fwd, unsigned char *w_bwd,
                                     cudaStream_t s);
+// avg = decay avg + (1 - decay) param over n floats
+cudaError_t launch_ema(float *avg, const float *param, size_t n, float decay, cudaStream_t s);
 cudaError_t launch_adam(float *param, float *grad, float *m, float *v, size_t n, float lr,
                         float beta1, float beta2, float eps, float step, cudaStream_t s);
 size_t nrc_train_scratch_bytes(int grid);

@@ -130,3 +130,31 @@ def test_trained_cache_lowers_the_error_of_a_frame(lib):
     print(f"4-spp frame rel RMSE: plain {e_plain:.4f}, with trained cache {e_cached:.4f}")
     assert np.isfinite(cached).all()
     assert e_cached < e_plain
+
+
+def test_moving_average_of_the_parameters_for_inference(lib):
+    """With the moving average on, queries read avg = d avg + (1 - d) param
+    (starting from the parameters), updated after each Adam step: checked
+    against the NumPy network on the average of the parameters before and
+    after one step."""
+    rng = np.random.default_rng(8)
+    c, w0, t0 = _cache(seed=6)
+    q = _queries(rng, 600)
+    before = c.query(q)
+    c.set_ema(0.75)
+    assert np.array_equal(c.query(q), before)
+    target = rng.uniform(0, 2, (4096, 3)).astype(np.float32)
+    rec = np.concatenate([_queries(rng, 4096), target, np.zeros((4096, 1), np.float32)], 1)
+    c.train(rec)
+    w1, t1 = c.get()
+    d = np.float32(0.75)
+    wa = d * w0 + (np.float32(1) - d) * w1
+    ta = d * t0 + (np.float32(1) - d) * t1
+    want, _, _, _ = ref.forward(q, wa, ta, LO, HI)
+    got = c.query(q)
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    print(f"moving-average inference rel err {err:.2e}")
+    assert err < 1e-2
+    c.set_ema(0.0)
+    live, _, _, _ = ref.forward(q, w1, t1, LO, HI)
+    assert np.linalg.norm(c.query(q) - live) / np.linalg.norm(live) < 1e-2
