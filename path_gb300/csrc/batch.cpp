@@ -377,7 +377,7 @@ Status Renderer::prepare_batch(const std::vector<BatchItem> &items, const SBVHSe
   for (size_t i = 0; i < n; ++i) {
     const size_t f = first_of[i];
     scene_box(flats[f], batch_.box[i].data(), batch_.box[i].data() + 3);
-    batch_.root[i] = node_off[f];
+    batch_.root[i] = wides[f].nodes.empty() ? kEmptyRoot : node_off[f];
     batch_.light_off[i] = light_off[f];
     batch_.n_lights[i] = (uint32_t)flats[f].light_v0.size();
     batch_.n_tris[i] = (uint32_t)flats[f].v0.size();

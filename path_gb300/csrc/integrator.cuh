@@ -273,7 +273,7 @@ __device__ __forceinline__ void wide_begin(const RenderParams &P, WideWalk &w, c
   w.ng_base = root;
   w.ng_bits = 1u | (1u << (8 + w.oct));
   w.sp = 0;
-  w.done = P.n_wide_nodes == 0;
+  w.done = P.n_wide_nodes == 0 || root == kEmptyRoot;
 }
 
 // A shadow ray only asks whether its closest hit lies within 1e-6 of the

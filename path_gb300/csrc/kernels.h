@@ -77,12 +77,15 @@ struct WaveQueues {
   uint32_t pad[3];
 };
 
+// the root of a batch scene without triangles: its rays meet nothing
+constexpr uint32_t kEmptyRoot = 0xffffffffu;
+
 // one scene of a batched render: its camera, samples and place in the
 // concatenated geometry (wide nodes, triangles, materials, lights)
 struct BatchScene {
   float f2w[12];
   uint32_t x_dim, y_dim, spp;
-  uint32_t root;               // wide-node index of the scene's root
+  uint32_t root;               // wide-node index of the scene's root (kEmptyRoot: no triangles)
   uint32_t light_off, n_lights; // its emissive triangles in the light table
   // radiance-cache coordinates of a batch with one cache: a position p of
   // this scene is (p - cache_lo) * cache_inv (its box onto [0, 1]^3) plus

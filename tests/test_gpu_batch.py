@@ -154,3 +154,32 @@ def test_batch_sample_offsets_equal_single_renders(lib):
     api.Renderer().render_batch(batch, s)
     for out, ref in zip(outs, refs):
         assert np.array_equal(bits(out), bits(ref))
+
+
+@pytest.mark.parametrize("gpu_build", [0, 1])
+def test_batch_with_empty_and_light_only_scenes(lib, gpu_build):
+    """Degenerate items in a batch (no triangles; nothing but the light)
+    render as they do alone, with host-built and GPU-built BVHs."""
+    s = scenes.path_settings(5, "wide")
+    s.gpu_build = gpu_build
+    empty = api.Scene()
+    empty.add_material(api.material("Diffuse", diffuse=(0.5, 0.5, 0.5)))
+    light_only = api.Scene()
+    m = light_only.add_material(api.material("Diffuse", diffuse=(0.5, 0.5, 0.5),
+                                             emission=(4, 4, 4)))
+    _, lt = scenes.room_triangles()
+    light_only.add_mesh(np.stack(lt).reshape(-1, 9), np.full(2, m, np.uint32))
+    items = [(empty, 16, 16, 4), (scenes.cornell_box(), 24, 16, 4), (light_only, 16, 24, 8)]
+    batch, outs, refs = [], [], []
+    for sc, w, h, spp in items:
+        f2w = scenes.cornell_camera(w, h)
+        out = np.zeros((h, w, 3), np.float32)
+        outs.append(out)
+        refs.append(_single(sc, s, spp, w, h, f2w))
+        batch.append((sc, api.SquareImage(w, h, f2w), out, spp))
+    r = api.Renderer()
+    r.render_batch(batch, s)
+    assert r.stats()["device_status"] == 0
+    assert not outs[0].any()
+    for out, ref in zip(outs, refs):
+        assert np.array_equal(bits(out), bits(ref))
