@@ -35,10 +35,11 @@ def _cache(seed=3):
     return c, w, t
 
 
-def test_inference_matches_numpy(lib):
+@pytest.mark.parametrize("n", [1, 129, 1000])
+def test_inference_matches_numpy(lib, n):
     rng = np.random.default_rng(1)
     c, w, t = _cache()
-    q = _queries(rng, 1000)
+    q = _queries(rng, n)
     got = c.query(q)
     want, _, _, _ = ref.forward(q, w, t, LO, HI)
     err = np.linalg.norm(got - want) / np.linalg.norm(want)
