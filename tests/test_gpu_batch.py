@@ -156,7 +156,7 @@ def test_batch_sample_offsets_equal_single_renders(lib):
         assert np.array_equal(bits(out), bits(ref))
 
 
-@pytest.mark.parametrize("gpu_build", [0, 1])
+@pytest.mark.parametrize("gpu_build", [0, 1, 2])
 def test_batch_with_empty_and_light_only_scenes(lib, gpu_build):
     """Degenerate items in a batch (no triangles; nothing but the light)
     render as they do alone, with host-built and GPU-built BVHs."""

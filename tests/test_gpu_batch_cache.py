@@ -172,3 +172,32 @@ def _run_with(r, cache, raw, s, train_paths, train_steps):
     r.render_batch_cached(cache, batch, s, cache_depth=2, train_paths=train_paths,
                           train_steps=train_steps)
     return outs
+
+
+def test_batch_cached_with_an_empty_scene_and_bgra_output(lib):
+    """An item without triangles and an item written as BGRA in a cached
+    batch: the empty item stays black, the BGRA item equals the same item's
+    FloatRGB image tone-mapped by the plain batch's BGRA path."""
+    s = scenes.path_settings(6, "wide")
+    empty = api.Scene()
+    empty.add_material(api.material("Diffuse", diffuse=(0.5, 0.5, 0.5)))
+    sc = scenes.cornell_box()
+    c, _, _ = _random_table_cache(12)
+    w = h = 16
+    f2w = scenes.cornell_camera(w, h)
+    e_out = np.zeros((h, w, 3), np.float32)
+    rgb = np.zeros((h, w, 3), np.float32)
+    bgra = np.zeros((h, w, 4), np.uint8)
+    r = api.Renderer()
+    r.render_batch_cached(c, [(empty, api.SquareImage(w, h, f2w), e_out, 4),
+                              (sc, api.SquareImage(w, h, f2w), rgb, 4)], s,
+                          cache_depth=2, train_paths=0, train_steps=0)
+    assert r.stats()["device_status"] == 0
+    assert not e_out.any()
+    e2 = np.zeros((h, w, 3), np.float32)
+    r.render_batch_cached(c, [(empty, api.SquareImage(w, h, f2w), e2, 4),
+                              (sc, api.SquareImage(w, h, f2w), bgra, 4)], s,
+                          cache_depth=2, train_paths=0, train_steps=0)
+    v = np.maximum(rgb.astype(np.float32), 0)
+    want = np.clip((v / (v + 1)) * 255, 0, 255).astype(np.uint8)
+    assert np.abs(bgra[..., 2::-1].astype(int) - want.astype(int)).max() <= 1
