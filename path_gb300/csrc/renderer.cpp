@@ -763,6 +763,11 @@ Status Renderer::render(const path_sample_spec &spec, const path_output &output,
   p.row_lo = row_lo;
   p.sample_offset = spec.sample_offset;
   p.cache_depth = cache_ != nullptr ? cache_depth_ : 0u;
+  if (cache_ != nullptr) {
+    // the frame's queries are evaluated over this scene's box (also after
+    // the cache served a batch in its cell coordinates)
+    cache_->set_bounds(prep_.lo, prep_.hi);
+  }
   p.rng_uniform = st.rng == PATH_RNG_UNIFORM ? 1u : 0u;
   p.row_hi = row_hi;
   // the streaming trace kernel's shared-memory copy of the BVH's top (host
@@ -1292,8 +1297,6 @@ Status Renderer::render_cached(const path_sample_spec &spec, const path_output &
     return sr;
   }
   const double render_ms = stats_.kernel_ms;
-  // the cache covers the scene's box
-  cache.set_bounds(prep_.lo, prep_.hi);
   if (train_paths > 0 && train_steps > 0) {
     const uint32_t per = std::max<uint32_t>(train_paths / train_steps, 1);
     for (uint32_t k = 0; k < train_steps; ++k) {

@@ -201,3 +201,26 @@ def test_batch_cached_with_an_empty_scene_and_bgra_output(lib):
     v = np.maximum(rgb.astype(np.float32), 0)
     want = np.clip((v / (v + 1)) * 255, 0, 255).astype(np.uint8)
     assert np.abs(bgra[..., 2::-1].astype(int) - want.astype(int)).max() <= 1
+
+
+def test_single_cached_frame_after_a_batch_uses_the_scene_box(lib):
+    """One cache used for a batch (cell coordinates) and then for a single
+    scene renders that scene's cached frame exactly as a cache that never
+    served a batch (the scene's box is set before the frame's queries)."""
+    s = scenes.path_settings(6, "wide")
+    s.kernel_approach = 1
+    sc = scenes.cornell_box()
+    w = h = 16
+    f2w = scenes.cornell_camera(w, h)
+    a, _, _ = _random_table_cache(21)
+    b, _, _ = _random_table_cache(21)
+    junk = np.zeros((h, w, 3), np.float32)
+    api.Renderer().render_batch_cached(a, [(sc, api.SquareImage(w, h, f2w), junk, 4)], s,
+                                       cache_depth=2, train_paths=0, train_steps=0)
+    ia = np.zeros((h, w, 3), np.float32)
+    ib = np.zeros((h, w, 3), np.float32)
+    api.Renderer().render_cached(a, api.SquareImage(w, h, f2w), ia, sc, 4, s, cache_depth=2,
+                                 train_paths=0, train_steps=0)
+    api.Renderer().render_cached(b, api.SquareImage(w, h, f2w), ib, sc, 4, s, cache_depth=2,
+                                 train_paths=0, train_steps=0)
+    assert np.array_equal(bits(ia), bits(ib))
