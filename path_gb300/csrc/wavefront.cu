@@ -567,13 +567,22 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
     if (live) {
       out[pos] = slot;
     }
-    const uint32_t pn = warp_append(&W.q->rays, want_next, lane);
-    if (want_next) {
-      W.rays[pn] = slot << 1;
-    }
-    const uint32_t pl = warp_append(&W.q->rays, want_light, lane);
-    if (want_light) {
-      W.rays[pl] = (slot << 1) | 1u;
+    // the warp's extension rays, then its light rays, with one atomic
+    {
+      const uint32_t mn = __ballot_sync(kFull, want_next);
+      const uint32_t ml = __ballot_sync(kFull, want_light);
+      const uint32_t below = (1u << lane) - 1u;
+      uint32_t rb = 0;
+      if (lane == 0 && (mn | ml) != 0) {
+        rb = atomicAdd(&W.q->rays, (uint32_t)(__popc(mn) + __popc(ml)));
+      }
+      rb = __shfl_sync(kFull, rb, 0);
+      if (want_next) {
+        W.rays[rb + __popc(mn & below)] = slot << 1;
+      }
+      if (want_light) {
+        W.rays[rb + __popc(mn) + __popc(ml & below)] = (slot << 1) | 1u;
+      }
     }
     if (next_base >= count) {
       break;
