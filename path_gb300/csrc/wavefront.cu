@@ -242,10 +242,13 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
   W.rays[i] = i << 1;
 }
 
+constexpr uint32_t kRayChunk = 64; // queue entries a warp reserves at a time
+
 // Persistent trace: each lane walks one ray through the wide BVH one node
 // (and the triangles of its leaf slots) per step; when a quarter of a warp's
-// lanes are idle they take new queue entries together (one atomic per
-// warp), so lanes rarely wait on the longest ray of a batch.
+// lanes are idle they take new queue entries together from the warp's
+// reserved run of entries (one atomic per kRayChunk entries), so lanes
+// rarely wait on the longest ray of a batch.
 // kStaged: the CTA first copies the BVH's top nodes (W.P.n_staged of them,
 // breadth first from the root) into shared memory, where every lane reads
 // them from then on.
@@ -271,17 +274,32 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
   uint32_t entry = 0;
   uint32_t st_base[kWideStack];
   uint32_t st_bits[kWideStack];
+  // the warp's reserved run of queue entries [next_i, chunk_end): taken
+  // kRayChunk at a time with one atomic (every warp adds to the same
+  // cursor), handed out to idle lanes in order
+  uint32_t next_i = 0, chunk_end = 0;
   while (true) {
     const uint32_t idle = __ballot_sync(kFull, !have);
     if (!drained && __popc(idle) >= 8) {
-      uint32_t base = 0;
-      if (lane == 0) {
-        base = atomicAdd(&W.q->ray_cursor, (uint32_t)__popc(idle));
+      const uint32_t need = (uint32_t)__popc(idle);
+      const uint32_t avail = chunk_end - next_i;
+      uint32_t nb = 0;
+      if (need > avail) {
+        if (lane == 0) {
+          nb = atomicAdd(&W.q->ray_cursor, kRayChunk);
+        }
+        nb = __shfl_sync(kFull, nb, 0);
       }
-      base = __shfl_sync(kFull, base, 0);
-      drained = base + (uint32_t)__popc(idle) >= count;
+      const uint32_t rank = (uint32_t)__popc(idle & ((1u << lane) - 1u));
+      const uint32_t i = rank < avail ? next_i + rank : nb + (rank - avail);
+      if (need > avail) {
+        next_i = nb + (need - avail);
+        chunk_end = nb + kRayChunk;
+      } else {
+        next_i += need;
+      }
+      drained = next_i >= count;
       if (!have) {
-        const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
         if (i < count) {
           entry = W.rays[i];
           const uint32_t slot = entry >> 1;
