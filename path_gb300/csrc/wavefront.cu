@@ -243,12 +243,13 @@ __global__ void k_wf_init(const WaveParams W, uint32_t n0) {
 }
 
 constexpr uint32_t kRayChunk = 64; // queue entries a warp reserves at a time
+constexpr int kRefillIdle = 4;     // idle lanes that make a warp take new rays
 
 // Persistent trace: each lane walks one ray through the wide BVH one node
-// (and the triangles of its leaf slots) per step; when a quarter of a warp's
-// lanes are idle they take new queue entries together from the warp's
-// reserved run of entries (one atomic per kRayChunk entries), so lanes
-// rarely wait on the longest ray of a batch.
+// (and the triangles of its leaf slots) per step; when kRefillIdle of a
+// warp's lanes are idle they take new queue entries together from the
+// warp's reserved run of entries (one atomic per kRayChunk entries), so
+// lanes rarely wait on the longest ray of a batch.
 // kStaged: the CTA first copies the BVH's top nodes (W.P.n_staged of them,
 // breadth first from the root) into shared memory, where every lane reads
 // them from then on.
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_wf_trace(const WaveParams W
   uint32_t next_i = 0, chunk_end = 0;
   while (true) {
     const uint32_t idle = __ballot_sync(kFull, !have);
-    if (!drained && __popc(idle) >= 8) {
+    if (!drained && __popc(idle) >= kRefillIdle) {
       const uint32_t need = (uint32_t)__popc(idle);
       const uint32_t avail = chunk_end - next_i;
       uint32_t nb = 0;
