@@ -217,7 +217,10 @@ typedef struct {
   uint64_t nodes_visited;
   uint64_t triangles_tested;
   uint32_t gpu_launches;     /* kernels this library launched for the render */
-  uint32_t device_status;    /* 0, or the first in-kernel error code */
+  uint32_t device_status;    /* 0, or the first in-kernel error code: 1 traversal
+                                stack overflow, 2 object list overflow, 3 bad
+                                node, 4 path beyond 4096 vertices, 5 an extension
+                                ray in a light-only last pass */
   uint32_t num_bvh_nodes;
   uint32_t num_wide_nodes;
   uint64_t h2d_bytes;        /* host -> device bytes copied by this render */

@@ -95,6 +95,7 @@ enum DeviceStatus : uint32_t {
   kStatusObjectsOverflow = 2,
   kStatusBadNode = 3,
   kStatusPathTooLong = 4,
+  kStatusPassCount = 5, // a light-only pass met a path with an extension ray
 };
 
 // Safety bound on the vertices of one path.  The reference loops until the

@@ -142,7 +142,14 @@ struct WaveParams {
   // scenes' materials and the fixed setting choices), for the choice of a
   // specialised shade kernel
   uint32_t feat;
+  // what the host knows of the pass's live slots (kPass*)
+  uint32_t pass;
 };
+
+// kPassFresh: every live slot is fresh (the first pass after k_wf_init);
+// kPassLightOnly: no live slot has an extension ray pending, only the light
+// ray of its last vertex (k_wf_finish shades the pass)
+constexpr uint32_t kPassGeneral = 0, kPassFresh = 1, kPassLightOnly = 2;
 
 // the features (kFeat*) of rendering a scene whose materials have the BSDF
 // types mat_types (bit per type) with the settings in p

@@ -1025,6 +1025,13 @@ Status Renderer::run_wavefront(const RenderParams &p, uint32_t n_blocks, bool co
         PG_TRY_CUDA(cudaEventRecord(trace_event(2 * trace_timed_ + 1), stream_), "event");
         ++trace_timed_;
       }
+      // what the host knows of the pass's live slots: all fresh in the
+      // first pass; none with an extension ray in the pass after the
+      // (N + 1)-th vertex when every sample has been in flight from the start
+      w.pass = round == 0 && k == 0 ? kPassFresh
+               : round == 0 && p.term_prob == 1 && n_slots == total && k == p.term_iters + 1
+                   ? kPassLightOnly
+                   : kPassGeneral;
       PG_TRY_CUDA(launch_wavefront_shade(w, parity, shade_grid, stream_, grad),
                   "wavefront shade");
       *launches += 3;

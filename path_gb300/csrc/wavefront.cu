@@ -73,7 +73,11 @@ __device__ __forceinline__ uint32_t scene_of(const WaveParams &W, unsigned long 
 // (id low word, id bits 32-39 | scene << 8, RNG dimension, iters | flags << 24).
 // A fresh path (iters 0: no vertex shaded yet) stores only o, d and the
 // state word: its light direction, multipliers and radiance are the start
-// values (path_begin_cam), which unpack_path restores.
+// values (path_begin_cam), which unpack_path restores.  Otherwise a word is
+// stored only when something reads it: ld (traced) and the light multiplier
+// (added on a visible light hit) only with a pending light ray, the path
+// multiplier only with a pending extension ray (path_step reads it only
+// after an extension hit, and sets both multipliers afresh each vertex).
 template <class S>
 __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
                                            const S &s, unsigned long long id,
@@ -81,9 +85,13 @@ __device__ __forceinline__ void store_path(const WaveParams &W, uint32_t slot,
   W.o[slot] = make_float4(s.o.x, s.o.y, s.o.z, s.light_target);
   W.d[slot] = make_float4(s.d.x, s.d.y, s.d.z, __uint_as_float(root));
   if (!fresh) {
-    W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, __uint_as_float(root));
-    W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
-    W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
+    if (s.has_light) {
+      W.ld[slot] = make_float4(s.ld.x, s.ld.y, s.ld.z, __uint_as_float(root));
+      W.lmult[slot] = make_float4(s.light_mult.r, s.light_mult.g, s.light_mult.b, 0.f);
+    }
+    if (s.has_next) {
+      W.mult[slot] = make_float4(s.multiplier.r, s.multiplier.g, s.multiplier.b, 0.f);
+    }
     W.total[slot] = make_float4(s.total.r, s.total.g, s.total.b, 0.f);
   }
   uint32_t flags = (s.has_next ? kFlagNext : 0u) | (s.has_light ? kFlagLight : 0u) |
@@ -106,9 +114,11 @@ __device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t s
 
 // A lane's slot state (and both hits) copied into shared memory by
 // asynchronous copies: the shade kernel stages a warp's next batch of slots
-// while it shades the current one.
+// while it shades the current one.  The light direction is not staged: a
+// vertex's step sets it afresh when it samples a light, and it is read
+// only by the trace.
 struct SlotStage {
-  float4 o, d, ld, mult, lmult, total;
+  float4 o, d, mult, lmult, total;
   uint4 state;
   uint2 hit_light, hit_ext;
 };
@@ -135,24 +145,28 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
-__device__ __forceinline__ void stage_slot(const WaveParams &W, uint32_t slot, SlotStage &g) {
+// fresh: every slot of the pass is fresh (the first pass after k_wf_init),
+// so only o, d, the state word and the extension hit are staged
+__device__ __forceinline__ void stage_slot(const WaveParams &W, uint32_t slot, SlotStage &g,
+                                           bool fresh) {
   cp_async16(&g.o, W.o + slot);
   cp_async16(&g.d, W.d + slot);
-  cp_async16(&g.ld, W.ld + slot);
-  cp_async16(&g.mult, W.mult + slot);
-  cp_async16(&g.lmult, W.lmult + slot);
-  cp_async16(&g.total, W.total + slot);
   cp_async16(&g.state, W.state + slot);
-  cp_async8(&g.hit_light, W.hit_light + slot);
   cp_async8(&g.hit_ext, W.hit_ext + slot);
+  if (!fresh) {
+    cp_async16(&g.mult, W.mult + slot);
+    cp_async16(&g.lmult, W.lmult + slot);
+    cp_async16(&g.total, W.total + slot);
+    cp_async8(&g.hit_light, W.hit_light + slot);
+  }
 }
 
-// a slot's path state from its seven words (global or staged)
+// a slot's path state from its staged words
 template <bool kUniform>
 __device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, uint32_t slot,
-                                                          float4 o, float4 d, float4 ld,
-                                                          float4 m, float4 lm, float4 t,
-                                                          uint4 st, PathStateT<kUniform> &s,
+                                                          float4 o, float4 d, float4 m,
+                                                          float4 lm, float4 t, uint4 st,
+                                                          PathStateT<kUniform> &s,
                                                           uint32_t &scene, uint32_t &root) {
   const RenderParams &P = W.P;
   unsigned long long id = (unsigned long long)st.x | ((unsigned long long)(st.y & 0xffu) << 32);
@@ -161,7 +175,7 @@ __device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, u
   s.o = mk(o.x, o.y, o.z);
   s.light_target = o.w;
   s.d = mk(d.x, d.y, d.z);
-  s.ld = mk(ld.x, ld.y, ld.z);
+  s.ld = mk(0.f, 0.f, 0.f);
   s.multiplier = mkrgb(m.x, m.y, m.z);
   s.light_mult = mkrgb(lm.x, lm.y, lm.z);
   s.total = mkrgb(t.x, t.y, t.z);
@@ -172,7 +186,6 @@ __device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, u
   s.count_emission = (flags & kFlagEmission) != 0;
   if (s.iters == 0) {
     // a fresh path: only o, d and this word were stored
-    s.ld = mk(0.f, 0.f, 0.f);
     s.multiplier = mkrgb(1.f, 1.f, 1.f);
     s.light_mult = zero_rgb();
     s.total = zero_rgb();
@@ -193,14 +206,6 @@ __device__ __forceinline__ unsigned long long unpack_path(const WaveParams &W, u
     s.rng.dim = st.z;
   }
   return id;
-}
-
-template <bool kUniform>
-__device__ __forceinline__ unsigned long long load_path(const WaveParams &W, uint32_t slot,
-                                                        PathStateT<kUniform> &s,
-                                                        uint32_t &scene, uint32_t &root) {
-  return unpack_path(W, slot, W.o[slot], W.d[slot], W.ld[slot], W.mult[slot], W.lmult[slot],
-                     W.total[slot], W.state[slot], s, scene, root);
 }
 
 template <bool kUniform>
@@ -430,7 +435,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
   bool valid = base + lane < count;
   uint32_t slot = valid ? in[base + lane] : 0u;
   if (valid) {
-    stage_slot(W, slot, g);
+    stage_slot(W, slot, g, W.pass == kPassFresh);
   }
   cp_async_commit();
   while (true) {
@@ -446,8 +451,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
     if (valid) {
       PathStateT<kUniform> s;
       uint32_t scene, root;
-      unsigned long long id = unpack_path(W, slot, g.o, g.d, g.ld, g.mult, g.lmult, g.total,
-                                          g.state, s, scene, root);
+      unsigned long long id = unpack_path(W, slot, g.o, g.d, g.mult, g.lmult, g.total, g.state,
+                                          s, scene, root);
       Hit lh = s.has_light ? unpack_hit(g.hit_light) : no_hit();
       Hit nh = s.has_next ? unpack_hit(g.hit_ext) : no_hit();
       if (!kGrad) {
@@ -607,11 +612,52 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
       break;
     }
     if (next_valid) {
-      stage_slot(W, next_slot, g);
+      stage_slot(W, next_slot, g, W.pass == kPassFresh);
     }
     cp_async_commit();
     slot = next_slot;
     valid = next_valid;
+  }
+}
+
+// The shade pass when no live path has an extension ray left, only the
+// light ray of its last vertex: under NIters{N} with every sample in flight
+// from the first pass, the pass after the (N + 1)-th shaded vertex.  Each
+// live slot adds its light ray's emission when the ray reached the light
+// point (the first lines of path_step, the same arithmetic) and writes its
+// sample's radiance: four words of slot state read instead of the shade
+// kernel's staged seven, and none of its code.  A slot with an extension
+// ray pending means the host counted the passes wrong: the slot sets
+// kStatusPassCount rather than dropping its path without a word.
+__global__ void __launch_bounds__(256) k_wf_finish(const WaveParams W, uint32_t parity) {
+  const RenderParams &P = W.P;
+  const uint32_t count = W.q->active[parity];
+  const uint32_t *in = W.active[parity];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += gridDim.x * blockDim.x) {
+    const uint32_t slot = in[i];
+    const uint4 st = W.state[slot];
+    const uint32_t flags = st.w >> 24;
+    if ((flags & kFlagNext) != 0) {
+      set_status(P.status, kStatusPassCount);
+      continue;
+    }
+    const unsigned long long id =
+        (unsigned long long)st.x | ((unsigned long long)(st.y & 0xffu) << 32);
+    const float4 t4 = W.total[slot];
+    rgb total = mkrgb(t4.x, t4.y, t4.z);
+    if ((flags & kFlagLight) != 0) {
+      const Hit lh = unpack_hit(W.hit_light[slot]);
+      if (lh.ok && pm::fabs(W.o[slot].w - lh.t) <= 1e-6f && (P.back_cull == 0 || !lh.back)) {
+        const float4 lm = W.lmult[slot];
+        const float4 c = __ldg(P.tri_data + 3 * lh.idx + 2);
+        total = total + emission_of(P.materials + __float_as_uint(c.w)) * mkrgb(lm.x, lm.y, lm.z);
+      }
+    }
+    float *dst = W.sample_rgb + 3 * (id - W.first_sample);
+    dst[0] = total.r;
+    dst[1] = total.g;
+    dst[2] = total.b;
   }
 }
 
@@ -712,6 +758,10 @@ cudaError_t launch_wavefront_trace(const WaveParams &w, uint32_t trace_grid,
 cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_t shade_grid,
                                    cudaStream_t s, bool grad) {
   dev::k_wf_prep<<<1, 1, 0, s>>>(w, parity);
+  if (w.pass == kPassLightOnly && !grad) {
+    dev::k_wf_finish<<<shade_grid, 256, 0, s>>>(w, parity);
+    return cudaGetLastError();
+  }
   const bool u = w.P.rng_uniform != 0;
   const bool cache = w.cache_q != nullptr;
   if (grad) {
