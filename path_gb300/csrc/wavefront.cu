@@ -410,9 +410,13 @@ __device__ __forceinline__ void warp_grad(double *out, uint32_t mat, const float
 // which measured faster than fewer warps without register spills.  kCache
 // (paths end into the radiance cache) is a template parameter so that the
 // plain kernel carries none of the cache-query code.
-// Each warp takes batches of 32 live slots; the state of its next batch is
-// copied into shared memory (cp.async) while it shades the current one, so
-// the slot loads of a batch overlap the previous batch's work.
+// Each warp takes batches of 32 live slots.  Once it has shaded a batch it
+// takes the next one and copies each slot's state into shared memory
+// (cp.async: all of a lane's words in flight at once, held in no register
+// and read where the step uses them); other warps shade while the copies
+// land.  The next batch's slot indices are taken only then, so that no
+// register holds them through the step (fewer spills under the 64-register
+// bound than taking them first).
 template <bool kGrad, bool kUniform, bool kCache, uint32_t kFeat = kFeatAll>
 __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_t parity) {
   __shared__ SlotStage s_stage[256];
@@ -439,10 +443,6 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
   }
   cp_async_commit();
   while (true) {
-    // the next batch's slots, read now and staged after this batch
-    const uint32_t next_base = take();
-    const bool next_valid = next_base + lane < count;
-    const uint32_t next_slot = next_valid ? in[next_base + lane] : 0u;
     cp_async_wait_all();
     bool live = false, finished = false, want_next = false, want_light = false;
     uint32_t gm_vertex = kNoMaterial, gm_light = kNoMaterial, gm_emit = kNoMaterial;
@@ -608,9 +608,13 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
         W.rays[rb + __popc(mn) + __popc(ml & below)] = (slot << 1) | 1u;
       }
     }
+    // the next batch's slots, staged before it is shaded
+    const uint32_t next_base = take();
     if (next_base >= count) {
       break;
     }
+    const bool next_valid = next_base + lane < count;
+    const uint32_t next_slot = next_valid ? in[next_base + lane] : 0u;
     if (next_valid) {
       stage_slot(W, next_slot, g, W.pass == kPassFresh);
     }

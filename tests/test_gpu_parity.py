@@ -308,6 +308,23 @@ def test_streaming_refill_equals_megakernel(lib, slots_log2):
     assert np.array_equal(bits(mega), bits(wave))
 
 
+@pytest.mark.parametrize("depth", [1, 2, 3, 63, 64])
+def test_streaming_pass_kinds_equal_megakernel(lib, depth):
+    """Every sample in flight under NIters{depth - 1}: the first pass stages
+    fresh slots only, and the pass after the last vertex is the light-only
+    finishing pass when it falls in the first round of passes (depth + 1 <=
+    64; at depth 64 it falls in the second round and the shade kernel runs
+    it).  The image is the megakernel's bit for bit, and no light-only pass
+    meets a path with an extension ray (device status 0)."""
+    sc = scenes.cornell_box()
+    s = scenes.path_settings(depth, "wide")
+    f2w = scenes.cornell_camera(32, 32)
+    mega = _render_gpu(sc, s, 4, 32, 32, f2w)
+    s.kernel_approach = 1
+    wave = _render_gpu(sc, s, 4, 32, 32, f2w)
+    assert np.array_equal(bits(mega), bits(wave))
+
+
 def _camera_rays(rng, n, f2w):
     """Rays through random film points of the Cornell camera."""
     m = np.asarray(f2w, np.float64).reshape(3, 4)
