@@ -500,7 +500,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
         const rgb g = mkrgb(gp[0] * inv_spp, gp[1] * inv_spp, gp[2] * inv_spp);
         const rgb beta = s.multiplier, lmult = s.light_mult;
         StepTrace tr;
-        bool cont = path_continues(P, s, path_step(P, scene_lights(W, scene), s, lh, nh, &tr));
+        bool cont = path_continues(
+            P, s, path_step<kUniform, kFeat>(P, scene_lights(W, scene), s, lh, nh, &tr));
         const uint32_t pm = W.pend_mat[slot];
         rgb nee_add = zero_rgb(), emit_add = zero_rgb();
         if (tr.light_added) {
@@ -785,12 +786,16 @@ cudaError_t launch_wavefront_shade(const WaveParams &w, uint32_t parity, uint32_
   if (grad) {
     if (u) {
       dev::k_wf_shade<true, true, false><<<shade_grid, 256, 0, s>>>(w, parity);
+    } else if (feat_covers(kFeatPlain, w.feat)) {
+      dev::k_wf_shade<true, false, false, kFeatPlain><<<shade_grid, 256, 0, s>>>(w, parity);
     } else {
       dev::k_wf_shade<true, false, false><<<shade_grid, 256, 0, s>>>(w, parity);
     }
   } else if (cache) {
     if (u) {
       dev::k_wf_shade<false, true, true><<<shade_grid, 256, 0, s>>>(w, parity);
+    } else if (feat_covers(kFeatPlain, w.feat)) {
+      dev::k_wf_shade<false, false, true, kFeatPlain><<<shade_grid, 256, 0, s>>>(w, parity);
     } else {
       dev::k_wf_shade<false, false, true><<<shade_grid, 256, 0, s>>>(w, parity);
     }
