@@ -173,6 +173,24 @@ __device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
   return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
 }
 
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
+      "sub.rn.f32x2 %0, ra, rb;\n\t}"
+      : "=l"(d)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
+}
+
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+  unsigned long long d;
+  asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
+      "mul.rn.f32x2 %0, ra, rb;\n\t}"
+      : "=l"(d)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return make_float2(__uint_as_float((uint32_t)d), __uint_as_float((uint32_t)(d >> 32)));
+}
+
 __device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
   unsigned long long d;
   asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%1, %2};\n\tmov.b64 rb, {%3, %4};\n\t"
@@ -336,11 +354,15 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
   }
   const f3 inv = w.inv;
   // per axis: t per quantum, offset of the node origin, rounding margin
-  const float ax = exp2_byte(n0.w & 0xffu) * inv.x;
-  const float ay = exp2_byte((n0.w >> 8) & 0xffu) * inv.y;
+  // (x and y as two-lane pairs: the same roundings as the scalar forms)
+  const float2 inv_xy = make_float2(inv.x, inv.y);
+  const float2 axy =
+      mul2_rn(make_float2(exp2_byte(n0.w & 0xffu), exp2_byte((n0.w >> 8) & 0xffu)), inv_xy);
+  const float2 bxy = mul2_rn(sub2_rn(make_float2(__uint_as_float(n0.x), __uint_as_float(n0.y)),
+                                     make_float2(w.r.o.x, w.r.o.y)),
+                             inv_xy);
+  const float ax = axy.x, ay = axy.y, bx = bxy.x, by = bxy.y;
   const float az = exp2_byte((n0.w >> 16) & 0xffu) * inv.z;
-  const float bx = (__uint_as_float(n0.x) - w.r.o.x) * inv.x;
-  const float by = (__uint_as_float(n0.y) - w.r.o.y) * inv.y;
   const float bz = (__uint_as_float(n0.z) - w.r.o.z) * inv.z;
   // 2^-20 (255 |a| + |b|), plus 2^-8 |a| + 2^-23 |b| for the rounding of
   // C = b - 2^15 a (at most 2^-9 |a| + 2^-24 |b|)
@@ -360,12 +382,12 @@ __device__ __forceinline__ void wide_node(const RenderParams &P, WideWalk &w,
   const uint32_t nzl = sz ? n4.z : n3.x, nzh = sz ? n4.w : n3.y;
   const uint32_t fzl = sz ? n3.x : n4.z, fzh = sz ? n3.y : n4.w;
   const float tcull = w.best.t;
-  const float Ax = __fmul_rn(ax, 32768.f), Ay = __fmul_rn(ay, 32768.f),
-              Az = __fmul_rn(az, 32768.f);
+  const float2 Axy = mul2_rn(axy, make_float2(32768.f, 32768.f));
+  const float Ax = Axy.x, Ay = Axy.y, Az = __fmul_rn(az, 32768.f);
   const float2 aax = make_float2(Ax, Ax), aay = make_float2(Ay, Ay), aaz = make_float2(Az, Az);
-  const float2 ccx = add2_rn(make_float2(bnx, bfx), make_float2(-Ax, -Ax));
-  const float2 ccy = add2_rn(make_float2(bny, bfy), make_float2(-Ay, -Ay));
-  const float2 ccz = add2_rn(make_float2(bnz, bfz), make_float2(-Az, -Az));
+  const float2 ccx = sub2_rn(make_float2(bnx, bfx), aax);
+  const float2 ccy = sub2_rn(make_float2(bny, bfy), aay);
+  const float2 ccz = sub2_rn(make_float2(bnz, bfz), aaz);
   // slot i's box test, a miss as the sign of tmax - tmin, tcull - tmin or
   // tmax (tmin <= tmax && tmin <= tcull && tmax >= 0; tcull >= 0; a box
   // holding a hit at t > 1e-5 has tmax > 0), shifted in from slot 7 down so
