@@ -114,7 +114,7 @@ __device__ __forceinline__ LightSet scene_lights(const WaveParams &W, uint32_t s
 
 // A lane's slot state (and both hits) copied into shared memory by
 // asynchronous copies: the shade kernel stages a warp's next batch of slots
-// while it shades the current one.  The light direction is not staged: a
+// once it has shaded the current one.  The light direction is not staged: a
 // vertex's step sets it afresh when it samples a light, and it is read
 // only by the trace.
 struct SlotStage {
