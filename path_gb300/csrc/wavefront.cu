@@ -460,6 +460,15 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
         StepTrace *trp = kCache ? &tr : nullptr;
         bool cont = path_continues(
             W.P, s, path_step<kUniform, kFeat>(W.P, scene_lights(W, scene), s, lh, nh, trp));
+        if constexpr (!kCache) {
+          // the sample id, scene and root read again from the staged words
+          // (volatile: no register holds them through the step)
+          const volatile uint32_t *vs = reinterpret_cast<const volatile uint32_t *>(&g.state);
+          const uint32_t sx = vs[0], sy = vs[1];
+          id = (unsigned long long)sx | ((unsigned long long)(sy & 0xffu) << 32);
+          scene = sy >> 8;
+          root = reinterpret_cast<const volatile uint32_t *>(&g.d)[3];
+        }
         if (trp != nullptr && tr.cache_query) {
           // the path ends into the radiance cache: its query and throughput
           const size_t k = (size_t)(id - W.first_sample);
