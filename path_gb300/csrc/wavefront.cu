@@ -501,16 +501,36 @@ __global__ void __launch_bounds__(256, 4) k_wf_shade(const WaveParams W, uint32_
         }
       } else {
         const RenderParams &P = W.P;
+        StepTrace tr;
+        bool cont = path_continues(
+            P, s, path_step<kUniform, kFeat>(P, scene_lights(W, scene), s, lh, nh, &tr));
+        // as in the plain branch: id, scene and root, and the vertex's
+        // multipliers before the step, from the staged words
+        rgb beta, lmult;
+        {
+          const SlotStage &st = s_stage[threadIdx.x];
+          const volatile uint32_t *vs = reinterpret_cast<const volatile uint32_t *>(&st.state);
+          const uint32_t sx = vs[0], sy = vs[1], sw = vs[3];
+          id = (unsigned long long)sx | ((unsigned long long)(sy & 0xffu) << 32);
+          scene = sy >> 8;
+          root = reinterpret_cast<const volatile uint32_t *>(&st.d)[3];
+          const volatile float *vm = reinterpret_cast<const volatile float *>(&st.mult);
+          const volatile float *vl = reinterpret_cast<const volatile float *>(&st.lmult);
+          if ((sw & 0xffffffu) == 0) {
+            // a fresh path: the start values unpack_path gave it
+            beta = mkrgb(1.f, 1.f, 1.f);
+            lmult = zero_rgb();
+          } else {
+            beta = mkrgb(vm[0], vm[1], vm[2]);
+            lmult = mkrgb(vl[0], vl[1], vl[2]);
+          }
+        }
         const float *lf = W.sample_rgb + 3 * (id - W.first_sample);
         const rgb l_sample = mkrgb(lf[0], lf[1], lf[2]);
         const unsigned long long pixel = id / P.spp;
         const float *gp = W.d_image + 3 * pixel;
         const float inv_spp = 1.f / (float)P.spp;
         const rgb g = mkrgb(gp[0] * inv_spp, gp[1] * inv_spp, gp[2] * inv_spp);
-        const rgb beta = s.multiplier, lmult = s.light_mult;
-        StepTrace tr;
-        bool cont = path_continues(
-            P, s, path_step<kUniform, kFeat>(P, scene_lights(W, scene), s, lh, nh, &tr));
         const uint32_t pm = W.pend_mat[slot];
         rgb nee_add = zero_rgb(), emit_add = zero_rgb();
         if (tr.light_added) {
